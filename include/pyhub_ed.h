@@ -1,0 +1,121 @@
+/*
+ * pyhub_ed.h -- C ABI of the GB300 exact-diagonalisation engine.
+ *
+ * The reference (PyHub) has no in-process native interface: its Python layer
+ * writes HDF5 files and runs Fortran executables with os.system
+ * (pyhub/core/core_solver.py:107-111), and pyhub/libs/__init__.py:9-23 holds a
+ * ctypes loader for a "libsrc" that is never built.  These entry points
+ * replace the Fortran routines that process boundary reaches; each
+ * declaration names the reference routine it stands in for.
+ *
+ * Conventions
+ *   - Every function returns 0 (ED_OK) on success or a nonzero ED_ERR_* code;
+ *     ed_last_error() then describes the failure (thread-local).
+ *   - All vectors are caller-owned device memory (e.g. torch tensors), passed
+ *     as plain pointers; no hot entry point allocates.  Entry points that
+ *     reduce (dot products, norms) take a caller-owned device scratch buffer;
+ *     ed_scratch_bytes() gives the size it needs.
+ *   - A sector vector is laid out as [nsdn rows][ld columns], element (d,u)
+ *     at d*ld + u, d the down-string index and u the up-string index; with
+ *     ld == nsup this is exactly the reference's index (D-1)*NSUP+U
+ *     (hprod_hubbard.f90:31).  Padding columns u >= nsup must hold zeros.
+ *   - Work is enqueued on the given CUDA stream (a cudaStream_t passed as
+ *     void*; NULL is the legacy default stream) and is asynchronous unless
+ *     stated.  Calls that share a scratch buffer must not overlap in time.
+ *   - Scalars produced on the device (dots, norms, RDMs) are FP64.
+ */
+#ifndef PYHUB_ED_H
+#define PYHUB_ED_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    ED_OK = 0,
+    ED_ERR_ARG = 1,      /* invalid argument (rejected before any launch) */
+    ED_ERR_CUDA = 2,     /* CUDA runtime error */
+    ED_ERR_MEM = 3,      /* device allocation failed (sector tables only) */
+    ED_ERR_RANGE = 4     /* size beyond a stated limit */
+};
+
+enum { ED_HUBBARD = 0, ED_HEISENBERG = 1 };
+enum { ED_F32 = 0, ED_F64 = 1 };
+
+typedef struct ed_sector ed_sector;
+
+/* Last error message of the calling thread ("" when none). */
+const char *ed_last_error(void);
+
+/* ABI version (major*100+minor). */
+int ed_version(void);
+
+/* Binomial coefficient C(n,k); replaces BINOM (funcmod.f90:7-16). */
+int64_t ed_binom(int n, int k);
+
+/* Host enumeration of the ne-of-norb spin strings in the reference's order;
+ * replaces HILBERT / WRITE_BASIS (compute_basis.f90:67-96, :27-64) and the
+ * basis.h5 cache read by READ_BASIS (basismod.f90:38-75).  out holds n
+ * entries, n == C(norb,ne). */
+int ed_basis(int norb, int ne, uint32_t *out, int64_t n);
+
+/* Index of a spin string in that order (the linear search of
+ * hprod_hubbard.f90:41-47 as a closed form); -1 when not an ne-string. */
+int64_t ed_rank(int norb, int ne, uint32_t s);
+
+/* Build the device tables of one sector.  Replaces the state that
+ * READ_INPUT / READ_BASIS load into HUBMOD (compute_solver.f90:11-19,
+ * :39-179).
+ *   kind ED_HUBBARD:    t = norb*norb hopping matrix (row-major, as given to
+ *                       FermiHubbard; a hop J->K uses t[K][J]), U = per-site
+ *                       interaction (norb), J ignored.
+ *   kind ED_HEISENBERG: J = norb*norb exchange matrix, nup = norb/2, ndn = 0
+ *                       (the reference's heisenberg.py:24 sector), t,U ignored.
+ * Sizes beyond 32 sites or 2^31 strings per spin are ED_ERR_RANGE. */
+int ed_sector_create(int norb, int nup, int ndn, int kind,
+                     const double *t, const double *U, const double *J,
+                     ed_sector **out);
+int ed_sector_destroy(ed_sector *s);
+int ed_sector_dims(const ed_sector *s, int64_t *nsup, int64_t *nsdn, int64_t *dim);
+/* Host copies of the two string tables (nsup and nsdn entries). */
+int ed_sector_strings(const ed_sector *s, uint32_t *up, uint32_t *dn);
+/* Nonzeros per row of the hop tables actually applied (diagnostics). */
+int ed_sector_nnz(const ed_sector *s, int64_t *nnz_up, int64_t *nnz_dn);
+
+/* Device scratch bytes needed by the reducing entry points for n elements
+ * and nvec vectors. */
+int64_t ed_scratch_bytes(int64_t n, int nvec);
+
+/* y = scale * H x.  Replaces HPROD (hprod_hubbard.f90:17-118 for Hubbard,
+ * hprod_heis.f90:1-61 for Heisenberg).  dtype ED_F32 or ED_F64 (storage and
+ * arithmetic of x and y; FP32 accumulates each element in FP32).  ld >= nsup
+ * is the row stride (Heisenberg: ld ignored, vector of nsup entries).
+ * If dots != NULL, dots[0] = <x,y> and dots[1] = <y,y> are written (FP64,
+ * device pointer), using scratch. */
+int ed_hv(ed_sector *s, void *stream, int dtype, int64_t ld,
+          const void *x, void *y, double scale,
+          double *dots, void *scratch, int64_t scratch_bytes);
+
+/* out[j] = <V_j, w> and, if z != NULL, out[nvec + j] = <V_j, z>, j < nvec.
+ * V_j = V + j*ldv elements.  FP64 results (device pointer).  The dot
+ * products of the Lanczos loop (lanczos.f90:53,55) and of the
+ * reorthogonalisation the reference lacks. */
+int ed_multidot(void *stream, int dtype, int64_t n, const void *V, int64_t ldv, int nvec,
+                const void *w, const void *z, double *out, void *scratch, int64_t scratch_bytes);
+
+/* out = w - sum_j coef[j] V_j (w may be NULL: out = -sum coef V); coef is a
+ * device FP64 array of nvec entries.  out may alias w.  If norm2 != NULL,
+ * norm2[0] = <out,out> (FP64, device).  The vector update of lanczos.f90:54
+ * generalised to a full projection; with w = NULL it forms a Ritz vector
+ * V*c as READ_PSI_HUBBARD does (compute_solver.f90:282). out_dtype may differ
+ * from dtype (e.g. an FP64 Ritz vector from an FP32 basis). */
+int ed_update(void *stream, int dtype, int out_dtype, int64_t n, const void *V, int64_t ldv, int nvec,
+              const double *coef, const void *w, void *out, double *norm2,
+              void *scratch, int64_t scratch_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PYHUB_ED_H */

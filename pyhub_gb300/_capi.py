@@ -1,0 +1,224 @@
+"""Typed ctypes bindings of include/pyhub_ed.h and a thin device-side sector
+object.  Vectors are torch CUDA tensors; only their data pointers cross the
+C ABI.  Every call checks the status code and raises ``EDError`` with the
+library's message."""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from .libs import libcore
+
+ED_OK, ED_ERR_ARG, ED_ERR_CUDA, ED_ERR_MEM, ED_ERR_RANGE = 0, 1, 2, 3, 4
+ED_HUBBARD, ED_HEISENBERG = 0, 1
+ED_F32, ED_F64 = 0, 1
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_I64 = ctypes.c_int64
+_D = ctypes.c_double
+
+_SIGS = {
+    "ed_last_error": (ctypes.c_char_p, []),
+    "ed_version": (_I, []),
+    "ed_binom": (_I64, [_I, _I]),
+    "ed_basis": (_I, [_I, _I, _P, _I64]),
+    "ed_rank": (_I64, [_I, _I, ctypes.c_uint32]),
+    "ed_sector_create": (_I, [_I, _I, _I, _I, _P, _P, _P, ctypes.POINTER(_P)]),
+    "ed_sector_destroy": (_I, [_P]),
+    "ed_sector_dims": (_I, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
+    "ed_sector_strings": (_I, [_P, _P, _P]),
+    "ed_sector_nnz": (_I, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
+    "ed_scratch_bytes": (_I64, [_I64, _I]),
+    "ed_hv": (_I, [_P, _P, _I, _I64, _P, _P, _D, _P, _P, _I64]),
+    "ed_multidot": (_I, [_P, _I, _I64, _P, _I64, _I, _P, _P, _P, _P, _I64]),
+    "ed_update": (_I, [_P, _I, _I, _I64, _P, _I64, _I, _P, _P, _P, _P, _P, _I64]),
+}
+
+_bound = None
+
+
+class EDError(RuntimeError):
+    """A nonzero status from the C ABI."""
+
+    def __init__(self, func: str, code: int, msg: str):
+        super().__init__(f"{func} failed with status {code}: {msg}")
+        self.code = code
+
+
+def lib():
+    global _bound
+    if _bound is None:
+        L = libcore()
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _bound = L
+    return _bound
+
+
+def check(func: str, rc: int):
+    if rc != ED_OK:
+        raise EDError(func, rc, lib().ed_last_error().decode(errors="replace"))
+
+
+def _ptr(t) -> int | None:
+    if t is None:
+        return None
+    return t.data_ptr()
+
+
+def _stream(stream) -> int | None:
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    return stream if isinstance(stream, int) else stream.cuda_stream
+
+
+def dtype_code(dt) -> int:
+    import torch
+    if dt == torch.float32:
+        return ED_F32
+    if dt == torch.float64:
+        return ED_F64
+    raise TypeError(f"unsupported vector dtype {dt}")
+
+
+# ------------------------------------------------------------------ basis ---
+
+def binom(n: int, k: int) -> int:
+    return int(lib().ed_binom(n, k))
+
+
+def basis(norb: int, ne: int) -> np.ndarray:
+    """Spin strings in the reference order (compute_basis.f90:67-96)."""
+    n = binom(norb, ne)
+    out = np.zeros(max(n, 1), dtype=np.uint32)
+    check("ed_basis", lib().ed_basis(norb, ne, out.ctypes.data, n))
+    return out[:n]
+
+
+def rank(norb: int, ne: int, s: int) -> int:
+    return int(lib().ed_rank(norb, ne, int(s) & 0xFFFFFFFF))
+
+
+def scratch_bytes(n: int, nvec: int) -> int:
+    return int(lib().ed_scratch_bytes(int(n), int(nvec)))
+
+
+# ----------------------------------------------------------------- sector ---
+
+@dataclass
+class Dims:
+    nsup: int
+    nsdn: int
+    dim: int
+
+
+class Sector:
+    """Device tables of one (norb, nup, ndn) sector; owns an ed_sector*.
+
+    Vectors in the internal layout are [nsdn, ld] with ld = nsup rounded up
+    to a multiple of 32 (zero padding); ``to_ref``/``from_ref`` convert to the
+    reference's flat index d*nsup+u."""
+
+    PAD = 32
+
+    def __init__(self, norb: int, nup: int, ndn: int, kind: int = ED_HUBBARD, t=None, U=None, J=None):
+        self.norb, self.nup, self.ndn, self.kind = int(norb), int(nup), int(ndn), kind
+        h = _P()
+        tt = None if t is None else np.ascontiguousarray(t, dtype=np.float64).reshape(norb, norb)
+        uu = None if U is None else np.ascontiguousarray(np.broadcast_to(np.asarray(U, dtype=np.float64), (norb,)))
+        jj = None if J is None else np.ascontiguousarray(J, dtype=np.float64).reshape(norb, norb)
+        self._keep = (tt, uu, jj)
+        check("ed_sector_create", lib().ed_sector_create(
+            self.norb, self.nup, self.ndn, kind,
+            None if tt is None else tt.ctypes.data, None if uu is None else uu.ctypes.data,
+            None if jj is None else jj.ctypes.data, ctypes.byref(h)))
+        self._h = h
+        a, b, c = _I64(), _I64(), _I64()
+        check("ed_sector_dims", lib().ed_sector_dims(h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        self.nsup, self.nsdn, self.dim = a.value, b.value, c.value
+        if kind == ED_HUBBARD:
+            self.ld = (self.nsup + self.PAD - 1) // self.PAD * self.PAD
+            self.n = self.nsdn * self.ld
+        else:
+            self.ld = self.nsup
+            self.n = (self.nsup + self.PAD - 1) // self.PAD * self.PAD
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().ed_sector_destroy(self._h)
+            self._h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def strings(self):
+        up = np.zeros(max(self.nsup, 1), dtype=np.uint32)
+        dn = np.zeros(max(self.nsdn, 1), dtype=np.uint32)
+        check("ed_sector_strings", lib().ed_sector_strings(self._h, up.ctypes.data, dn.ctypes.data))
+        return up[:self.nsup], dn[:self.nsdn]
+
+    def nnz(self):
+        a, b = _I64(), _I64()
+        check("ed_sector_nnz", lib().ed_sector_nnz(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    # -------------------------------------------------------- layouts
+    def zeros(self, dtype, device=None, *shape):
+        import torch
+        return torch.zeros(*shape, self.n, dtype=dtype, device=device or "cuda")
+
+    def to_ref(self, v):
+        """Internal layout -> reference flat layout (a view when ld == nsup)."""
+        if self.kind == ED_HUBBARD:
+            return v.view(*v.shape[:-1], self.nsdn, self.ld)[..., : self.nsup].reshape(*v.shape[:-1], self.dim)
+        return v[..., : self.dim]
+
+    def from_ref(self, r, out=None):
+        import torch
+        if out is None:
+            out = torch.zeros(*r.shape[:-1], self.n, dtype=r.dtype, device=r.device)
+        if self.kind == ED_HUBBARD:
+            out.view(*r.shape[:-1], self.nsdn, self.ld)[..., : self.nsup] = r.reshape(*r.shape[:-1], self.nsdn, self.nsup)
+        else:
+            out[..., : self.dim] = r
+        return out
+
+    # -------------------------------------------------------- products
+    def hv(self, x, y, scale: float = 1.0, dots=None, scratch=None, ld: int | None = None, stream=None):
+        """y = scale * H x (device tensors in the internal layout unless ld is given)."""
+        ld = self.ld if ld is None else ld
+        sb = 0 if scratch is None else scratch.numel() * scratch.element_size()
+        check("ed_hv", lib().ed_hv(self._h, _stream(stream), dtype_code(x.dtype), int(ld), _ptr(x), _ptr(y),
+                                   float(scale), _ptr(dots), _ptr(scratch), int(sb)))
+
+
+def multidot(V, nvec: int, w, out, scratch, z=None, n: int | None = None, stream=None):
+    """out[j] = <V_j, w> (and out[nvec+j] = <V_j, z>) for j < nvec, FP64 on device."""
+    n = w.numel() if n is None else n
+    ldv = V.stride(0) if V.dim() > 1 else n
+    sb = scratch.numel() * scratch.element_size()
+    check("ed_multidot", lib().ed_multidot(_stream(stream), dtype_code(V.dtype), int(n), _ptr(V), int(ldv), int(nvec),
+                                           _ptr(w), _ptr(z), _ptr(out), _ptr(scratch), int(sb)))
+
+
+def update(V, nvec: int, coef, w, out, norm2=None, scratch=None, n: int | None = None, stream=None):
+    """out = w - sum_j coef_j V_j (w may be None), optional <out,out> into norm2."""
+    n = out.numel() if n is None else n
+    ldv = V.stride(0) if (V is not None and V.dim() > 1) else n
+    sb = 0 if scratch is None else scratch.numel() * scratch.element_size()
+    vdt = dtype_code(V.dtype) if V is not None else dtype_code(out.dtype)
+    check("ed_update", lib().ed_update(_stream(stream), vdt, dtype_code(out.dtype), int(n), _ptr(V), int(ldv),
+                                       int(nvec), _ptr(coef), _ptr(w), _ptr(out), _ptr(norm2), _ptr(scratch), int(sb)))

@@ -1,0 +1,281 @@
+"""GPU Lanczos drivers built on the sector H*v.
+
+Replaces LANCZOS (lanczos.f90:1-133), EXACT_DIAG's role for the ground state
+(exact_diag.f90:2-33) and READ_PSI_HUBBARD's Ritz-vector reconstruction
+(compute_solver.f90:282-284).
+
+Differences from the reference, by design:
+  * the Krylov basis lives in HBM instead of an HDF5 file
+    (lanczos.f90:42-49, 137-161);
+  * full reorthogonalisation with one reduction per step: the multi-dot pass
+    of step k returns both V^T H u_k and V^T u_k, so the Gram matrix
+    G = V^T V is known exactly and the projection w - V G^-1 V^T w costs one
+    more pass over V (delayed classical Gram-Schmidt, "DCGS2", Bielich,
+    Langou, Thomas, Swirydowicz, Yamazaki, Boman, Parallel Computing 2022);
+  * vectors may be stored in FP32 while every scalar (dots, norms, the
+    tridiagonal, its eigensolve) is FP64, followed by an FP64 refinement
+    Lanczos started from the FP32 Ritz vector;
+  * the start vector is a seeded uniform[-0.5,0.5) draw (the reference's
+    RAND()-0.5 is unseeded, lanczos.f90:22-25).
+
+The convergence rule of the reference (blocks of NADD=5 steps, degeneracy
+aware test on Ritz value NDEG+1, lanczos.f90:61-89) is available as
+``ReferenceRule``.
+"""
+from __future__ import annotations
+
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import scipy.linalg as sla
+
+from .. import _capi
+
+NADD = 5
+
+
+def _torch():
+    import torch
+    return torch
+
+
+class ReferenceRule:
+    """lanczos.f90:44-91: check every NADD steps; the Ritz value NDEG+1 must
+    move by less than acc; a converged value equal to the lowest one raises
+    NDEG (a degenerate copy) and the loop goes on."""
+
+    def __init__(self, acc: float = 1e-8):
+        self.acc = float(acc)
+        self.ev = 0.0
+        self.ndeg = 0
+        self.converged = False
+
+    def __call__(self, val: np.ndarray, step: int = 0) -> bool:
+        i = min(self.ndeg, len(val) - 1)
+        if abs(val[i] - self.ev) < self.acc:
+            if abs(val[i] - val[0]) > self.acc and (self.ndeg + 1) > 1:
+                self.converged = True
+            else:
+                self.ndeg += 1
+        else:
+            self.ev = val[i]
+        return self.converged
+
+
+class EnergyRule:
+    """Stop when the lowest Ritz value moved by less than tol over one check."""
+
+    def __init__(self, tol: float, min_steps: int = 0):
+        self.tol = float(tol)
+        self.min_steps = min_steps
+        self.prev = None
+        self.converged = False
+        self.ndeg = 1
+
+    def __call__(self, val: np.ndarray, step: int = 1 << 30) -> bool:
+        e = float(val[0])
+        if self.prev is not None and abs(e - self.prev) < self.tol and step >= self.min_steps:
+            self.converged = True
+        self.prev = e
+        return self.converged
+
+
+@dataclass
+class KrylovResult:
+    alpha: np.ndarray
+    beta: np.ndarray            # beta[k] couples steps k and k+1 (len == len(alpha))
+    ritz: np.ndarray            # eigenvalues of the final tridiagonal
+    ritz_vectors: np.ndarray    # its eigenvectors (columns)
+    steps: int
+    converged: bool
+    breakdown: bool
+    psi: object = None          # FP64 device tensor, internal layout (lowest Ritz vector)
+    conv: float = 0.0
+    ndeg: int = 0
+    times: dict = field(default_factory=dict)
+    gram_offdiag: float = 0.0   # max |G - I| of the stored basis (orthogonality check)
+
+
+def start_vector(sec, seed: int = 0, dtype=None, device=None):
+    """Seeded uniform[-0.5,0.5) start vector in the internal layout (padding 0).
+    Drawn in the reference layout so that the draw does not depend on ld."""
+    torch = _torch()
+    g = torch.Generator(device=device or "cuda")
+    g.manual_seed(int(seed))
+    r = torch.rand(sec.dim, generator=g, dtype=torch.float64, device=device or "cuda") - 0.5
+    v = sec.from_ref(r)
+    return v if dtype is None else v.to(dtype)
+
+
+def _tridiag_eigs(alpha, beta, k, vectors=False):
+    a = np.asarray(alpha[:k], dtype=np.float64)
+    b = np.asarray(beta[: k - 1], dtype=np.float64)
+    if k == 1:
+        return (a.copy(), np.ones((1, 1))) if vectors else a.copy()
+    if vectors:
+        return sla.eigh_tridiagonal(a, b)
+    return sla.eigh_tridiagonal(a, b, eigvals_only=True)
+
+
+class _Scratch:
+    def __init__(self, n, nvec, device):
+        torch = _torch()
+        nb = _capi.scratch_bytes(n, max(nvec, 2))
+        self.buf = torch.empty((nb + 7) // 8, dtype=torch.float64, device=device)
+        self.dots = torch.zeros(2 * max(nvec, 2) + 2, dtype=torch.float64, device=device)
+        self.nrm = torch.zeros(2, dtype=torch.float64, device=device)
+        self.coef = torch.zeros(max(nvec, 2), dtype=torch.float64, device=device)
+
+
+def lanczos_full(sec, v0, max_steps: int, dtype=None, rule=None, check_every: int = NADD,
+                 min_steps: int = 0, want_vector: bool = True, vec_index: int = 0,
+                 timer=None) -> KrylovResult:
+    """Lanczos with full reorthogonalisation (delayed CGS with the exact Gram
+    matrix).  v0: start vector (device tensor, internal layout).  The basis
+    of max_steps+1 vectors is stored in ``dtype`` (FP32 or FP64); scalars are
+    FP64.  Stops after max_steps, on breakdown, or when ``rule`` is met at a
+    check.  Returns the tridiagonal, its eigenpairs and (optionally) the Ritz
+    vector ``vec_index`` as an FP64 device tensor."""
+    torch = _torch()
+    dtype = dtype or v0.dtype
+    dev = v0.device
+    n = sec.n
+    m = int(max_steps)
+    t_start = time.perf_counter()
+    V = torch.zeros((m + 1, n), dtype=dtype, device=dev)
+    w = torch.zeros(n, dtype=dtype, device=dev)
+    ws = _Scratch(n, m + 1, dev)
+    V[0].copy_(v0)
+    _capi.multidot(V, 1, V[0], ws.dots, ws.buf)
+    n0 = float(ws.dots[0].item())
+    if not (n0 > 0.0 and math.isfinite(n0)):
+        raise ValueError("start vector has zero or non-finite norm")
+    s = np.zeros(m + 2)
+    s[0] = 1.0 / math.sqrt(n0)
+    G = np.zeros((m + 2, m + 2))
+    G[0, 0] = s[0] * s[0] * n0
+    L = np.zeros((m + 2, m + 2))       # Cholesky factor of G, grown a row per step
+    alpha = np.zeros(m + 1)
+    beta = np.zeros(m + 1)
+    k_done = 0
+    converged = breakdown = False
+    val = None
+    t_hv = t_dot = t_upd = 0.0
+    for k in range(m):
+        if timer: timer("hv", k)
+        sec.hv(V[k], w)
+        _capi.multidot(V, k + 1, w, ws.dots, ws.buf, z=V[k])
+        d = ws.dots[: 2 * (k + 1)].cpu().numpy()
+        a, b = d[: k + 1], d[k + 1:]
+        sv = s[: k + 1]
+        G[k, : k + 1] = sv * sv[k] * b
+        G[: k + 1, k] = G[k, : k + 1]
+        # grow the Cholesky factor by row k
+        if k == 0:
+            L[0, 0] = math.sqrt(G[0, 0])
+        else:
+            l = sla.solve_triangular(L[:k, :k], G[k, :k], lower=True, check_finite=False)
+            L[k, :k] = l
+            L[k, k] = math.sqrt(max(G[k, k] - float(l @ l), 1e-300))
+        c = sv * sv[k] * a
+        y = sla.cho_solve((L[: k + 1, : k + 1], True), c, check_finite=False)
+        coef = y * sv / sv[k]
+        ws.coef[: k + 1].copy_(torch.from_numpy(coef))
+        _capi.update(V, k + 1, ws.coef, w, V[k + 1], norm2=ws.nrm, scratch=ws.buf)
+        nw2 = float(ws.nrm[0].item())
+        alpha[k] = c[k]
+        bk = sv[k] * math.sqrt(max(nw2, 0.0))
+        beta[k] = bk
+        k_done = k + 1
+        if not math.isfinite(nw2):
+            raise FloatingPointError(f"non-finite norm at Lanczos step {k}")
+        if bk <= 1e-13 * max(1.0, abs(alpha[k])):
+            breakdown = True
+        else:
+            s[k + 1] = 1.0 / math.sqrt(nw2)
+            G[k + 1, k + 1] = 1.0
+        if rule is not None and (k_done % check_every == 0 or breakdown) and k_done >= min_steps:
+            val = _tridiag_eigs(alpha, beta, k_done)
+            if rule(val, k_done):
+                converged = True
+                break
+        if breakdown:
+            converged = True
+            break
+    t_loop = time.perf_counter()
+    val, vec = _tridiag_eigs(alpha, beta, k_done, vectors=True)
+    res = KrylovResult(alpha=alpha[:k_done].copy(), beta=beta[:k_done].copy(), ritz=val, ritz_vectors=vec,
+                       steps=k_done, converged=converged, breakdown=breakdown,
+                       ndeg=getattr(rule, "ndeg", 0) if rule is not None else 0)
+    gi = G[:k_done, :k_done] - np.eye(k_done)
+    res.gram_offdiag = float(np.abs(gi).max()) if k_done > 0 else 0.0
+    if want_vector:
+        z = vec[:, vec_index]
+        coef = -(z * s[:k_done])
+        ws.coef[:k_done].copy_(torch.from_numpy(coef))
+        psi = torch.zeros(n, dtype=torch.float64, device=dev)
+        _capi.update(V, k_done, ws.coef, None, psi, norm2=ws.nrm, scratch=ws.buf)
+        nrm = math.sqrt(float(ws.nrm[0].item()))
+        psi.mul_(1.0 / nrm)
+        res.psi = psi
+    res.times = {"loop": t_loop - t_start, "total": time.perf_counter() - t_start}
+    del V, w, ws
+    return res
+
+
+@dataclass
+class GroundState:
+    e0: float
+    psi: object                 # FP64 device tensor, internal layout
+    ritz: np.ndarray
+    alpha: np.ndarray
+    beta: np.ndarray
+    steps: int
+    refine_steps: int
+    converged: bool
+    ndeg: int
+    times: dict
+    mode: str
+    e0_unrefined: float = float("nan")
+    ritz_vectors: np.ndarray = None
+
+
+def ground_state(sec, mode: str = "mixed", steps: int = 200, seed: int = 0, v0=None, rule=None,
+                 refine_steps: int = 60, refine_tol: float = 1e-13, check_every: int = NADD,
+                 nb_vectors: int = 1) -> GroundState:
+    """Ground state of the sector operator.
+
+    mode "f64":   FP64 vectors, FP64 scalars (the plain FP64 GPU Lanczos).
+    mode "f32":   FP32 vectors, FP64 scalars, no refinement.
+    mode "mixed": FP32 vectors + FP64 scalars for ``steps`` steps, then an
+                  FP64 Lanczos restarted from the FP32 Ritz vector until the
+                  lowest Ritz value moves less than refine_tol*max(1,|E0|)
+                  between checks (at most refine_steps steps)."""
+    torch = _torch()
+    t0 = time.perf_counter()
+    if v0 is None:
+        v0 = start_vector(sec, seed)
+    if mode == "f64":
+        r = lanczos_full(sec, v0.to(torch.float64), steps, torch.float64, rule=rule, check_every=check_every)
+        torch.cuda.synchronize()
+        return GroundState(e0=float(r.ritz[0]), psi=r.psi, ritz=r.ritz, alpha=r.alpha, beta=r.beta, steps=r.steps,
+                           refine_steps=0, converged=r.converged, ndeg=r.ndeg,
+                           times={"total": time.perf_counter() - t0, "fp64": r.times["total"]}, mode=mode,
+                           e0_unrefined=float(r.ritz[0]), ritz_vectors=r.ritz_vectors)
+    r32 = lanczos_full(sec, v0.to(torch.float32), steps, torch.float32, rule=rule, check_every=check_every)
+    t1 = time.perf_counter()
+    if mode == "f32":
+        return GroundState(e0=float(r32.ritz[0]), psi=r32.psi, ritz=r32.ritz, alpha=r32.alpha, beta=r32.beta,
+                           steps=r32.steps, refine_steps=0, converged=r32.converged, ndeg=r32.ndeg,
+                           times={"total": t1 - t0, "fp32": r32.times["total"]}, mode=mode,
+                           e0_unrefined=float(r32.ritz[0]), ritz_vectors=r32.ritz_vectors)
+    rr = EnergyRule(refine_tol * max(1.0, abs(float(r32.ritz[0]))), min_steps=2 * check_every)
+    r64 = lanczos_full(sec, r32.psi, refine_steps, torch.float64, rule=rr, check_every=check_every)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    return GroundState(e0=float(r64.ritz[0]), psi=r64.psi, ritz=r64.ritz, alpha=r32.alpha, beta=r32.beta,
+                       steps=r32.steps, refine_steps=r64.steps, converged=r32.converged or rr.converged,
+                       ndeg=r32.ndeg, times={"total": t2 - t0, "fp32": t1 - t0, "refine": t2 - t1}, mode=mode,
+                       e0_unrefined=float(r32.ritz[0]), ritz_vectors=r64.ritz_vectors)

@@ -1,0 +1,451 @@
+// ed_hv.cu -- on-the-fly Hamiltonian-vector products.
+//
+// Hubbard (replaces HPROD, hprod_hubbard.f90:17-118).  With the vector viewed
+// as a matrix X[d][u] (row = down string, contiguous up strings), H = A_up
+// acting inside each row + A_dn mixing rows + a diagonal:
+//   y[d][u] = diag(d,u) x[d][u] + sum_{q in up(u)} c x[d][q] + sum_{e in dn(d)} c x[e][u]
+// Pass 1 (row pass): each CTA stages whole rows of x in shared memory and
+//   applies the diagonal and the up hops from there (gathers stay on chip).
+// Pass 2 (slab pass): the down hops are row-axpys y[d][:] += c x[e][:].
+//   Columns are cut into slabs so that one slab of x (nsdn rows x slab
+//   width) stays resident in L2 while every output row of that slab gathers
+//   its ~N neighbour rows; x therefore streams from HBM about once.  The pass
+//   also forms <x,y> and <y,y> for the Lanczos scalars.
+//
+// Heisenberg (replaces HPROD, hprod_heis.f90:1-61): one gather per
+// antiparallel bond with the flipped string ranked through byte tables.
+#include "ed_common.cuh"
+
+namespace ed {
+
+struct HubArgs {
+    int64_t nsup, nsdn, ld;
+    const uint32_t *ustr; const int32_t *uptr; const int32_t *usrc; const void *ucf; const double *uediag;
+    const uint32_t *dstr; const int32_t *dptr; const int32_t *dsrc; const void *dcf; const double *dediag;
+    double u_site[kMaxSites];
+    int u_uniform;
+    double u_value;
+    double scale;
+};
+
+template <typename T>
+__device__ __forceinline__ T u_energy(const HubArgs &a, uint32_t both)
+{
+    if (a.u_uniform) return (T)a.u_value * (T)__popc(both);
+    T e = 0;
+    while (both) {
+        int b = __ffs(both) - 1;
+        e += (T)a.u_site[b];
+        both &= both - 1;
+    }
+    return e;
+}
+
+// Copy n elements from global src to shared dst (dst 16-byte aligned).
+template <typename T>
+__device__ __forceinline__ void stage_row(T *dst, const T *__restrict__ src, int64_t n, bool vec_ok)
+{
+    constexpr int VW = 16 / sizeof(T);
+    using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+    if (vec_ok) {
+        int64_t nv = (n + VW - 1) / VW;  // may read into the zero padding of the row
+        const V *s4 = reinterpret_cast<const V *>(src);
+        V *d4 = reinterpret_cast<V *>(dst);
+        for (int64_t i = threadIdx.x; i < nv; i += blockDim.x) d4[i] = __ldg(s4 + i);
+    } else {
+        for (int64_t i = threadIdx.x; i < n; i += blockDim.x) dst[i] = __ldg(src + i);
+    }
+}
+
+// Pass 1: diagonal + up hops, R rows per CTA iteration.
+template <typename T, int R>
+__global__ void __launch_bounds__(512) hub_row_kernel(const T *__restrict__ x, T *__restrict__ y,
+                                                      const HubArgs a, int64_t sld, int vec_ok)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *xs = reinterpret_cast<T *>(smem_raw);
+    const T *__restrict__ cf = static_cast<const T *>(a.ucf);
+    const int64_t nsup = a.nsup, ld = a.ld;
+    for (int64_t d0 = (int64_t)blockIdx.x * R; d0 < a.nsdn; d0 += (int64_t)gridDim.x * R) {
+        const int nr = (int)min((int64_t)R, a.nsdn - d0);
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+            if (r < nr) stage_row<T>(xs + r * sld, x + (d0 + r) * ld, nsup, vec_ok != 0);
+        __syncthreads();
+        uint32_t sd[R];
+        T ed[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            sd[r] = (r < nr) ? a.dstr[d0 + r] : 0u;
+            ed[r] = (r < nr) ? (T)a.dediag[d0 + r] : (T)0;
+        }
+        for (int64_t u = threadIdx.x; u < nsup; u += blockDim.x) {
+            const uint32_t su = __ldg(a.ustr + u);
+            const T eu = (T)__ldg(a.uediag + u);
+            T acc[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r) acc[r] = (eu + ed[r] + u_energy<T>(a, su & sd[r])) * xs[r * sld + u];
+            const int e0 = __ldg(a.uptr + u), e1 = __ldg(a.uptr + u + 1);
+            for (int e = e0; e < e1; ++e) {
+                const int q = __ldg(a.usrc + e);
+                const T c = __ldg(cf + e);
+#pragma unroll
+                for (int r = 0; r < R; ++r) acc[r] += c * xs[r * sld + q];
+            }
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+                if (r < nr) y[(d0 + r) * ld + u] = acc[r] * (T)a.scale;
+        }
+        __syncthreads();
+    }
+}
+
+// Pass 2: down hops, y[d][slab] += sum_e c_e x[src_e][slab]; optional dots.
+// Work items (slab, group of 8 rows) are visited slab-major by a persistent
+// grid so that the CTAs in flight share one or two slabs of x in L2.
+template <typename T, int VW>
+__global__ void __launch_bounds__(256) hub_slab_kernel(const T *__restrict__ x, T *__restrict__ y,
+                                                       const HubArgs a, int64_t slab_w, int64_t ngroups,
+                                                       int64_t nitems, double *__restrict__ partials)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const T *__restrict__ cf = static_cast<const T *>(a.dcf);
+    const int64_t nsup = a.nsup, ld = a.ld;
+    const T sc = (T)a.scale;
+    double dxy = 0.0, dyy = 0.0;
+    for (int64_t item = blockIdx.x; item < nitems; item += gridDim.x) {
+        const int64_t slab = item / ngroups, g = item - slab * ngroups;
+        const int64_t d = g * 8 + warp;
+        if (d >= a.nsdn) continue;
+        const int64_t c0 = slab * slab_w, c1 = min(c0 + slab_w, nsup);
+        const int e0 = __ldg(a.dptr + d), e1 = __ldg(a.dptr + d + 1);
+        T *yr = y + d * ld;
+        float pxy = 0.f, pyy = 0.f;
+        double qxy = 0.0, qyy = 0.0;
+        int64_t c = c0 + (int64_t)lane * VW;
+        for (; c + VW <= c1; c += 32 * VW) {
+            T acc[VW];
+#pragma unroll
+            for (int k = 0; k < VW; ++k) acc[k] = yr[c + k];
+            for (int e = e0; e < e1; ++e) {
+                const T w = __ldg(cf + e) * sc;
+                const T *xr = x + (int64_t)__ldg(a.dsrc + e) * ld + c;
+                if constexpr (VW == 4 && sizeof(T) == 4) {
+                    const float4 v = __ldg(reinterpret_cast<const float4 *>(xr));
+                    acc[0] += w * v.x; acc[1] += w * v.y; acc[2] += w * v.z; acc[3] += w * v.w;
+                } else if constexpr (VW == 2 && sizeof(T) == 8) {
+                    const double2 v = __ldg(reinterpret_cast<const double2 *>(xr));
+                    acc[0] += w * v.x; acc[1] += w * v.y;
+                } else {
+#pragma unroll
+                    for (int k = 0; k < VW; ++k) acc[k] += w * __ldg(xr + k);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < VW; ++k) yr[c + k] = acc[k];
+            if (partials) {
+#pragma unroll
+                for (int k = 0; k < VW; ++k) {
+                    const T xv = __ldg(x + d * ld + c + k);
+                    if constexpr (sizeof(T) == 4) { pxy += xv * acc[k]; pyy += acc[k] * acc[k]; }
+                    else { qxy += xv * acc[k]; qyy += acc[k] * acc[k]; }
+                }
+            }
+        }
+        // ragged tail of the slab (scalar)
+        for (int64_t cc = c; cc < c1; ++cc) {
+            T acc = yr[cc];
+            for (int e = e0; e < e1; ++e)
+                acc += __ldg(cf + e) * sc * __ldg(x + (int64_t)__ldg(a.dsrc + e) * ld + cc);
+            yr[cc] = acc;
+            if (partials) {
+                const T xv = __ldg(x + d * ld + cc);
+                if constexpr (sizeof(T) == 4) { pxy += xv * acc; pyy += acc * acc; }
+                else { qxy += xv * acc; qyy += acc * acc; }
+            }
+        }
+        dxy += (double)pxy + qxy;
+        dyy += (double)pyy + qyy;
+    }
+    if (partials) {
+        __shared__ double red[2][8];
+        dxy = warp_sum(dxy);
+        dyy = warp_sum(dyy);
+        if (lane == 0) { red[0][warp] = dxy; red[1][warp] = dyy; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double sxy = 0.0, syy = 0.0;
+            for (int w = 0; w < 8; ++w) { sxy += red[0][w]; syy += red[1][w]; }
+            partials[2 * blockIdx.x] = sxy;
+            partials[2 * blockIdx.x + 1] = syy;
+        }
+    }
+}
+
+// Sum nblocks rows of m partials into out[m] (FP64, fixed order).
+__global__ void reduce_partials_kernel(const double *__restrict__ partials, int nblocks, int m,
+                                       double *__restrict__ out)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nw = blockDim.x >> 5;
+    for (int j = blockIdx.x * nw + warp; j < m; j += gridDim.x * nw) {
+        double s = 0.0;
+        for (int b = lane; b < nblocks; b += 32) s += partials[(int64_t)b * m + j];
+        s = warp_sum(s);
+        if (lane == 0) out[j] = s;
+    }
+}
+
+int launch_reduce(const double *partials, int nblocks, int m, double *out, cudaStream_t st)
+{
+    int threads = 256, per = threads / 32;
+    int blocks = (m + per - 1) / per;
+    if (blocks > 1024) blocks = 1024;
+    reduce_partials_kernel<<<blocks, threads, 0, st>>>(partials, nblocks, m, out);
+    ED_CHECK_LAUNCH();
+    return ED_OK;
+}
+
+// ------------------------------------------------------------ Heisenberg
+
+struct HeisArgs {
+    int norb, nholes;
+    int64_t n;
+    const uint32_t *lut;  // [4][33][256]
+    int nbond;
+    int8_t bj[kMaxSites * kMaxSites / 2];
+    int8_t bk[kMaxSites * kMaxSites / 2];
+    double flip_jk[kMaxSites * kMaxSites / 2];
+    double flip_kj[kMaxSites * kMaxSites / 2];
+    double zz[kMaxSites * kMaxSites / 2];
+    double dconst;
+    double scale;
+    uint32_t binom[kMaxSites + 1][17];
+};
+
+__device__ __forceinline__ uint32_t heis_rank(const uint32_t *__restrict__ lut, uint32_t h)
+{
+    uint32_t r = 0;
+    int c = 0;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        const uint32_t byte = (h >> (8 * b)) & 255u;
+        r += __ldg(lut + (b * 33 + c) * 256 + byte);
+        c += __popc(byte);
+    }
+    return r;
+}
+
+// colex unrank of an m-hole pattern among norb positions
+__device__ __forceinline__ uint32_t heis_unrank(const HeisArgs &a, uint32_t r)
+{
+    uint32_t h = 0;
+    int p = a.norb - 1;
+    for (int i = a.nholes; i >= 1; --i) {
+        while (p >= i && a.binom[p][i] > r) --p;
+        // largest p with C(p,i) <= r (p >= i-1 always satisfies since C(i-1,i)=0)
+        if (p < i) p = i - 1;
+        h |= 1u << p;
+        r -= a.binom[p][i];
+        --p;
+    }
+    return h;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) heis_kernel(const T *__restrict__ x, T *__restrict__ y, const HeisArgs a,
+                                                   double *__restrict__ partials)
+{
+    double dxy = 0.0, dyy = 0.0;
+    const uint32_t full = (a.norb >= 32) ? 0xFFFFFFFFu : ((1u << a.norb) - 1u);
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t h = heis_unrank(a, (uint32_t)p);  // bit j: site j+1 is a down spin
+        T dg = (T)a.dconst;
+        T acc = 0;
+        for (int b = 0; b < a.nbond; ++b) {
+            const int J = a.bj[b], K = a.bk[b];
+            const uint32_t hj = (h >> (J - 1)) & 1u, hk = (h >> (K - 1)) & 1u;
+            if (hj == hk) {
+                dg += (T)(0.25 * a.zz[b]);
+                continue;
+            }
+            dg -= (T)(0.25 * a.zz[b]);
+            // target has K up (hk==0) and J down (hj==1): element flip_jk, else flip_kj
+            const double c = hj ? a.flip_jk[b] : a.flip_kj[b];
+            if (c == 0.0) continue;
+            const uint32_t q = h ^ ((1u << (J - 1)) | (1u << (K - 1)));
+            acc += (T)c * __ldg(x + heis_rank(a.lut, q));
+        }
+        (void)full;
+        const T xv = x[p];
+        const T out = (dg * xv + acc) * (T)a.scale;
+        y[p] = out;
+        if (partials) { dxy += (double)xv * (double)out; dyy += (double)out * (double)out; }
+    }
+    if (partials) {
+        __shared__ double red[2][8];
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        dxy = warp_sum(dxy);
+        dyy = warp_sum(dyy);
+        if (lane == 0) { red[0][warp] = dxy; red[1][warp] = dyy; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double sxy = 0.0, syy = 0.0;
+            for (int w = 0; w < 8; ++w) { sxy += red[0][w]; syy += red[1][w]; }
+            partials[2 * blockIdx.x] = sxy;
+            partials[2 * blockIdx.x + 1] = syy;
+        }
+    }
+}
+
+// ------------------------------------------------------------ launchers
+
+static constexpr int kMaxPartialBlocks = 1024;
+
+template <typename T>
+static int hub_hv(ed_sector *s, cudaStream_t st, int64_t ld, const T *x, T *y, double scale, double *dots,
+                  double *partials)
+{
+    HubArgs a;
+    a.nsup = s->nsup; a.nsdn = s->nsdn; a.ld = ld;
+    a.ustr = s->up.str; a.uptr = s->up.ptr; a.usrc = s->up.src; a.uediag = s->up.ediag;
+    a.dstr = s->dn.str; a.dptr = s->dn.ptr; a.dsrc = s->dn.src; a.dediag = s->dn.ediag;
+    if (sizeof(T) == 4) { a.ucf = s->up.cf32; a.dcf = s->dn.cf32; }
+    else { a.ucf = s->up.cf64; a.dcf = s->dn.cf64; }
+    for (int b = 0; b < kMaxSites; ++b) a.u_site[b] = s->u_site[b];
+    a.u_uniform = s->u_uniform ? 1 : 0;
+    a.u_value = s->u_value;
+    a.scale = scale;
+    const int nsm = num_sms();
+    constexpr int VWS = 16 / sizeof(T);
+    // ---- pass 1
+    const int64_t sld = (s->nsup + VWS - 1) / VWS * VWS;
+    const bool vec_ok = (ld % VWS == 0) && ((reinterpret_cast<uintptr_t>(x) & 15) == 0);
+    int maxsm = 0;
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    }
+    const size_t row_bytes = (size_t)sld * sizeof(T);
+    if (row_bytes > (size_t)maxsm) {
+        set_error("up-string row of %lld entries does not fit in shared memory (%d bytes)",
+                  (long long)s->nsup, maxsm);
+        return ED_ERR_RANGE;
+    }
+    // two rows per CTA when they fit with two CTAs per SM, else one
+    constexpr int R2 = 2;
+    const bool two = (size_t)R2 * row_bytes * 2 <= (size_t)maxsm;
+    const int threads = 512;
+    if (two) {
+        size_t smem = (size_t)R2 * row_bytes;
+        ED_CHECK_CUDA(cudaFuncSetAttribute(hub_row_kernel<T, R2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int64_t blocks = (s->nsdn + R2 - 1) / R2;
+        int64_t cap = (int64_t)nsm * 2;
+        if (blocks > cap) blocks = cap;
+        hub_row_kernel<T, R2><<<(unsigned)blocks, threads, smem, st>>>(x, y, a, sld, vec_ok ? 1 : 0);
+    } else {
+        size_t smem = row_bytes;
+        ED_CHECK_CUDA(cudaFuncSetAttribute(hub_row_kernel<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int64_t blocks = s->nsdn;
+        int64_t cap = (int64_t)nsm * 2;
+        if (blocks > cap) blocks = cap;
+        hub_row_kernel<T, 1><<<(unsigned)blocks, threads, smem, st>>>(x, y, a, sld, vec_ok ? 1 : 0);
+    }
+    ED_CHECK_LAUNCH();
+    // ---- pass 2
+    // slab width: the x slab (nsdn rows x width) should take at most ~48 MB of L2
+    int64_t slab_w = (int64_t)(48.0e6 / ((double)s->nsdn * sizeof(T)));
+    slab_w = slab_w / 256 * 256;
+    if (slab_w < 256) slab_w = 256;
+    if (slab_w > s->nsup) slab_w = (s->nsup + VWS - 1) / VWS * VWS;
+    const int64_t ngroups = (s->nsdn + 7) / 8;
+    const int64_t nslab = (s->nsup + slab_w - 1) / slab_w;
+    const int64_t nitems = ngroups * nslab;
+    int64_t blocks2 = (int64_t)nsm * 8;
+    if (blocks2 > kMaxPartialBlocks) blocks2 = kMaxPartialBlocks;
+    if (blocks2 > nitems) blocks2 = nitems;
+    if (blocks2 < 1) blocks2 = 1;
+    const bool vec2 = (ld % VWS == 0) && ((reinterpret_cast<uintptr_t>(x) & 15) == 0) &&
+                      ((reinterpret_cast<uintptr_t>(y) & 15) == 0);
+    double *part = dots ? partials : nullptr;
+    if (vec2)
+        hub_slab_kernel<T, VWS><<<(unsigned)blocks2, 256, 0, st>>>(x, y, a, slab_w, ngroups, nitems, part);
+    else
+        hub_slab_kernel<T, 1><<<(unsigned)blocks2, 256, 0, st>>>(x, y, a, slab_w, ngroups, nitems, part);
+    ED_CHECK_LAUNCH();
+    if (dots) return launch_reduce(partials, (int)blocks2, 2, dots, st);
+    return ED_OK;
+}
+
+template <typename T>
+static int heis_hv(ed_sector *s, cudaStream_t st, const T *x, T *y, double scale, double *dots, double *partials)
+{
+    HeisArgs a;
+    const HeisTables &h = s->heis;
+    a.norb = s->norb;
+    a.nholes = s->norb - s->nup;
+    a.n = s->nsup;
+    a.lut = h.lut;
+    if (h.nbond > kMaxSites * kMaxSites / 2) { set_error("too many bonds"); return ED_ERR_RANGE; }
+    a.nbond = h.nbond;
+    for (int b = 0; b < h.nbond; ++b) {
+        a.bj[b] = h.bj[b]; a.bk[b] = h.bk[b];
+        a.flip_jk[b] = h.flip_jk[b]; a.flip_kj[b] = h.flip_kj[b]; a.zz[b] = h.zz[b];
+    }
+    a.dconst = h.dconst;
+    a.scale = scale;
+    for (int n = 0; n <= kMaxSites; ++n)
+        for (int k = 0; k <= 16; ++k) a.binom[n][k] = (uint32_t)ed_binom(n, k);
+    const int nsm = num_sms();
+    int64_t blocks = (s->nsup + 255) / 256;
+    int64_t cap = (int64_t)nsm * 8;
+    if (cap > kMaxPartialBlocks) cap = kMaxPartialBlocks;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    heis_kernel<T><<<(unsigned)blocks, 256, 0, st>>>(x, y, a, dots ? partials : nullptr);
+    ED_CHECK_LAUNCH();
+    if (dots) return launch_reduce(partials, (int)blocks, 2, dots, st);
+    return ED_OK;
+}
+
+}  // namespace ed
+
+using namespace ed;
+
+extern "C" int64_t ed_scratch_bytes(int64_t n, int nvec)
+{
+    (void)n;
+    if (nvec < 1) nvec = 1;
+    return (int64_t)kMaxPartialBlocks * 2 * nvec * (int64_t)sizeof(double) + 4096;
+}
+
+extern "C" int ed_hv(ed_sector *s, void *stream, int dtype, int64_t ld, const void *x, void *y, double scale,
+                     double *dots, void *scratch, int64_t scratch_bytes)
+{
+    clear_error();
+    ED_REQUIRE(s != nullptr, "sector is NULL");
+    ED_REQUIRE(x != nullptr && y != nullptr, "x or y is NULL");
+    ED_REQUIRE(x != y, "x and y must not alias");
+    ED_REQUIRE(dtype == ED_F32 || dtype == ED_F64, "dtype must be ED_F32 or ED_F64");
+    if (dots) {
+        ED_REQUIRE(scratch != nullptr, "dots requested without scratch");
+        ED_REQUIRE(scratch_bytes >= ed_scratch_bytes(s->dim, 1), "scratch of %lld bytes is below the %lld needed",
+                   (long long)scratch_bytes, (long long)ed_scratch_bytes(s->dim, 1));
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (s->dim == 0) return ED_OK;
+    if (s->kind == ED_HUBBARD) {
+        ED_REQUIRE(ld >= s->nsup, "ld=%lld below nsup=%lld", (long long)ld, (long long)s->nsup);
+        if (dtype == ED_F32)
+            return hub_hv<float>(s, st, ld, static_cast<const float *>(x), static_cast<float *>(y), scale, dots,
+                                 static_cast<double *>(scratch));
+        return hub_hv<double>(s, st, ld, static_cast<const double *>(x), static_cast<double *>(y), scale, dots,
+                              static_cast<double *>(scratch));
+    }
+    if (dtype == ED_F32)
+        return heis_hv<float>(s, st, static_cast<const float *>(x), static_cast<float *>(y), scale, dots,
+                              static_cast<double *>(scratch));
+    return heis_hv<double>(s, st, static_cast<const double *>(x), static_cast<double *>(y), scale, dots,
+                           static_cast<double *>(scratch));
+}

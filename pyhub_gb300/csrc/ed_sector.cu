@@ -1,0 +1,430 @@
+// ed_sector.cu -- sector object: spin-string tables, gather-form hop tables,
+// diagonal terms and the Heisenberg rank tables; error state; basis and rank
+// entry points of the C ABI.
+//
+// Reference counterparts: HILBERT (compute_basis.f90:67-96) for the string
+// order, KINOP/ANTICOM (funcmod.f90:18-41) for hops and signs, the linear
+// search of hprod_hubbard.f90:41-47 for the rank, READ_INPUT
+// (compute_solver.f90:39-179) for the parameter tables.
+#include "ed_common.cuh"
+
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+namespace ed {
+
+static thread_local char g_err[1024] = "";
+
+void set_error(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+void clear_error() { g_err[0] = '\0'; }
+
+int num_sms()
+{
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 152;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 152;
+    return n > 0 ? n : 152;
+}
+
+// ------------------------------------------------------------ combinatorics
+
+static int64_t g_binom[kMaxSites + 2][kMaxSites + 2];
+static bool g_binom_ready = false;
+
+static void binom_init()
+{
+    if (g_binom_ready) return;
+    for (int n = 0; n <= kMaxSites + 1; ++n)
+        for (int k = 0; k <= kMaxSites + 1; ++k) {
+            if (k > n) g_binom[n][k] = 0;
+            else if (k == 0 || k == n) g_binom[n][k] = 1;
+            else g_binom[n][k] = g_binom[n - 1][k - 1] + g_binom[n - 1][k];
+        }
+    g_binom_ready = true;
+}
+
+static inline int64_t binom(int n, int k)
+{
+    if (n < 0 || k < 0 || n > kMaxSites + 1 || k > kMaxSites + 1) return 0;
+    return g_binom[n][k];
+}
+
+// Empty-site pattern of a string: bit j set when site j+1 is empty
+// (site POS lives in string bit norb-POS).
+static inline uint32_t holes_of(int norb, uint32_t s)
+{
+    uint32_t h = 0;
+    for (int j = 0; j < norb; ++j)
+        if (!((s >> (norb - 1 - j)) & 1u)) h |= 1u << j;
+    return h;
+}
+
+static inline uint32_t string_of_holes(int norb, uint32_t h)
+{
+    uint32_t s = 0;
+    for (int j = 0; j < norb; ++j)
+        if (!((h >> j) & 1u)) s |= 1u << (norb - 1 - j);
+    return s;
+}
+
+// The reference enumerates strings as k-subsets of bit positions in
+// lexicographic order.  That index equals the colex rank of the empty-site
+// pattern: sum over its set bits p_1 < p_2 < ... of C(p_i, i).
+static inline int64_t rank_host(int norb, uint32_t s)
+{
+    uint32_t h = holes_of(norb, s);
+    int64_t r = 0;
+    int i = 0;
+    for (int p = 0; p < norb; ++p)
+        if ((h >> p) & 1u) r += binom(p, ++i);
+    return r;
+}
+
+static void enumerate_strings(int norb, int ne, uint32_t *out, int64_t n)
+{
+    int m = norb - ne;  // holes
+    uint32_t h = (m >= 32) ? 0xFFFFFFFFu : ((1u << m) - 1u);
+    for (int64_t i = 0; i < n; ++i) {
+        out[i] = string_of_holes(norb, h);
+        if (h == 0) break;
+        // next pattern with the same popcount in increasing numeric (colex) order
+        uint32_t c = h & (0u - h);
+        uint32_t r = h + c;
+        h = (((r ^ h) >> 2) / c) | r;
+    }
+}
+
+// Fortran view T(J,K) of a row-major norb*norb buffer (1-based J,K).
+static inline double tf(const double *t, int norb, int J, int K) { return t[(K - 1) * norb + (J - 1)]; }
+
+static inline uint32_t site_bit(int norb, int pos) { return 1u << (norb - pos); }
+
+// Mask of the string bits of the sites strictly between sites a and b.
+static inline uint32_t between_mask(int norb, int a, int b)
+{
+    int lo = a < b ? a : b, hi = a < b ? b : a;
+    uint32_t m = 0;
+    for (int p = lo + 1; p < hi; ++p) m |= site_bit(norb, p);
+    return m;
+}
+
+// ------------------------------------------------------------ hop tables
+
+struct HostHop {
+    std::vector<uint32_t> str;
+    std::vector<int32_t> ptr, src;
+    std::vector<double> coef, ediag;
+};
+
+static int build_hop_host(int norb, int ne, const double *t, HostHop &h)
+{
+    int64_t n = binom(norb, ne);
+    h.str.resize((size_t)n);
+    enumerate_strings(norb, ne, h.str.data(), n);
+    h.ptr.resize((size_t)n + 1);
+    h.ediag.resize((size_t)n);
+    // active (J,K) pairs, J != K
+    std::vector<int> pj, pk;
+    std::vector<double> pt;
+    for (int K = 1; K <= norb; ++K)
+        for (int J = 1; J <= norb; ++J) {
+            if (J == K) continue;
+            double v = tf(t, norb, J, K);
+            if (std::fabs(v) >= kTol14) { pj.push_back(J); pk.push_back(K); pt.push_back(v); }
+        }
+    uint32_t between[kMaxSites * kMaxSites];
+    for (size_t a = 0; a < pj.size(); ++a) between[a] = between_mask(norb, pj[a], pk[a]);
+    h.src.clear();
+    h.coef.clear();
+    h.src.reserve((size_t)(n * (int64_t)std::min<size_t>(pj.size(), (size_t)ne * (norb - ne)) + 1));
+    h.coef.reserve(h.src.capacity());
+    for (int64_t p = 0; p < n; ++p) {
+        h.ptr[(size_t)p] = (int32_t)h.src.size();
+        uint32_t s = h.str[(size_t)p];
+        double dg = 0.0;
+        for (int J = 1; J <= norb; ++J) {
+            double v = tf(t, norb, J, J);
+            if ((s & site_bit(norb, J)) && std::fabs(v) >= kTol14) dg += v;
+        }
+        h.ediag[(size_t)p] = dg;
+        for (size_t a = 0; a < pj.size(); ++a) {
+            uint32_t bj = site_bit(norb, pj[a]), bk = site_bit(norb, pk[a]);
+            if (!(s & bk) || (s & bj)) continue;  // target needs K occupied, J empty
+            uint32_t q = s - bk + bj;
+            double sign = (__builtin_popcount(s & between[a]) & 1) ? -1.0 : 1.0;
+            h.src.push_back((int32_t)rank_host(norb, q));
+            h.coef.push_back(sign * pt[a]);
+        }
+        if (h.src.size() > (size_t)INT32_MAX) return ED_ERR_RANGE;
+    }
+    h.ptr[(size_t)n] = (int32_t)h.src.size();
+    return ED_OK;
+}
+
+template <typename T>
+static int upload(T **dst, const T *src, size_t count)
+{
+    *dst = nullptr;
+    if (count == 0) count = 1;  // keep a valid pointer for empty tables
+    cudaError_t e = cudaMalloc((void **)dst, count * sizeof(T));
+    if (e != cudaSuccess) {
+        set_error("cudaMalloc of %zu bytes for sector tables failed: %s", count * sizeof(T),
+                  cudaGetErrorString(e));
+        *dst = nullptr;
+        return ED_ERR_MEM;
+    }
+    if (src) {
+        e = cudaMemcpy(*dst, src, count * sizeof(T), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            set_error("cudaMemcpy to sector tables failed: %s", cudaGetErrorString(e));
+            return ED_ERR_CUDA;
+        }
+    }
+    return ED_OK;
+}
+
+static int upload_hop(const HostHop &h, int norb, int ne, HopTable &d)
+{
+    d.norb = norb;
+    d.ne = ne;
+    d.n = (int64_t)h.str.size();
+    d.nnz = (int64_t)h.src.size();
+    std::vector<float> c32(h.coef.begin(), h.coef.end());
+    int rc;
+    if ((rc = upload(&d.str, h.str.data(), h.str.size()))) return rc;
+    if ((rc = upload(&d.ptr, h.ptr.data(), h.ptr.size()))) return rc;
+    if ((rc = upload(&d.src, h.src.data(), h.src.size()))) return rc;
+    if ((rc = upload(&d.cf32, c32.data(), c32.size()))) return rc;
+    if ((rc = upload(&d.cf64, h.coef.data(), h.coef.size()))) return rc;
+    if ((rc = upload(&d.ediag, h.ediag.data(), h.ediag.size()))) return rc;
+    d.owner = true;
+    return ED_OK;
+}
+
+static void free_hop(HopTable &d)
+{
+    if (!d.owner) { d = HopTable(); return; }
+    cudaFree(d.str); cudaFree(d.ptr); cudaFree(d.src);
+    cudaFree(d.cf32); cudaFree(d.cf64); cudaFree(d.ediag);
+    d = HopTable();
+}
+
+// ------------------------------------------------------------ Heisenberg
+
+static int build_heis(ed_sector *s, const double *J)
+{
+    int norb = s->norb;
+    HeisTables &h = s->heis;
+    // byte-chunk colex tables: lut[b][c][x] = sum over set bits q of x, taken in
+    // increasing order with running index i = c+1, c+2, ..., of C(8b+q, i)
+    std::vector<uint32_t> lut(4 * 33 * 256, 0u);
+    for (int b = 0; b < 4; ++b)
+        for (int c = 0; c <= 32; ++c)
+            for (int x = 0; x < 256; ++x) {
+                int64_t r = 0;
+                int i = c;
+                for (int q = 0; q < 8; ++q)
+                    if ((x >> q) & 1) r += binom(8 * b + q, ++i);
+                lut[(b * 33 + c) * 256 + x] = (uint32_t)r;
+            }
+    int rc = upload(&h.lut, lut.data(), lut.size());
+    if (rc) return rc;
+    h.nbond = 0;
+    h.dconst = 0.0;
+    for (int a = 1; a <= norb; ++a) {
+        double jaa = tf(J, norb, a, a);
+        if (std::fabs(jaa) > kTol14) h.dconst += 0.5 * jaa;  // hprod_heis.f90:11-21
+        h.dconst += 0.25 * jaa;                              // Sz_J Sz_J J(J,J), :54-58
+    }
+    for (int a = 1; a <= norb; ++a)
+        for (int b = a + 1; b <= norb; ++b) {
+            double jab = tf(J, norb, a, b), jba = tf(J, norb, b, a);
+            if (jab == 0.0 && jba == 0.0) continue;
+            int k = h.nbond++;
+            h.bj[k] = (int8_t)a;
+            h.bk[k] = (int8_t)b;
+            // The four ANTICOM factors of hprod_heis.f90:39-45 reduce to
+            // (-1)^(J+K) for a complementary down string, so the element that
+            // moves the up spin J->K is -(-1)^(J+K) J(J,K) (when |J(J,K)|>tol).
+            double par = ((a + b) & 1) ? -1.0 : 1.0;
+            h.flip_jk[k] = (std::fabs(jab) > kTol14) ? -par * jab : 0.0;  // target: b up, a down
+            h.flip_kj[k] = (std::fabs(jba) > kTol14) ? -par * jba : 0.0;  // target: a up, b down
+            h.zz[k] = jab + jba;
+        }
+    return ED_OK;
+}
+
+}  // namespace ed
+
+using namespace ed;
+
+extern "C" {
+
+const char *ed_last_error(void) { return g_err; }
+
+int ed_version(void) { return 100; }
+
+int64_t ed_binom(int n, int k)
+{
+    binom_init();
+    if (n < 0 || k < 0 || k > n || n > kMaxSites) {
+        if (n > kMaxSites || n < 0) return -1;
+        return 0;
+    }
+    return binom(n, k);
+}
+
+int ed_basis(int norb, int ne, uint32_t *out, int64_t n)
+{
+    clear_error();
+    binom_init();
+    ED_REQUIRE(norb >= 1 && norb <= kMaxSites, "norb=%d outside 1..%d", norb, kMaxSites);
+    ED_REQUIRE(ne >= 0 && ne <= norb, "ne=%d outside 0..norb", ne);
+    ED_REQUIRE(out != nullptr, "out is NULL");
+    ED_REQUIRE(n == binom(norb, ne), "n=%lld but C(%d,%d)=%lld", (long long)n, norb, ne,
+               (long long)binom(norb, ne));
+    enumerate_strings(norb, ne, out, n);
+    return ED_OK;
+}
+
+int64_t ed_rank(int norb, int ne, uint32_t s)
+{
+    binom_init();
+    if (norb < 1 || norb > kMaxSites || ne < 0 || ne > norb) return -1;
+    if (norb < 32 && (s >> norb)) return -1;
+    if (__builtin_popcount(s) != ne) return -1;
+    return rank_host(norb, s);
+}
+
+int ed_sector_create(int norb, int nup, int ndn, int kind, const double *t, const double *U,
+                     const double *J, ed_sector **out)
+{
+    clear_error();
+    binom_init();
+    ED_REQUIRE(out != nullptr, "out is NULL");
+    *out = nullptr;
+    if (norb < 1 || norb > kMaxSites) {
+        set_error("norb=%d outside 1..%d", norb, kMaxSites);
+        return ED_ERR_RANGE;
+    }
+    ED_REQUIRE(kind == ED_HUBBARD || kind == ED_HEISENBERG, "unknown kind %d", kind);
+    ED_REQUIRE(nup >= 0 && nup <= norb && ndn >= 0 && ndn <= norb,
+               "particle numbers (%d,%d) outside 0..%d", nup, ndn, norb);
+    int64_t nsup = binom(norb, nup), nsdn = binom(norb, ndn);
+    if (nsup > INT32_MAX || nsdn > INT32_MAX) {
+        set_error("a spin species has more than 2^31 strings");
+        return ED_ERR_RANGE;
+    }
+    if (kind == ED_HEISENBERG) {
+        ED_REQUIRE(J != nullptr, "Heisenberg sector needs J");
+        if (ndn != 0 || nup != norb / 2) {
+            set_error("Heisenberg sector is (norb/2, 0) as in the reference, got (%d,%d)", nup, ndn);
+            return ED_ERR_ARG;
+        }
+    } else {
+        ED_REQUIRE(t != nullptr && U != nullptr, "Hubbard sector needs t and U");
+    }
+    ed_sector *s = new (std::nothrow) ed_sector();
+    if (!s) { set_error("host allocation failed"); return ED_ERR_MEM; }
+    s->kind = kind;
+    s->norb = norb;
+    s->nup = nup;
+    s->ndn = ndn;
+    s->nsup = nsup;
+    s->nsdn = nsdn;
+    s->dim = nsup * nsdn;
+    cudaGetDevice(&s->device);
+    int rc = ED_OK;
+    if (kind == ED_HUBBARD) {
+        for (int i = 0; i < norb * norb; ++i) {
+            if (!std::isfinite(t[i])) { delete s; set_error("t has a non-finite entry at %d", i); return ED_ERR_ARG; }
+            s->t_host[i] = t[i];
+        }
+        s->u_uniform = true;
+        s->u_value = U[0];
+        for (int p = 1; p <= norb; ++p) {
+            if (!std::isfinite(U[p - 1])) { delete s; set_error("U has a non-finite entry at %d", p - 1); return ED_ERR_ARG; }
+            s->u_site[norb - p] = U[p - 1];  // bit norb-p holds site p
+            if (U[p - 1] != U[0]) s->u_uniform = false;
+        }
+        HostHop hu;
+        rc = build_hop_host(norb, nup, t, hu);
+        if (!rc) rc = upload_hop(hu, norb, nup, s->up);
+        if (!rc) {
+            if (ndn == nup) {
+                s->dn = s->up;
+                s->dn.owner = false;
+            } else {
+                HostHop hd;
+                rc = build_hop_host(norb, ndn, t, hd);
+                if (!rc) rc = upload_hop(hd, norb, ndn, s->dn);
+            }
+        }
+    } else {
+        for (int i = 0; i < norb * norb; ++i) {
+            if (!std::isfinite(J[i])) { delete s; set_error("J has a non-finite entry at %d", i); return ED_ERR_ARG; }
+            s->j_host[i] = J[i];
+        }
+        rc = build_heis(s, J);
+    }
+    if (rc) {
+        std::string keep = g_err;
+        ed_sector_destroy(s);
+        set_error("%s", keep.c_str());
+        return rc;
+    }
+    *out = s;
+    return ED_OK;
+}
+
+int ed_sector_destroy(ed_sector *s)
+{
+    if (!s) return ED_OK;
+    free_hop(s->dn);
+    free_hop(s->up);
+    if (s->heis.lut) cudaFree(s->heis.lut);
+    delete s;
+    return ED_OK;
+}
+
+int ed_sector_dims(const ed_sector *s, int64_t *nsup, int64_t *nsdn, int64_t *dim)
+{
+    clear_error();
+    ED_REQUIRE(s != nullptr, "sector is NULL");
+    if (nsup) *nsup = s->nsup;
+    if (nsdn) *nsdn = s->nsdn;
+    if (dim) *dim = s->dim;
+    return ED_OK;
+}
+
+int ed_sector_strings(const ed_sector *s, uint32_t *up, uint32_t *dn)
+{
+    clear_error();
+    binom_init();
+    ED_REQUIRE(s != nullptr, "sector is NULL");
+    if (up) enumerate_strings(s->norb, s->nup, up, s->nsup);
+    if (dn) enumerate_strings(s->norb, s->ndn, dn, s->nsdn);
+    return ED_OK;
+}
+
+int ed_sector_nnz(const ed_sector *s, int64_t *nnz_up, int64_t *nnz_dn)
+{
+    clear_error();
+    ED_REQUIRE(s != nullptr, "sector is NULL");
+    if (nnz_up) *nnz_up = s->up.nnz;
+    if (nnz_dn) *nnz_dn = s->dn.nnz;
+    return ED_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,257 @@
+// ed_vec.cu -- Krylov-space vector kernels: many dot products in one pass
+// over the basis, and the projection update w - V c with its norm.
+//
+// These carry the Lanczos scalars of lanczos.f90:53-58 (DOT_PRODUCT, the
+// three-term update, NORM2) and the full reorthogonalisation that the
+// reference lacks (its LANCZOS_NORM, lanczos.f90:137-161, only measures the
+// loss).  FP32 vectors: products are formed and summed in FP32 over 16
+// elements per thread, every such partial is promoted to FP64 and all further
+// accumulation is FP64, so no FP64 multiply is spent per element.  FP64
+// vectors: FP64 throughout.
+#include "ed_common.cuh"
+
+namespace ed {
+
+int launch_reduce(const double *partials, int nblocks, int m, double *out, cudaStream_t st);
+
+static constexpr int kVecThreads = 256;
+static constexpr int kEPT = 16;                      // elements per thread per chunk
+static constexpr int kChunk = kVecThreads * kEPT;    // 4096 elements
+static constexpr int kMaxBlocks = 1024;
+
+template <typename T>
+__device__ __forceinline__ void load_chunk(T (&r)[kEPT], const T *__restrict__ p, int64_t base, int64_t n)
+{
+    // thread t owns elements base + t*4 + k*1024 + j (j<4), k < kEPT/4: float4 / double2x2 friendly
+#pragma unroll
+    for (int k = 0; k < kEPT / 4; ++k) {
+        const int64_t i = base + (int64_t)k * (kVecThreads * 4) + threadIdx.x * 4;
+        if (i + 3 < n) {
+            if constexpr (sizeof(T) == 4) {
+                const float4 v = __ldg(reinterpret_cast<const float4 *>(p + i));
+                r[4 * k] = v.x; r[4 * k + 1] = v.y; r[4 * k + 2] = v.z; r[4 * k + 3] = v.w;
+            } else {
+                const double2 v0 = __ldg(reinterpret_cast<const double2 *>(p + i));
+                const double2 v1 = __ldg(reinterpret_cast<const double2 *>(p + i + 2));
+                r[4 * k] = v0.x; r[4 * k + 1] = v0.y; r[4 * k + 2] = v1.x; r[4 * k + 3] = v1.y;
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) r[4 * k + j] = (i + j < n) ? __ldg(p + i + j) : (T)0;
+        }
+    }
+}
+
+// partials[block][j] (j < nvec) = sum over the block's chunks of <V_j, w>,
+// partials[block][nvec + j] the same with z (when z != NULL).
+template <typename T>
+__global__ void __launch_bounds__(kVecThreads) multidot_kernel(int64_t n, const T *__restrict__ V, int64_t ldv,
+                                                               int nvec, const T *__restrict__ w,
+                                                               const T *__restrict__ z,
+                                                               double *__restrict__ partials)
+{
+    extern __shared__ double acc[];  // [8 warps][m]
+    const int m = z ? 2 * nvec : nvec;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int j = threadIdx.x; j < 8 * m; j += blockDim.x) acc[j] = 0.0;
+    __syncthreads();
+    const int64_t nchunks = (n + kChunk - 1) / kChunk;
+    for (int64_t ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+        const int64_t base = ch * kChunk;
+        T rw[kEPT], rz[kEPT];
+        load_chunk<T>(rw, w, base, n);
+        if (z) load_chunk<T>(rz, z, base, n);
+        for (int j = 0; j < nvec; ++j) {
+            T rv[kEPT];
+            load_chunk<T>(rv, V + (int64_t)j * ldv, base, n);
+            T pw = 0, pz = 0;
+#pragma unroll
+            for (int k = 0; k < kEPT; ++k) pw += rv[k] * rw[k];
+            double sw = warp_sum((double)pw);
+            if (lane == 0) acc[warp * m + j] += sw;
+            if (z) {
+#pragma unroll
+                for (int k = 0; k < kEPT; ++k) pz += rv[k] * rz[k];
+                double sz = warp_sum((double)pz);
+                if (lane == 0) acc[warp * m + nvec + j] += sz;
+            }
+        }
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < m; j += blockDim.x) {
+        double s = 0.0;
+        for (int q = 0; q < 8; ++q) s += acc[q * m + j];
+        partials[(int64_t)blockIdx.x * m + j] = s;
+    }
+}
+
+// out = w - sum_j coef_j V_j (w may be NULL), optional partial <out,out>.
+// Accumulation type A: FP32 for an FP32 basis with FP32 output, FP64 otherwise.
+template <typename T, typename O, typename A>
+__global__ void __launch_bounds__(kVecThreads) update_kernel(int64_t n, const T *__restrict__ V, int64_t ldv,
+                                                             int nvec, const double *__restrict__ coef,
+                                                             const O *w, O *out, double *__restrict__ partials)
+{
+    extern __shared__ double cs_raw[];
+    A *cs = reinterpret_cast<A *>(cs_raw);
+    for (int j = threadIdx.x; j < nvec; j += blockDim.x) cs[j] = (A)coef[j];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double nrm = 0.0;
+    const int64_t nchunks = (n + kChunk - 1) / kChunk;
+    for (int64_t ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+        const int64_t base = ch * kChunk;
+        A r[kEPT];
+        if (w) {
+            O rw[kEPT];
+            load_chunk<O>(rw, w, base, n);
+#pragma unroll
+            for (int k = 0; k < kEPT; ++k) r[k] = (A)rw[k];
+        } else {
+#pragma unroll
+            for (int k = 0; k < kEPT; ++k) r[k] = (A)0;
+        }
+        for (int j = 0; j < nvec; ++j) {
+            T rv[kEPT];
+            load_chunk<T>(rv, V + (int64_t)j * ldv, base, n);
+            const A c = cs[j];
+#pragma unroll
+            for (int k = 0; k < kEPT; ++k) r[k] -= c * (A)rv[k];
+        }
+        O ro[kEPT];
+#pragma unroll
+        for (int k = 0; k < kEPT; ++k) ro[k] = (O)r[k];
+#pragma unroll
+        for (int k = 0; k < kEPT / 4; ++k) {
+            const int64_t i = base + (int64_t)k * (kVecThreads * 4) + threadIdx.x * 4;
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (i + j < n) out[i + j] = ro[4 * k + j];
+        }
+        if (partials) {
+            if constexpr (sizeof(O) == 4) {
+                float p = 0.f;
+#pragma unroll
+                for (int k = 0; k < kEPT; ++k) p += ro[k] * ro[k];
+                nrm += (double)p;
+            } else {
+#pragma unroll
+                for (int k = 0; k < kEPT; ++k) nrm += (double)ro[k] * (double)ro[k];
+            }
+        }
+    }
+    if (partials) {
+        __shared__ double red[8];
+        nrm = warp_sum(nrm);
+        if (lane == 0) red[warp] = nrm;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double s = 0.0;
+            for (int q = 0; q < 8; ++q) s += red[q];
+            partials[blockIdx.x] = s;
+        }
+    }
+}
+
+static int grid_for(int64_t n)
+{
+    int64_t nchunks = (n + kChunk - 1) / kChunk;
+    int64_t cap = (int64_t)num_sms() * 4;
+    if (cap > kMaxBlocks) cap = kMaxBlocks;
+    if (nchunks < cap) cap = nchunks;
+    return (int)(cap < 1 ? 1 : cap);
+}
+
+}  // namespace ed
+
+using namespace ed;
+
+extern "C" int ed_multidot(void *stream, int dtype, int64_t n, const void *V, int64_t ldv, int nvec, const void *w,
+                           const void *z, double *out, void *scratch, int64_t scratch_bytes)
+{
+    clear_error();
+    ED_REQUIRE(dtype == ED_F32 || dtype == ED_F64, "dtype must be ED_F32 or ED_F64");
+    ED_REQUIRE(n >= 0 && nvec >= 0, "negative size");
+    ED_REQUIRE(out != nullptr, "out is NULL");
+    if (nvec == 0 || n == 0) {
+        if (nvec > 0) ED_CHECK_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * (z ? 2 : 1) * nvec, (cudaStream_t)stream));
+        return ED_OK;
+    }
+    ED_REQUIRE(V != nullptr && w != nullptr, "V or w is NULL");
+    ED_REQUIRE(ldv >= n, "ldv=%lld below n=%lld", (long long)ldv, (long long)n);
+    const size_t esz = dtype == ED_F32 ? 4 : 8;
+    ED_REQUIRE((reinterpret_cast<uintptr_t>(V) % 16) == 0 && (reinterpret_cast<uintptr_t>(w) % 16) == 0 &&
+                   (!z || (reinterpret_cast<uintptr_t>(z) % 16) == 0) && ((ldv * esz) % 16) == 0,
+               "V, w, z and the vector stride must be 16-byte aligned");
+    ED_REQUIRE(scratch != nullptr && scratch_bytes >= ed_scratch_bytes(n, nvec),
+               "scratch of %lld bytes is below the %lld needed", (long long)scratch_bytes,
+               (long long)ed_scratch_bytes(n, nvec));
+    const int m = z ? 2 * nvec : nvec;
+    const size_t smem = sizeof(double) * 8 * (size_t)m;
+    ED_REQUIRE(smem <= 200 * 1024, "nvec=%d too large for one pass", nvec);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int grid = grid_for(n);
+    double *part = static_cast<double *>(scratch);
+    if (dtype == ED_F32) {
+        ED_CHECK_CUDA(cudaFuncSetAttribute(multidot_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        multidot_kernel<float><<<grid, kVecThreads, smem, st>>>(n, static_cast<const float *>(V), ldv, nvec,
+                                                               static_cast<const float *>(w),
+                                                               static_cast<const float *>(z), part);
+    } else {
+        ED_CHECK_CUDA(cudaFuncSetAttribute(multidot_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        multidot_kernel<double><<<grid, kVecThreads, smem, st>>>(n, static_cast<const double *>(V), ldv, nvec,
+                                                                static_cast<const double *>(w),
+                                                                static_cast<const double *>(z), part);
+    }
+    ED_CHECK_LAUNCH();
+    return launch_reduce(part, grid, m, out, st);
+}
+
+extern "C" int ed_update(void *stream, int dtype, int out_dtype, int64_t n, const void *V, int64_t ldv, int nvec,
+                         const double *coef, const void *w, void *out, double *norm2, void *scratch,
+                         int64_t scratch_bytes)
+{
+    clear_error();
+    ED_REQUIRE(dtype == ED_F32 || dtype == ED_F64, "dtype must be ED_F32 or ED_F64");
+    ED_REQUIRE(out_dtype == ED_F32 || out_dtype == ED_F64, "out_dtype must be ED_F32 or ED_F64");
+    ED_REQUIRE(n >= 0 && nvec >= 0, "negative size");
+    ED_REQUIRE(out != nullptr, "out is NULL");
+    ED_REQUIRE(nvec == 0 || (V != nullptr && coef != nullptr), "V or coef is NULL");
+    ED_REQUIRE(nvec == 0 || ldv >= n, "ldv=%lld below n=%lld", (long long)ldv, (long long)n);
+    const size_t esz = dtype == ED_F32 ? 4 : 8, osz = out_dtype == ED_F32 ? 4 : 8;
+    ED_REQUIRE((nvec == 0 || ((reinterpret_cast<uintptr_t>(V) % 16) == 0 && ((ldv * esz) % 16) == 0)) &&
+                   (reinterpret_cast<uintptr_t>(out) % 16) == 0 && (!w || (reinterpret_cast<uintptr_t>(w) % 16) == 0),
+               "V, w, out and the vector stride must be 16-byte aligned");
+    (void)osz;
+    ED_REQUIRE(nvec <= 8192, "nvec=%d too large", nvec);
+    if (norm2) {
+        ED_REQUIRE(scratch != nullptr && scratch_bytes >= ed_scratch_bytes(n, 1),
+                   "scratch of %lld bytes is below the %lld needed", (long long)scratch_bytes,
+                   (long long)ed_scratch_bytes(n, 1));
+    }
+    if (n == 0) return ED_OK;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int grid = grid_for(n);
+    double *part = norm2 ? static_cast<double *>(scratch) : nullptr;
+    const size_t smem = sizeof(double) * (size_t)(nvec > 0 ? nvec : 1);
+    if (dtype == ED_F32 && out_dtype == ED_F32) {
+        update_kernel<float, float, float><<<grid, kVecThreads, smem, st>>>(
+            n, static_cast<const float *>(V), ldv, nvec, coef, static_cast<const float *>(w),
+            static_cast<float *>(out), part);
+    } else if (dtype == ED_F32 && out_dtype == ED_F64) {
+        update_kernel<float, double, double><<<grid, kVecThreads, smem, st>>>(
+            n, static_cast<const float *>(V), ldv, nvec, coef, static_cast<const double *>(w),
+            static_cast<double *>(out), part);
+    } else if (dtype == ED_F64 && out_dtype == ED_F64) {
+        update_kernel<double, double, double><<<grid, kVecThreads, smem, st>>>(
+            n, static_cast<const double *>(V), ldv, nvec, coef, static_cast<const double *>(w),
+            static_cast<double *>(out), part);
+    } else {
+        update_kernel<double, float, double><<<grid, kVecThreads, smem, st>>>(
+            n, static_cast<const double *>(V), ldv, nvec, coef, static_cast<const float *>(w),
+            static_cast<float *>(out), part);
+    }
+    ED_CHECK_LAUNCH();
+    if (norm2) return launch_reduce(part, grid, 1, norm2, st);
+    return ED_OK;
+}

@@ -1,0 +1,62 @@
+"""CPU checks of the C-ABI library: it loads, exports every function that
+include/pyhub_ed.h declares, and its host-only entry points (basis
+enumeration, rank, argument validation) behave.  No kernel is launched."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = set()
+    for f in os.listdir(os.path.join(ROOT, "include")):
+        if f.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", f)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names |= set(re.findall(r"\b(ed_[a-z0-9_]+)\s*\(", src))
+    return names
+
+
+def test_library_exports_every_declared_symbol(edlib):
+    lib = ctypes.CDLL(os.path.join(ROOT, "pyhub_gb300", "libpyhub_ed.so"))
+    declared = _declared()
+    assert len(declared) >= 10
+    missing = [n for n in sorted(declared) if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+@pytest.mark.parametrize("no,ne", [(8, 4), (12, 5), (16, 8), (20, 10), (5, 0), (5, 5), (32, 1)])
+def test_basis_matches_oracle(edlib, no, ne):
+    b = edlib.basis(no, ne)
+    ref = O.hilbert(no, ne)
+    assert np.array_equal(b, ref)
+    for i in np.random.default_rng(0).choice(len(b), size=min(200, len(b)), replace=False):
+        assert edlib.rank(no, ne, int(b[i])) == i
+
+
+def test_binom_and_rank_edges(edlib):
+    assert edlib.binom(32, 16) == 601080390
+    assert edlib.rank(8, 4, 0b1111) == O.rank(8, 4, 0b1111)
+    assert edlib.rank(8, 4, 0b111) == -1          # wrong particle number
+    assert edlib.rank(8, 4, 0x1F0) == -1          # bits beyond norb
+
+
+def test_invalid_arguments_rejected_before_launch(edlib):
+    with pytest.raises(edlib.EDError) as e:
+        edlib.Sector(40, 2, 2, edlib.ED_HUBBARD, t=np.zeros((40, 40)), U=np.zeros(40))
+    assert e.value.code == edlib.ED_ERR_RANGE
+    with pytest.raises(edlib.EDError):
+        edlib.Sector(4, 2, 2, edlib.ED_HEISENBERG, J=np.zeros((4, 4)))  # sector must be (2, 0)
+    t = np.zeros((4, 4))
+    t[0, 1] = np.nan
+    with pytest.raises(edlib.EDError, match="non-finite"):
+        edlib.Sector(4, 2, 2, edlib.ED_HUBBARD, t=t, U=np.zeros(4))
+    L = edlib.lib()
+    assert L.ed_hv(None, None, 0, 0, None, None, 1.0, None, None, 0) == edlib.ED_ERR_ARG
+    assert "NULL" in L.ed_last_error().decode()

@@ -1,0 +1,195 @@
+"""CPU tests of the oracle: basis order, rank, and the sign conventions of
+the restated HPROD / RDM / GF routines against an independent Jordan-Wigner
+construction, plus physics identities.  No GPU."""
+import itertools
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+
+@pytest.mark.parametrize("no,ne", [(4, 2), (8, 4), (12, 6), (12, 5), (14, 7), (16, 8), (6, 0), (6, 6), (10, 3)])
+def test_hilbert_order_is_lexicographic_subsets(no, ne):
+    # compute_basis.f90 HILBERT enumerates subsets of bit positions in lexicographic order
+    assert np.array_equal(O.hilbert(no, ne), O.hilbert_py(no, ne))
+
+
+def test_hilbert_python_restatement_of_move_bmove():
+    """A line-by-line Python restatement of HILBERT/MOVE/BMOVE agrees with the C one."""
+    def move(s, posf):
+        a = 1 << (posf - 1)
+        return (s ^ a) ^ (1 << posf)
+
+    def bmove(no, s):
+        nsm = 0
+        while (s >> (no - nsm - 1)) & 1:
+            nsm += 1
+        sf = s - sum(1 << (no - i) for i in range(1, nsm + 1))
+        posle = no
+        while not (sf >> (posle - 1)) & 1:
+            posle -= 1
+        sf -= 1 << (posle - 1)
+        sm = sf + sum(1 << (posle - 1 + i) for i in range(1, nsm + 2))
+        return sm, posle + 1 + nsm
+
+    for no, ne in [(6, 3), (9, 4), (11, 5)]:
+        ns = O.binom(no, ne)
+        b = [sum(1 << (i - 1) for i in range(1, ne + 1))]
+        pos = ne
+        while len(b) < ns:
+            while pos < no and len(b) < ns:
+                b.append(move(b[-1], pos))
+                pos += 1
+            if len(b) < ns:
+                s, pos = bmove(no, b[-1])
+                b.append(s)
+        assert np.array_equal(np.array(b, dtype=np.uint32), O.hilbert(no, ne))
+
+
+@pytest.mark.parametrize("no,ne", [(8, 4), (12, 5), (14, 7), (16, 8), (20, 3)])
+def test_rank_inverts_hilbert(no, ne):
+    b = O.hilbert(no, ne)
+    idx = np.random.default_rng(0).choice(len(b), size=min(300, len(b)), replace=False)
+    for i in idx:
+        assert O.rank(no, ne, int(b[i])) == i
+
+
+def test_kinop_anticom_definitions():
+    # KINOP (funcmod.f90:18-27): site POS <-> bit NORB-POS
+    norb = 6
+    s = 0b101100  # sites 1,3,4 occupied
+    assert O.lib().orc_kinop(norb, s, 1, 2) == 0b011100
+    assert O.lib().orc_kinop(norb, s, 2, 5) == 0       # site 2 empty
+    assert O.lib().orc_kinop(norb, s, 1, 3) == 0       # site 3 occupied
+    assert O.lib().orc_kinop(norb, s, 3, 3) == s       # J==K occupied: diagonal
+    # ANTICOM: (-1)^(occupied sites before POS)
+    assert O.lib().orc_anticom(norb, 1, s) == 1.0
+    assert O.lib().orc_anticom(norb, 2, s) == -1.0
+    assert O.lib().orc_anticom(norb, 4, s) == 1.0
+    assert O.lib().orc_anticom(norb, 6, s) == -1.0
+
+
+HUB = [(2, 1, 1), (3, 1, 2), (4, 2, 2), (4, 1, 3), (5, 2, 3), (5, 3, 3), (6, 3, 3), (6, 2, 4), (6, 0, 2)]
+
+
+@pytest.mark.parametrize("case", HUB)
+@pytest.mark.parametrize("sym", [True, False])
+def test_hubbard_restatement_equals_jordan_wigner(case, sym):
+    n, nu, nd = case
+    rng = np.random.default_rng(n * 7 + nu)
+    t = rng.standard_normal((n, n))
+    if sym:
+        t = t + t.T
+    U = rng.uniform(0, 5, n)
+    sec = O.Sector(n, nu, nd)
+    H_or = O.dense_h(lambda v: O.hprod_hubbard(sec, t, U, v), sec.dim)
+    H_jw = O.jw_hubbard_sector(sec, t, U)
+    assert np.abs(H_or - H_jw).max() <= 1e-13 * max(1.0, np.abs(H_jw).max())
+
+
+@pytest.mark.parametrize("case", [(4, 2, 2), (6, 3, 3), (7, 3, 2), (8, 4, 4)])
+def test_fast_hprod_equals_reference_loop(case):
+    n, nu, nd = case
+    rng = np.random.default_rng(1)
+    t = rng.standard_normal((n, n))
+    t = t + t.T
+    U = rng.uniform(0, 5, n)
+    sec = O.Sector(n, nu, nd)
+    x = rng.standard_normal(sec.dim)
+    a = O.hprod_hubbard(sec, t, U, x)
+    b = O.hprod_hubbard(sec, t, U, x, fast=True, nthreads=2)
+    assert np.linalg.norm(a - b) <= 1e-14 * np.linalg.norm(a)
+
+
+def test_pair_sample_sums_to_full_product():
+    n, nu, nd = 6, 3, 2
+    t = O.ring(n)
+    sec = O.Sector(n, nu, nd)
+    x = np.random.default_rng(2).standard_normal(sec.dim)
+    full = O.hprod_hubbard(sec, t, 0.0, x)
+    y = np.zeros(sec.dim)
+    pairs = [(J, K) for J in range(1, n + 1) for K in range(1, n + 1)]
+    O.hprod_hubbard_pairs(sec, t, pairs, x, y)
+    assert np.allclose(y, full, rtol=0, atol=1e-13)
+
+
+@pytest.mark.parametrize("n", [2, 4, 6])
+def test_heisenberg_restatement_equals_jordan_wigner(n):
+    rng = np.random.default_rng(n)
+    J = rng.standard_normal((n, n))
+    J = J + J.T
+    H_or = O.dense_h(lambda v: O.hprod_heis(n, J, v), O.binom(n, n // 2))
+    H_jw = O.jw_heis_sector(n, J)
+    assert np.abs(H_or - H_jw).max() <= 1e-13 * np.abs(H_jw).max()
+    x = rng.standard_normal(len(H_or))
+    assert np.allclose(O.hprod_heis(n, J, x, fast=True), H_or @ x, rtol=0, atol=1e-12)
+
+
+def test_heisenberg_spectrum_bipartite_vs_triangle():
+    """hprod_heis.f90:44-45 pairs ANTICOM(J,dn)*ANTICOM(K,new_dn) with the down
+    hop K->J, which flips the sign of the transverse exchange.  On bipartite
+    clusters that is a sublattice gauge transformation (same spectrum as the
+    physical sum_JK J_JK S_J.S_K); on a triangle it is not."""
+    for n in (4, 6):
+        J = O.ring(n, 1.0)
+        a = np.linalg.eigvalsh(O.jw_heis_sector(n, J))
+        b = np.linalg.eigvalsh(O.jw_heis_sector(n, J, physical=True))
+        assert np.allclose(a, b, atol=1e-12)
+    J = np.ones((3, 3)) - np.eye(3)
+    a = np.linalg.eigvalsh(O.jw_heis_sector(3, J))
+    b = np.linalg.eigvalsh(O.jw_heis_sector(3, J, physical=True))
+    assert not np.allclose(a, b)
+
+
+def test_c1_ring_identities():
+    """L=8 ring, U=4: reference-rule Lanczos = dense ED; Tr gamma = N;
+    sum t gamma + sum U <n n> = E0 on the exact eigenvector; S^2 = 0."""
+    sec = O.Sector(8, 4, 4)
+    t, U = O.ring(8), 4.0
+    H = O.dense_h(lambda v: O.hprod_hubbard(sec, t, U, v, fast=True), sec.dim)
+    val, vec, ndeg = O.exact_diag(H)
+    assert ndeg == 1
+    v0 = np.random.default_rng(0).uniform(-0.5, 0.5, sec.dim)
+    r = O.lanczos_ref(lambda v: O.hprod_hubbard(sec, t, U, v, fast=True), v0, 600, 1e-8)
+    assert r["converged"] and abs(r["eigenvalues"][0] - val[0]) < 1e-9
+    psi = vec[:, 0]
+    g = O.one_rdm(sec, psi)
+    assert abs(np.trace(g["up"]) - 4) < 1e-12 and abs(np.trace(g["down"]) - 4) < 1e-12
+    ni = O.two_rdm_ni(sec, psi)
+    e = np.sum(t * (g["up"] + g["down"])) + U * ni.sum()
+    assert abs(e - val[0]) < 1e-11
+    sm = O.j_spin(sec, psi)
+    assert abs(sm.sum()) < 1e-10
+    assert np.allclose(sm, sm.T)
+
+
+def test_gf_start_vectors_match_jordan_wigner():
+    """LCZ_{H,E}_{UP,DOWN} start vectors equal c|psi> / c^+|psi> built in the
+    Fock space with down modes ordered before up modes."""
+    from oracle.oracle import _fock_index, _jw_ops
+    n, nu, nd = 4, 2, 1
+    sec = O.Sector(n, nu, nd)
+    rng = np.random.default_rng(4)
+    psi = rng.standard_normal(sec.dim)
+    c = _jw_ops(2 * n)
+    fock = np.zeros(1 << (2 * n))
+    idx = [_fock_index(n, int(u), int(d)) for d in sec.bdn for u in sec.bup]
+    fock[idx] = psi
+    for kind in ("h_up", "h_down", "e_up", "e_down"):
+        sec1, st = O.gf_start(kind, sec, n, psi)
+        idx1 = [_fock_index(n, int(u), int(d)) for d in sec1.bdn for u in sec1.bup]
+        for pos in range(1, n + 1):
+            mode = (n + pos - 1) if kind.endswith("up") else (pos - 1)
+            op = c[mode] if kind.startswith("h") else c[mode].T
+            out = op @ fock
+            assert np.allclose(out[idx1], st[pos - 1], atol=1e-14)
+
+
+def test_boltzmann_zero_temperature():
+    w = O.boltzmann(np.array([-3.0, -2.0, -1.0]), 0.0, 1)
+    assert np.array_equal(w, [1.0])
+    w = O.boltzmann(np.array([-3.0, -2.0, -1.0]), 0.0, 2)
+    assert np.array_equal(w, [1.0, 0.0])
+    w = O.boltzmann(np.array([-3.0, -2.9, 50.0]), 1.0, 1)
+    assert len(w) == 2 and np.allclose(w, [1.0, np.exp(-0.1)])
