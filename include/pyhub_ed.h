@@ -115,6 +115,32 @@ int ed_update(void *stream, int dtype, int out_dtype, int64_t n, const void *V, 
               const double *coef, const void *w, void *out, double *norm2,
               void *scratch, int64_t scratch_bytes);
 
+/* Device scratch bytes needed by ed_rdm for npairs site pairs. */
+int64_t ed_rdm_scratch_bytes(int npairs);
+
+/* Raw reduced-density sums of <bra| ... |ket> for a list of site pairs
+ * (pairs: host int32 [2*npairs], 1-based (J,K)).  Replaces ONE_RDM,
+ * the local-U branch of TWO_RDM and J_SPIN (static_rq.f90:153-395) and the
+ * Heisenberg J_SPIN (static_rq_heis.f90:58-116).  out (device FP64,
+ * [npairs][6] for Hubbard followed by nothing, [npairs][2] for Heisenberg):
+ *   Hubbard    q0: J!=K up hop J->K bra.ket sum / J==K <n_up>;  q1: <Sz_J Sz_K>;
+ *              q2: J==K <n_down>;  q3: J==K <n_up n_down>;
+ *              q4: J!=K down hop J->K (flags bit 0);
+ *              q5: J!=K transverse spin term of J_SPIN (flags bit 1)
+ *              (q0..q3 of all pairs come first, then q4,q5 of all pairs);
+ *   Heisenberg q0: J!=K transverse term / J==K 0.5<1>;  q1: <Sz_J Sz_K>. */
+int ed_rdm(ed_sector *s, void *stream, int dtype, int64_t ld, const void *bra, const void *ket,
+           int npairs, const int32_t *pairs, int flags, double *out, void *scratch, int64_t scratch_bytes);
+
+/* Green's-function start vector out = c_{site,s}|psi> (kind 0: up, 1: down)
+ * or c^+_{site,s}|psi> (kind 2: up, 3: down), site 1-based, psi in sector src
+ * (row stride ld0), out in sector dst (row stride ld1, written entirely).
+ * Replaces LCZ_H_UP/LCZ_H_DOWN/LCZ_E_UP/LCZ_E_DOWN
+ * (spgf_bandlanczos.f90:453-560), including their sign (-1)^N_down on the up
+ * operators. */
+int ed_gf_start(const ed_sector *src, const ed_sector *dst, void *stream, int kind, int site,
+                int dtype, int64_t ld0, const void *psi, int out_dtype, int64_t ld1, void *out);
+
 #ifdef __cplusplus
 }
 #endif

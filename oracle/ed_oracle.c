@@ -268,6 +268,21 @@ void orc_hprod_hubbard_ref_pairs(int norb, int nup, int ndn,
     }
 }
 
+/* The on-site U part of the reference loop for one site J only
+ * (hprod_hubbard.f90:27-35), adding into y: the bounded sample used with
+ * orc_hprod_hubbard_ref_pairs to time the reference loop on large sectors. */
+void orc_hprod_hubbard_ref_udiag(int norb, const uint32_t *bup, int64_t nsup,
+                                 const uint32_t *bdn, int64_t nsdn, int J, double uj,
+                                 const double *x, double *y)
+{
+    for (int64_t u = 0; u < nsup; ++u) {
+        if (!is_part(norb, J, bup[u])) continue;
+        for (int64_t d = 0; d < nsdn; ++d)
+            if (is_part(norb, J, bdn[d]))
+                y[d * nsup + u] = y[d * nsup + u] + x[d * nsup + u] * uj;
+    }
+}
+
 /* ---------------------------------------- Heisenberg H*v, reference order --- */
 
 /* Restatement of HPROD for the Sz=0 Heisenberg sector (hprod_heis.f90:1-61):

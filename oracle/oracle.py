@@ -73,6 +73,7 @@ def lib():
             L.orc_anticom.argtypes = [i32, i32, ctypes.c_uint32]
             L.orc_hprod_hubbard_ref.argtypes = [i32, i32, i32, P, i64, P, i64, P, P, P, P]
             L.orc_hprod_hubbard_ref_pairs.argtypes = [i32, i32, i32, P, i64, P, i64, P, P, i32, P, P]
+            L.orc_hprod_hubbard_ref_udiag.argtypes = [i32, P, i64, P, i64, i32, ctypes.c_double, P, P]
             L.orc_hprod_hubbard_fast.argtypes = [i32, i32, i32, P, i64, P, i64, P, P, P, P, i32]
             L.orc_hprod_heis_ref.argtypes = [i32, P, i64, P, P, P]
             L.orc_hprod_heis_fast.argtypes = [i32, P, i64, P, P, P, i32]
@@ -155,6 +156,12 @@ def hprod_hubbard_pairs(sec: Sector, t, pairs, x, y) -> None:
     pr = np.ascontiguousarray(np.asarray(pairs, dtype=np.int32).reshape(-1, 2))
     lib().orc_hprod_hubbard_ref_pairs(sec.norb, sec.nup, sec.ndn, _p(sec.bup), sec.nsup, _p(sec.bdn),
                                       sec.nsdn, _p(t), _p(pr), len(pr), _p(x), _p(y))
+
+
+def hprod_hubbard_udiag(sec: Sector, J: int, uj: float, x, y) -> None:
+    """U term of the reference loop for site J (1-based) only, adds into y."""
+    lib().orc_hprod_hubbard_ref_udiag(sec.norb, _p(sec.bup), sec.nsup, _p(sec.bdn), sec.nsdn, int(J), float(uj),
+                                      _p(x), _p(y))
 
 
 def heis_sector(norb: int) -> Sector:

@@ -35,7 +35,12 @@ _SIGS = {
     "ed_hv": (_I, [_P, _P, _I, _I64, _P, _P, _D, _P, _P, _I64]),
     "ed_multidot": (_I, [_P, _I, _I64, _P, _I64, _I, _P, _P, _P, _P, _I64]),
     "ed_update": (_I, [_P, _I, _I, _I64, _P, _I64, _I, _P, _P, _P, _P, _P, _I64]),
+    "ed_rdm_scratch_bytes": (_I64, [_I]),
+    "ed_rdm": (_I, [_P, _P, _I, _I64, _P, _P, _I, _P, _I, _P, _P, _I64]),
+    "ed_gf_start": (_I, [_P, _P, _P, _I, _I, _I, _I64, _P, _I, _I64, _P]),
 }
+
+GF_KINDS = {"h_up": 0, "h_down": 1, "e_up": 2, "e_down": 3}
 
 _bound = None
 
@@ -197,12 +202,43 @@ class Sector:
         return out
 
     # -------------------------------------------------------- products
+    def rdm_raw(self, bra, ket=None, pairs=None, flags: int = 3, ld: int | None = None, stream=None):
+        """Raw per-pair sums of ed_rdm as a host float64 array
+        ([npairs, 6] for Hubbard, [npairs, 2] for Heisenberg) and the pair list."""
+        import torch
+        ket = bra if ket is None else ket
+        if pairs is None:
+            pairs = [(J, K) for J in range(1, self.norb + 1) for K in range(1, self.norb + 1)]
+        pr = np.ascontiguousarray(np.asarray(pairs, dtype=np.int32).reshape(-1, 2))
+        npairs = len(pr)
+        nq = 6 if self.kind == ED_HUBBARD else 2
+        out = torch.zeros(nq * npairs, dtype=torch.float64, device=bra.device)
+        nb = int(lib().ed_rdm_scratch_bytes(npairs))
+        scratch = torch.empty((nb + 7) // 8, dtype=torch.float64, device=bra.device)
+        ld = self.ld if ld is None else ld
+        check("ed_rdm", lib().ed_rdm(self._h, _stream(stream), dtype_code(bra.dtype), int(ld), _ptr(bra), _ptr(ket),
+                                     npairs, pr.ctypes.data, int(flags), _ptr(out), _ptr(scratch), nb))
+        o = out.cpu().numpy()
+        if self.kind == ED_HUBBARD:
+            raw = np.concatenate([o[: 4 * npairs].reshape(npairs, 4), o[4 * npairs:].reshape(npairs, 2)], axis=1)
+        else:
+            raw = o.reshape(npairs, 2)
+        return raw, pr
+
     def hv(self, x, y, scale: float = 1.0, dots=None, scratch=None, ld: int | None = None, stream=None):
         """y = scale * H x (device tensors in the internal layout unless ld is given)."""
         ld = self.ld if ld is None else ld
         sb = 0 if scratch is None else scratch.numel() * scratch.element_size()
         check("ed_hv", lib().ed_hv(self._h, _stream(stream), dtype_code(x.dtype), int(ld), _ptr(x), _ptr(y),
                                    float(scale), _ptr(dots), _ptr(scratch), int(sb)))
+
+
+def gf_start(src: "Sector", dst: "Sector", kind: str, site: int, psi, out, stream=None):
+    """out = c_{site}|psi> or c^+_{site}|psi> (kind 'h_up','h_down','e_up','e_down'),
+    both vectors in their sectors' internal layouts."""
+    check("ed_gf_start", lib().ed_gf_start(src.handle, dst.handle, _stream(stream), GF_KINDS[kind], int(site),
+                                           dtype_code(psi.dtype), src.ld, _ptr(psi), dtype_code(out.dtype), dst.ld,
+                                           _ptr(out)))
 
 
 def multidot(V, nvec: int, w, out, scratch, z=None, n: int | None = None, stream=None):

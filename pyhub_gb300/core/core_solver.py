@@ -1,0 +1,373 @@
+"""CoreSolver with the reference's API (pyhub/core/core_solver.py:17-291).
+
+The reference marshals every parameter into solver.h5, runs a Fortran
+executable with os.system and reads results back lazily
+(core_solver.py:31-111, 118-249).  Here ``kernel`` runs in process on the
+GPU through the C ABI and keeps results in memory; the property names,
+signatures and return shapes are the reference's.
+
+Solve dispatch follows SOLVE (solve.f90:1-23): a sector smaller than
+``max_lcz`` is diagonalised densely (EXACT_DIAG, exact_diag.f90:2-33, its
+columns built with the GPU H*v), a larger one with Lanczos under the
+reference's convergence rule (lanczos.f90:44-91) at most max_lcz-5 steps.
+Extra keyword arguments select the precision ("f64", "mixed" = FP32 vectors
+with FP64 scalars and an FP64 refinement, "auto") and the
+reorthogonalisation ("full" when the basis fits in device memory, else the
+reference's three-term recurrence with the Ritz vector rebuilt by a second
+pass instead of being read back from stored vectors).
+"""
+from __future__ import annotations
+
+import math
+from copy import deepcopy as dc
+from time import perf_counter as pc
+
+import numpy as np
+
+from .. import _capi
+from . import lanczos as LZ
+from .basis import Basis
+from .reduced_quantities import (GreenFunction, StaticQuantities, all_pairs, assemble_heisenberg,
+                                 assemble_hubbard)
+
+F32_TOL14 = float(np.float32(1e-14))
+F32_TOL8 = float(np.float32(1e-8))
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("pyhub_gb300 runs on a CUDA GPU; no device is visible")
+    return torch
+
+
+class CoreSolver(Basis, GreenFunction, StaticQuantities):
+
+    def __init__(self, nb_sites, n_up: int, n_down: int, exec_name, T=0., order='spin'):
+        Basis.__init__(self, nb_sites, hilbert=(n_up, n_down), order=order)
+        self.T = T
+        self.exec_name = exec_name
+        self.t_matrix = np.zeros((nb_sites, nb_sites))
+        self.J_matrix = np.zeros((nb_sites, nb_sites))
+        self.U = 0.
+        self.is_solve = False
+        self.is_reduced_quantities = False
+        self.is_spgf = False
+        self.is_tprf = False
+        self.excited_state = 0
+        self._sol = None
+        self._rq = None
+        self._spgf = None
+        self._sectors = {}
+
+    # ----------------------------------------------------------- sectors
+    @property
+    def _kind(self):
+        return _capi.ED_HEISENBERG if self.exec_name == 'heisenberg.x' else _capi.ED_HUBBARD
+
+    def _u_vector(self):
+        U = self.U
+        if isinstance(U, (float, int, np.floating, np.integer)):
+            return np.full(self.nb_sites, float(U))
+        U = np.asarray(U, dtype=np.float64)
+        if U.ndim == 1 and U.shape == (self.nb_sites,):
+            return U
+        if U.ndim == 4:
+            raise NotImplementedError("the U_ijkl interaction (is_Uloc=3) is not built")
+        raise ValueError(f'U must be a float or a np.ndarray of size (nb_sites,) or '
+                         f'(nb_sites,nb_sites,nb_sites,nb_sites,), not {type(self.U)}')
+
+    def sector(self, nup: int, ndn: int):
+        key = (int(nup), int(ndn))
+        if key not in self._sectors:
+            if self._kind == _capi.ED_HUBBARD:
+                self._sectors[key] = _capi.Sector(self.nb_sites, nup, ndn, _capi.ED_HUBBARD,
+                                                  t=np.asarray(self.t_matrix, dtype=np.float64), U=self._u_vector())
+            else:
+                self._sectors[key] = _capi.Sector(self.nb_sites, nup, ndn, _capi.ED_HEISENBERG,
+                                                  J=np.asarray(self.J_matrix, dtype=np.float64))
+        return self._sectors[key]
+
+    # ----------------------------------------------------------- solve
+    def kernel(self, max_lcz: int = 600, acc_lcz: float = 1.e-8, nb_comp_states=1, compute_rq=True,
+               compute_spgf=False, nb_sites_comp=None, store_H=False, verbose=False, *, dtype: str = "auto",
+               reorth: str = "auto", seed: int = 0, refine_steps: int = 60):
+        torch = _torch()
+        self.max_lcz = max_lcz
+        self.acc_lcz = acc_lcz
+        self.compute_rq = compute_rq
+        self.nb_comp_states_ = nb_comp_states
+        self.compute_spgf = compute_spgf
+        self.compute_tprf = False
+        self.store_H = store_H
+        self.verbose = verbose
+        self.nb_sites_comp = self.nb_sites if nb_sites_comp is None else nb_sites_comp
+        tall = pc()
+        self._sectors = {}
+        self._rq = None
+        self._spgf = None
+        sec = self.sector(self.nup[0], self.ndown[0])
+        self.printv('start calculation')
+        if sec.dim < max_lcz:
+            self._sol = self._exact_diag(sec, store_H)
+        else:
+            self._sol = self._lanczos(sec, max_lcz, acc_lcz, nb_comp_states, dtype, reorth, seed, refine_steps)
+        self._sol["boltzmann"] = self._boltzmann(self._sol["eigenvalues"], nb_comp_states)
+        self.is_solve = True
+        self.wgt = dc(self.boltzmann)
+        torch.cuda.synchronize()
+        if compute_rq:
+            self.reduced_quantities()
+        if compute_spgf:
+            self.spgf(nb_sites_comp=self.nb_sites_comp)
+        self.time = pc() - tall
+        self.printv(f'total elapsed time {np.around(self.time, 4)} s\n')
+
+    def _exact_diag(self, sec, store_H):
+        torch = _torch()
+        D = sec.dim
+        cols = torch.zeros((D, sec.n), dtype=torch.float64, device="cuda")
+        e = torch.zeros(sec.n, dtype=torch.float64, device="cuda")
+        eref = sec.to_ref(torch.arange(sec.n, device="cuda", dtype=torch.float64))
+        pos = eref.long()  # internal position of reference index i
+        for i in range(D):
+            e.zero_()
+            e[pos[i]] = 1.0
+            sec.hv(e, cols[i])
+        H = sec.to_ref(cols).T.contiguous().cpu().numpy()  # H[:, i] = H e_i
+        val, vec = np.linalg.eigh(H)
+        ndeg = 1
+        for i in range(1, len(val)):
+            if abs(val[i] - val[0]) < F32_TOL14:
+                ndeg += 1
+            else:
+                break
+        return {"eigenvalues": val, "eigenvectors_ref": vec, "is_lanczos": False, "deg": ndeg,
+                "H": H if store_H else None, "nstates": D}
+
+    def _lanczos(self, sec, max_lcz, acc_lcz, nb_comp_states, dtype, reorth, seed, refine_steps):
+        torch = _torch()
+        steps = max(max_lcz - 5, 5)
+        if dtype == "auto":
+            dtype = "f64" if (sec.dim <= (1 << 22) or nb_comp_states > 1 or self.T > F32_TOL8) else "mixed"
+        if dtype not in ("f64", "mixed", "f32"):
+            raise ValueError(f"dtype must be 'auto', 'f64', 'mixed' or 'f32', not {dtype}")
+        esz = 8 if dtype == "f64" else 4
+        free, _ = torch.cuda.mem_get_info()
+        fits = (steps + 3) * sec.n * esz <= 0.8 * free
+        if reorth == "auto":
+            reorth = "full" if fits else "none"
+        v0 = LZ.start_vector(sec, seed)
+        rule = LZ.ReferenceRule(acc_lcz)
+        nvec = max(1, int(nb_comp_states))
+        if reorth == "full":
+            if dtype == "f64":
+                r = LZ.lanczos_full(sec, v0, steps, torch.float64, rule=rule, want_vector=False, keep_basis=True)
+                psis = [r.ritz_vector(k) for k in range(min(nvec, r.steps))]
+                ritz, alpha, beta, steps_done, conv = r.ritz, r.alpha, r.beta, r.steps, r.converged
+                r.release()
+            else:
+                r = LZ.lanczos_full(sec, v0.to(torch.float32), steps, torch.float32, rule=rule)
+                e32 = float(r.ritz[0])
+                psi = r.psi
+                r.release()
+                if dtype == "mixed":
+                    rr = LZ.EnergyRule(1e-13 * max(1.0, abs(e32)), min_steps=10)
+                    r2 = LZ.lanczos_full(sec, psi, refine_steps, torch.float64, rule=rr)
+                    psi = r2.psi
+                    ritz = np.concatenate([[r2.ritz[0]], r.ritz[1:]])
+                    r2.release()
+                else:
+                    ritz = r.ritz
+                psis = [psi]
+                alpha, beta, steps_done, conv = r.alpha, r.beta, r.steps, r.converged
+        else:
+            vt = torch.float64 if dtype == "f64" else torch.float32
+            r = LZ.lanczos_plain(sec, v0.to(vt), steps, rule=rule, nvec=nvec)
+            psis = r.psis
+            ritz, alpha, beta, steps_done, conv = r.ritz, r.alpha, r.beta, r.steps, r.converged
+        return {"eigenvalues": np.asarray(ritz), "psis": psis, "is_lanczos": True, "deg": rule.ndeg,
+                "alpha": alpha, "beta": beta, "nb_lcz": steps_done, "conv": rule.conv,
+                "converged": conv, "H": None, "nstates": sec.dim, "precision": dtype, "reorth": reorth}
+
+    def _boltzmann(self, val, nb_comp_states):
+        """BOLTZMANN (boltzmann.f90:1-29)."""
+        T = self.T
+        nval = len(val)
+        nw = nval + 1
+        with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+            for k in range(2, nval + 1):
+                if np.exp((val[0] - val[k - 1]) / T) <= F32_TOL8:
+                    nw = k
+                    break
+        nw = max(nw - 1, nb_comp_states)
+        w = np.zeros(nw)
+        if T >= F32_TOL8:
+            w[:] = np.exp((val[0] - val[:nw]) / T)
+        else:
+            w[0] = 1.0
+        return w
+
+    def set_state(self, excited_state=-1):
+        self.excited_state = excited_state
+        self.wgt = dc(self.boltzmann)
+        if excited_state != -1:
+            self.wgt[:] = 0.
+            self.wgt[excited_state] = 1.
+
+    # ----------------------------------------------------------- states
+    def _state_device(self, k: int):
+        """State k (FP64, internal layout of the solve sector)."""
+        torch = _torch()
+        sec = self.sector(self.nup[0], self.ndown[0])
+        if not self._sol["is_lanczos"]:
+            v = torch.tensor(self._sol["eigenvectors_ref"][:, k], dtype=torch.float64, device="cuda")
+            return sec.from_ref(v)
+        psis = self._sol["psis"]
+        if k >= len(psis) or psis[k] is None:
+            raise IndexError(f"state {k} was not kept; raise nb_comp_states in kernel()")
+        return psis[k]
+
+    def reduced_quantities(self):
+        t0 = pc()
+        self.printv('start reduced quantities calculation')
+        sec = self.sector(self.nup[0], self.ndown[0])
+        nw = len(self.wgt)
+        N = self.nb_sites
+        dm_up = np.zeros((nw, N, N))
+        dm_dn = np.zeros((nw, N, N))
+        ni = np.zeros((nw, N))
+        sisj = np.zeros((nw, N, N))
+        for b in range(nw):
+            if self.wgt[b] == 0.0 and b > 0:
+                continue
+            psi = self._state_device(b)
+            if self._kind == _capi.ED_HUBBARD:
+                flags = 2 | (1 if self.nup[0] != self.ndown[0] else 0)
+                raw, _ = sec.rdm_raw(psi, pairs=all_pairs(N), flags=flags)
+                gu, gd, n_, sm = assemble_hubbard(raw, N, self.nup[0], self.ndown[0])
+                dm_up[b], dm_dn[b], ni[b], sisj[b] = gu, gd, n_, sm
+            else:
+                raw, _ = sec.rdm_raw(psi, pairs=all_pairs(N))
+                sisj[b] = assemble_heisenberg(raw, N)
+        self._rq = {"density_matrix_up": dm_up, "density_matrix_down": dm_dn, "ni": ni, "sisj": sisj}
+        self.is_reduced_quantities = True
+        self.printv(f'end calculation | elapsed time {np.around(pc() - t0, 4)} s')
+
+    def spgf(self, nb_sites_comp=None, nsteps: int = None, offdiag: bool = True):
+        from . import greens as GR
+        self.nb_sites_comp = self.nb_sites if nb_sites_comp is None else nb_sites_comp
+        if self._kind != _capi.ED_HUBBARD:
+            raise NotImplementedError("Green's functions are defined for the Hubbard solver")
+        if self.T > F32_TOL8 and self._sol["is_lanczos"]:
+            raise ValueError('SET TEMPERATURE TO 0 FOR LANCZOS GF')
+        t0 = pc()
+        self.printv('start spgf calculation')
+        out = []
+        for b in range(len(self.wgt)):
+            if self.wgt[b] == 0.0 and b > 0:
+                out.append(None)
+                continue
+            out.append(GR.particle_hole_poles(self, self._state_device(b), float(self.e[b]), self.nb_sites_comp,
+                                              nsteps=nsteps, offdiag=offdiag))
+        self._spgf = out
+        self.is_spgf = True
+        self.printv(f'end calculation | elapsed time {np.around(pc() - t0, 4)} s')
+        self.gf = self.compute_gf()
+
+    def tprf(self):
+        pass
+
+    def printv(self, *args):
+        if self.verbose:
+            print(*args)
+
+    # ----------------------------------------------------------- properties
+    @property
+    def filename(self):
+        return 'solver.h5'
+
+    @property
+    def boltzmann(self):
+        return np.array(self._sol["boltzmann"], dtype=float)
+
+    @property
+    def Z(self):
+        return np.sum(self.wgt)
+
+    @property
+    def nb_deg(self):
+        return self._sol["deg"]
+
+    @property
+    def H(self):
+        if self._sol.get("H") is None:
+            raise KeyError("H was not stored: call kernel(store_H=True) on a sector smaller than max_lcz")
+        return self._sol["H"]
+
+    @property
+    def e(self):
+        return np.array(self._sol["eigenvalues"])
+
+    @property
+    def etot(self):
+        return self.e0
+
+    @property
+    def e0(self):
+        return self.e[:self.nb_comp_states] @ self.wgt / self.Z
+
+    @property
+    def lcz_results(self):
+        if not self._sol["is_lanczos"]:
+            raise KeyError("the sector was diagonalised densely (no Lanczos run)")
+        lcz = {'alpha': np.array(self._sol["alpha"]), 'beta': np.array(self._sol["beta"]),
+               'conv': self._sol["conv"], 'step': self._sol["nb_lcz"]}
+        if lcz['step'] > self.max_lcz:
+            raise StopIteration('Lanczos not converged, step,', lcz['step'],
+                                f' greater than the maximum wanted {self.max_lcz}')
+        return lcz
+
+    @property
+    def nb_lcz(self):
+        if not self._sol["is_lanczos"]:
+            raise KeyError("the sector was diagonalised densely (no Lanczos run)")
+        return self._sol["nb_lcz"]
+
+    @property
+    def nb_comp_states(self):
+        return len(self.boltzmann)
+
+    @property
+    def psi0(self):
+        w = self.boltzmann / self.Z
+        sec = self.sector(self.nup[0], self.ndown[0])
+        acc = None
+        for b, wb in enumerate(w):
+            if wb == 0.0:
+                continue
+            v = sec.to_ref(self._state_device(b)).double().cpu().numpy() * wb
+            acc = v if acc is None else acc + v
+        return acc
+
+    def psi(self, vector: int):
+        sec = self.sector(self.nup[0], self.ndown[0])
+        return sec.to_ref(self._state_device(vector)).double().cpu().numpy()
+
+    def psi_as_dict(self, vector: int):
+        psi = self.psi(vector)
+        index = np.where(abs(psi) > 1.e-12)[0]
+        return {'basis': self.basis[index], 'coeff': psi[index]}
+
+    @property
+    def is_lanczos(self):
+        return bool(self._sol and self._sol["is_lanczos"])
+
+    @property
+    def U_matrix(self):
+        if isinstance(self.U, np.ndarray):
+            if len(self.U.shape) == 4 or len(self.U.shape) == 1:
+                return self.U
+            raise ValueError
+        if isinstance(self.U, (float, int)):
+            return np.full(self.nb_sites, self.U, dtype=float)

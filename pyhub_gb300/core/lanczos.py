@@ -51,9 +51,11 @@ class ReferenceRule:
         self.ev = 0.0
         self.ndeg = 0
         self.converged = False
+        self.conv = 0.0   # VAL(NDEG+1) - EV at the last check (the lcz_conv attribute)
 
     def __call__(self, val: np.ndarray, step: int = 0) -> bool:
         i = min(self.ndeg, len(val) - 1)
+        self.conv = float(val[i] - self.ev)
         if abs(val[i] - self.ev) < self.acc:
             if abs(val[i] - val[0]) > self.acc and (self.ndeg + 1) > 1:
                 self.converged = True
@@ -96,6 +98,26 @@ class KrylovResult:
     ndeg: int = 0
     times: dict = field(default_factory=dict)
     gram_offdiag: float = 0.0   # max |G - I| of the stored basis (orthogonality check)
+    basis: object = None        # kept Krylov basis (keep_basis=True)
+    scales: np.ndarray = None
+    _ws: object = None
+
+    def ritz_vector(self, k: int):
+        """Ritz vector k as an FP64 device tensor (needs keep_basis=True)."""
+        torch = _torch()
+        if self.basis is None:
+            raise RuntimeError("the Krylov basis was not kept")
+        z = self.ritz_vectors[:, k]
+        coef = -(z * self.scales[: self.steps])
+        self._ws.coef[: self.steps].copy_(torch.from_numpy(coef))
+        psi = torch.zeros(self.basis.shape[1], dtype=torch.float64, device=self.basis.device)
+        _capi.update(self.basis, self.steps, self._ws.coef, None, psi, norm2=self._ws.nrm, scratch=self._ws.buf)
+        psi.mul_(1.0 / math.sqrt(float(self._ws.nrm[0].item())))
+        return psi
+
+    def release(self):
+        self.basis = None
+        self._ws = None
 
 
 def start_vector(sec, seed: int = 0, dtype=None, device=None):
@@ -119,6 +141,41 @@ def _tridiag_eigs(alpha, beta, k, vectors=False):
     return sla.eigh_tridiagonal(a, b, eigvals_only=True)
 
 
+class KernelTimer:
+    """CUDA-event timing of the C-ABI calls of a Krylov loop, by call kind,
+    on the current stream (where the calls enqueue their kernels).  Records
+    algorithmic bytes and kernel launches per call; read after a
+    synchronize."""
+
+    LAUNCHES = {"hv": 3, "multidot": 2, "update": 2}
+
+    def __init__(self):
+        self.ev = {}
+        self.bytes = {}
+        self.calls = {}
+
+    def __call__(self, kind: str, nbytes: float):
+        torch = _torch()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        self.ev.setdefault(kind, []).append((a, b))
+        self.bytes[kind] = self.bytes.get(kind, 0.0) + float(nbytes)
+        self.calls[kind] = self.calls.get(kind, 0) + 1
+        return b
+
+    def summary(self):
+        out = {}
+        for k, lst in self.ev.items():
+            t = sum(a.elapsed_time(b) for a, b in lst) * 1e-3
+            out[k] = {"calls": self.calls[k], "seconds": t, "bytes": self.bytes[k],
+                      "launches": self.calls[k] * self.LAUNCHES.get(k, 1)}
+        return out
+
+    def launches(self):
+        return sum(self.calls[k] * self.LAUNCHES.get(k, 1) for k in self.calls)
+
+
 class _Scratch:
     def __init__(self, n, nvec, device):
         torch = _torch()
@@ -131,7 +188,7 @@ class _Scratch:
 
 def lanczos_full(sec, v0, max_steps: int, dtype=None, rule=None, check_every: int = NADD,
                  min_steps: int = 0, want_vector: bool = True, vec_index: int = 0,
-                 timer=None) -> KrylovResult:
+                 keep_basis: bool = False, timer: KernelTimer = None) -> KrylovResult:
     """Lanczos with full reorthogonalisation (delayed CGS with the exact Gram
     matrix).  v0: start vector (device tensor, internal layout).  The basis
     of max_steps+1 vectors is stored in ``dtype`` (FP32 or FP64); scalars are
@@ -162,11 +219,17 @@ def lanczos_full(sec, v0, max_steps: int, dtype=None, rule=None, check_every: in
     k_done = 0
     converged = breakdown = False
     val = None
-    t_hv = t_dot = t_upd = 0.0
+    es = V.element_size()
     for k in range(m):
-        if timer: timer("hv", k)
+        if timer is not None:
+            e = timer("hv", 2.0 * sec.dim * es)
         sec.hv(V[k], w)
+        if timer is not None:
+            e.record()
+            e = timer("multidot", (k + 2) * sec.dim * es)
         _capi.multidot(V, k + 1, w, ws.dots, ws.buf, z=V[k])
+        if timer is not None:
+            e.record()
         d = ws.dots[: 2 * (k + 1)].cpu().numpy()
         a, b = d[: k + 1], d[k + 1:]
         sv = s[: k + 1]
@@ -183,7 +246,11 @@ def lanczos_full(sec, v0, max_steps: int, dtype=None, rule=None, check_every: in
         y = sla.cho_solve((L[: k + 1, : k + 1], True), c, check_finite=False)
         coef = y * sv / sv[k]
         ws.coef[: k + 1].copy_(torch.from_numpy(coef))
+        if timer is not None:
+            e = timer("update", (k + 3) * sec.dim * es)
         _capi.update(V, k + 1, ws.coef, w, V[k + 1], norm2=ws.nrm, scratch=ws.buf)
+        if timer is not None:
+            e.record()
         nw2 = float(ws.nrm[0].item())
         alpha[k] = c[k]
         bk = sv[k] * math.sqrt(max(nw2, 0.0))
@@ -221,8 +288,92 @@ def lanczos_full(sec, v0, max_steps: int, dtype=None, rule=None, check_every: in
         psi.mul_(1.0 / nrm)
         res.psi = psi
     res.times = {"loop": t_loop - t_start, "total": time.perf_counter() - t_start}
-    del V, w, ws
+    if rule is not None:
+        res.conv = float(getattr(rule, "conv", 0.0))
+    if keep_basis:
+        res.basis, res.scales, res._ws = V, s, ws
+    del w
     return res
+
+
+@dataclass
+class PlainResult:
+    alpha: np.ndarray
+    beta: np.ndarray
+    ritz: np.ndarray
+    ritz_vectors: np.ndarray
+    steps: int
+    converged: bool
+    psis: list
+    times: dict
+
+
+def lanczos_plain(sec, v0, max_steps: int, rule=None, check_every: int = NADD, nvec: int = 1,
+                  want_vectors: bool = True) -> PlainResult:
+    """The reference's three-term recurrence without reorthogonalisation
+    (lanczos.f90:52-58) on three device vectors, alpha fused into the H*v
+    pass.  Ritz vectors are rebuilt by running the same (deterministic)
+    recurrence a second time and accumulating sum_k z_k v_k in FP64, instead
+    of storing every Krylov vector as the reference does (lanczos.f90:42-49)."""
+    torch = _torch()
+    dev = v0.device
+    n = sec.n
+    m = int(max_steps)
+    t0 = time.perf_counter()
+    ws = _Scratch(n, 4, dev)
+    R = torch.zeros((3, n), dtype=v0.dtype, device=dev)
+
+    def run(steps, z=None, psis=None):
+        R.zero_()
+        R[0].copy_(v0)
+        _capi.multidot(R, 1, R[0], ws.dots, ws.buf)
+        s_prev, s_cur = 0.0, 1.0 / math.sqrt(float(ws.dots[0].item()))
+        alpha, beta = [], []
+        bprev = 0.0
+        done = 0
+        conv = False
+        for k in range(steps):
+            cur, nxt, prv = k % 3, (k + 1) % 3, (k + 2) % 3
+            if psis is not None:
+                for j, p in enumerate(psis):
+                    ws.coef[0] = -z[k, j] * s_cur
+                    _capi.update(R[cur:cur + 1], 1, ws.coef, p, p)
+            sec.hv(R[cur], R[nxt], dots=ws.dots, scratch=ws.buf)
+            a = s_cur * s_cur * float(ws.dots[0].item())
+            coef = np.zeros(3)
+            coef[cur] = a
+            if k > 0:
+                coef[prv] = bprev * s_prev / s_cur
+            ws.coef[:3].copy_(torch.from_numpy(coef))
+            _capi.update(R, 3, ws.coef, R[nxt], R[nxt], norm2=ws.nrm, scratch=ws.buf)
+            nw2 = float(ws.nrm[0].item())
+            b = s_cur * math.sqrt(max(nw2, 0.0))
+            alpha.append(a)
+            beta.append(b)
+            done = k + 1
+            if not math.isfinite(nw2):
+                raise FloatingPointError(f"non-finite norm at Lanczos step {k}")
+            if b <= 1e-13 * max(1.0, abs(a)):
+                conv = True
+                break
+            s_prev, s_cur, bprev = s_cur, 1.0 / math.sqrt(nw2), b
+            if psis is None and rule is not None and done % check_every == 0:
+                if rule(_tridiag_eigs(np.array(alpha), np.array(beta), done), done):
+                    conv = True
+                    break
+        return np.array(alpha), np.array(beta), done, conv
+
+    alpha, beta, done, conv = run(m)
+    val, vec = _tridiag_eigs(alpha, beta, done, vectors=True)
+    psis = []
+    if want_vectors:
+        psis = [torch.zeros(n, dtype=torch.float64, device=dev) for _ in range(min(nvec, done))]
+        run(done, z=vec[:, : len(psis)], psis=psis)
+        for p in psis:
+            _capi.multidot(p.view(1, -1), 1, p, ws.dots, ws.buf)
+            p.mul_(1.0 / math.sqrt(float(ws.dots[0].item())))
+    return PlainResult(alpha=alpha, beta=beta, ritz=val, ritz_vectors=vec, steps=done, converged=conv,
+                       psis=psis, times={"total": time.perf_counter() - t0})
 
 
 @dataclass
@@ -244,7 +395,7 @@ class GroundState:
 
 def ground_state(sec, mode: str = "mixed", steps: int = 200, seed: int = 0, v0=None, rule=None,
                  refine_steps: int = 60, refine_tol: float = 1e-13, check_every: int = NADD,
-                 nb_vectors: int = 1) -> GroundState:
+                 timer: KernelTimer = None) -> GroundState:
     """Ground state of the sector operator.
 
     mode "f64":   FP64 vectors, FP64 scalars (the plain FP64 GPU Lanczos).
@@ -258,13 +409,15 @@ def ground_state(sec, mode: str = "mixed", steps: int = 200, seed: int = 0, v0=N
     if v0 is None:
         v0 = start_vector(sec, seed)
     if mode == "f64":
-        r = lanczos_full(sec, v0.to(torch.float64), steps, torch.float64, rule=rule, check_every=check_every)
+        r = lanczos_full(sec, v0.to(torch.float64), steps, torch.float64, rule=rule, check_every=check_every,
+                         timer=timer)
         torch.cuda.synchronize()
         return GroundState(e0=float(r.ritz[0]), psi=r.psi, ritz=r.ritz, alpha=r.alpha, beta=r.beta, steps=r.steps,
                            refine_steps=0, converged=r.converged, ndeg=r.ndeg,
                            times={"total": time.perf_counter() - t0, "fp64": r.times["total"]}, mode=mode,
                            e0_unrefined=float(r.ritz[0]), ritz_vectors=r.ritz_vectors)
-    r32 = lanczos_full(sec, v0.to(torch.float32), steps, torch.float32, rule=rule, check_every=check_every)
+    r32 = lanczos_full(sec, v0.to(torch.float32), steps, torch.float32, rule=rule, check_every=check_every,
+                       timer=timer)
     t1 = time.perf_counter()
     if mode == "f32":
         return GroundState(e0=float(r32.ritz[0]), psi=r32.psi, ritz=r32.ritz, alpha=r32.alpha, beta=r32.beta,
@@ -272,7 +425,8 @@ def ground_state(sec, mode: str = "mixed", steps: int = 200, seed: int = 0, v0=N
                            times={"total": t1 - t0, "fp32": r32.times["total"]}, mode=mode,
                            e0_unrefined=float(r32.ritz[0]), ritz_vectors=r32.ritz_vectors)
     rr = EnergyRule(refine_tol * max(1.0, abs(float(r32.ritz[0]))), min_steps=2 * check_every)
-    r64 = lanczos_full(sec, r32.psi, refine_steps, torch.float64, rule=rr, check_every=check_every)
+    r64 = lanczos_full(sec, r32.psi, refine_steps, torch.float64, rule=rr, check_every=check_every,
+                       timer=timer)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
     return GroundState(e0=float(r64.ritz[0]), psi=r64.psi, ritz=r64.ritz, alpha=r32.alpha, beta=r32.beta,

@@ -1,0 +1,209 @@
+"""Static reduced quantities and Green's functions with the reference's API
+(pyhub/core/reduced_quantities.py:6-169).
+
+The reference reads Fortran-written datasets from solver.h5 on every
+property access.  Here the same quantities are computed on the GPU
+(ed_rdm: ONE_RDM, TWO_RDM's local-U branch and J_SPIN of static_rq.f90, or
+J_SPIN of static_rq_heis.f90) for every Boltzmann-weighted state and kept in
+memory with the reference's shapes: density matrices [NW, N, N] in the
+Python view of the file (element [w][a][b] = DENS_MAT(b+1, a+1) of state w),
+``ni`` [NW, N] and ``sisj`` [NW, N, N].
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from ..tools.pole import Pole
+
+
+def all_pairs(norb: int):
+    return [(J, K) for J in range(1, norb + 1) for K in range(1, norb + 1)]
+
+
+def assemble_hubbard(raw: np.ndarray, norb: int, nup: int, ndn: int):
+    """Reference symmetrisation of the raw ed_rdm sums over all pairs:
+    DENS_MAT(J,K) computed for K<=J and mirrored, the down matrix copied from
+    the up one when N_up == N_down (static_rq.f90:161-241), NI from the local
+    branch (:307-316), SMATRIX(J,K) for K<=J mirrored (:331-393).
+    Returns (gamma_up, gamma_down, ni, sisj) as the reference's Python reads them."""
+    q = raw.reshape(norb, norb, 6)  # q[J-1][K-1][:]
+    gu = np.zeros((norb, norb))
+    gd = np.zeros((norb, norb))
+    sm = np.zeros((norb, norb))
+    ni = np.zeros(norb)
+    for J in range(norb):
+        for K in range(J + 1):
+            if J == K:
+                nu, nd, do, zz = q[J, J, 0], q[J, J, 2], q[J, J, 3], q[J, J, 1]
+                gu[J, J] = nu
+                gd[J, J] = nd
+                ni[J] = do
+                sm[J, J] = 0.5 * (nu - do) + 0.5 * (nd - do) + zz
+            else:
+                gu[J, K] = gu[K, J] = q[J, K, 0]
+                gd[J, K] = gd[K, J] = q[J, K, 4]
+                sm[J, K] = sm[K, J] = q[J, K, 5] + q[J, K, 1]
+    if nup == ndn:
+        gd = gu.copy()
+    return gu, gd, ni, sm
+
+
+def assemble_heisenberg(raw: np.ndarray, norb: int):
+    """SMATRIX(J,K) for every J,K (static_rq_heis.f90:66-114); the Python
+    view of the file is its transpose."""
+    q = raw.reshape(norb, norb, 2)
+    smat = q[:, :, 0] + q[:, :, 1]      # [J-1][K-1] = SMATRIX(J,K)
+    return smat.T.copy()
+
+
+class StaticQuantities:
+
+    def __init__(self):
+        pass
+
+    def _wnorm(self):
+        return self.wgt / np.sum(self.wgt)
+
+    @property
+    def one_rdm(self):
+        w = self._wnorm()
+        return {"up": np.einsum("ijk,i->jk", self._rq["density_matrix_up"], w),
+                "down": np.einsum("ijk,i->jk", self._rq["density_matrix_down"], w)}
+
+    @property
+    def ni(self):
+        return np.einsum("ij,i->j", self._rq["ni"], self._wnorm())
+
+    @property
+    def two_rdm(self):
+        raise NotImplementedError("the two-body density (dbl_occ, U_ijkl path is_Uloc=3) is not built")
+
+    @property
+    def density(self):
+        return {spin: np.diag(self.one_rdm[spin]) for spin in ["up", "down"]}
+
+    @property
+    def density_matrix(self):
+        return self.one_rdm
+
+    @property
+    def one_rdm0(self):
+        return {"up": self.Vk @ np.diag([1.0 if i < self.nup[0] else 0.0 for i in range(self.nb_sites)]) @ self.Vk.T,
+                "down": self.Vk @ np.diag([1.0 if i < self.ndown[0] else 0.0 for i in range(self.nb_sites)]) @ self.Vk.T}
+
+    @property
+    def density_matrix0(self):
+        return self.one_rdm0
+
+    @property
+    def wi(self):
+        return self.ni
+
+    @property
+    def spin_cor_matrix(self):
+        return np.einsum("ijk,i->jk", self._rq["sisj"], self._wnorm())
+
+    @property
+    def s2(self):
+        return np.sum(self.spin_cor_matrix)
+
+    @property
+    def eta_k(self):
+        return {"up": np.diag(self.Vk.T @ self.density_matrix["up"] @ self.Vk),
+                "down": np.diag(self.Vk.T @ self.density_matrix["down"] @ self.Vk)}
+
+    @property
+    def eta_k0(self):
+        return {"up": np.array([1.0 if i < self.nup[0] else 0.0 for i in range(self.nb_sites)]),
+                "down": np.array([1.0 if i < self.ndown[0] else 0.0 for i in range(self.nb_sites)])}
+
+    @property
+    def e_one_body(self):
+        return (np.einsum("ij,ij->", self.one_rdm["up"], self.t_matrix)
+                + np.einsum("ij,ij->", self.one_rdm["down"], self.t_matrix))
+
+    @property
+    def e_two_body(self):
+        return (np.sum(self.ni * self.U_matrix)
+                + np.einsum("bij,ij,b", self._rq["sisj"], self.J_matrix, self._wnorm()))
+
+
+class GreenFunction:
+
+    def __init__(self):
+        pass
+
+    def compute_gf(self):
+        """G[spin][i,j] as Pole objects, with the reference's pole placement
+        (reduced_quantities.py:84-92): greater poles at E_n(N+1) - E0, lesser
+        poles at E0 - E_n(N-1), weights from the start-vector overlaps."""
+        w = self._wnorm()
+        gf = {}
+        for spin in ("up", "down"):
+            g = np.empty((self.nb_sites_comp, self.nb_sites_comp), dtype=object)
+            for i in range(self.nb_sites_comp):
+                for j in range(self.nb_sites_comp):
+                    parts = []
+                    for b, wb in enumerate(w):
+                        if wb == 0.0:
+                            continue
+                        for part in ("greater", "lesser"):
+                            pos, wts = self._spgf[b][spin][part].pole(i, j)
+                            parts.append(Pole({"positions": pos, "weights": wts * wb}).clean(wtol=1.e-8))
+                    g[i, j] = Pole.sum(parts)
+            gf[spin] = g
+        return gf
+
+    @property
+    def nb_poles(self):
+        b0 = self._spgf[0]
+        return np.array([[b0["up"]["lesser"].npoles, b0["down"]["lesser"].npoles],
+                         [b0["up"]["greater"].npoles, b0["down"]["greater"].npoles]], dtype=int)
+
+    @property
+    def ip(self):
+        return {spin: (self._spgf[0][spin]["lesser"].e_lowest - self.e0) for spin in ["up", "down"]}
+
+    @property
+    def ae(self):
+        return {spin: (self.e0 - self._spgf[0][spin]["greater"].e_lowest) for spin in ["up", "down"]}
+
+    @property
+    def mu(self):
+        return {spin: (-self.ip[spin] - self.ae[spin]) / 2 for spin in ["up", "down"]}
+
+    @property
+    def density_matrix_from_gf(self):
+        return self.one_rdm_from_gf
+
+    @property
+    def one_rdm_from_gf(self):
+        w = self._wnorm()
+        out = {}
+        for spin in ("up", "down"):
+            out[spin] = sum(wb * self._spgf[b][spin]["lesser"].static() for b, wb in enumerate(w) if wb != 0.0)
+        return out
+
+    @property
+    def gf0(self):
+        return {"up": np.array([[Pole({"positions": self.ek, "weights": self.Vk[i, :] * self.Vk[j, :]})
+                                 for i in range(self.nb_sites)] for j in range(self.nb_sites)]),
+                "down": np.array([[Pole({"positions": self.ek, "weights": self.Vk[i, :] * self.Vk[j, :]})
+                                   for i in range(self.nb_sites)] for j in range(self.nb_sites)])}
+
+    def self_energy(self, w, eta=0.05):
+        """Sigma(w) = G0^-1 - G^-1 with the reference's pseudo-inverses
+        (reduced_quantities.py:134-161), G evaluated from its poles."""
+        if isinstance(w, (list, np.ndarray)):
+            A = [self.self_energy(w_, eta=eta) for w_ in w]
+            n = self.nb_sites_comp
+            return {s: np.array([[[A[k][s][i, j] for k in range(len(w))] for i in range(n)] for j in range(n)],
+                                dtype=np.complex128) for s in ("up", "down")}
+        g0 = np.linalg.pinv(np.einsum("ik,jk,k->ij", self.Vk, self.Vk, 1. / (w - self.ek + 1j * eta)))
+        out = {}
+        for s in ("up", "down"):
+            G = np.array([[self.gf[s][i, j].retarded(w, eta=eta) for j in range(self.nb_sites_comp)]
+                          for i in range(self.nb_sites_comp)])
+            n = self.nb_sites_comp
+            out[s] = g0[:n, :n] - np.linalg.pinv(G)
+        return out

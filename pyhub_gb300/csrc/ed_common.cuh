@@ -61,13 +61,19 @@ struct HopTable {
     float *cf32 = nullptr;     // [nnz]
     double *cf64 = nullptr;    // [nnz]
     double *ediag = nullptr;   // [n]  sum of T(J,J) over occupied J (|T(J,J)| >= tol)
+    // The same table in sliced-ELL form for the row pass: strings in slices of
+    // 32; slice s holds width[s] slots, slot-major, so that the 32 lanes of a
+    // warp read one slot with one coalesced load.  Padding slots point at the
+    // string itself with coefficient 0.
+    int64_t nslice = 0, ell_slots = 0;
+    int32_t *ell_off = nullptr;    // [nslice+1] first slot of each slice
+    int32_t *ell_src = nullptr;    // [ell_slots*32]
+    float *ell_cf32 = nullptr;
+    double *ell_cf64 = nullptr;
     bool owner = true;
 };
 
 struct HeisTables {
-    // colex rank of the empty-site pattern in byte chunks:
-    // rank = sum_b lut[b][pop(lower chunks)][byte_b]
-    uint32_t *lut = nullptr;   // [4][33][256]
     int nbond = 0;             // unordered pairs {J,K} with a nonzero flip or zz term
     int8_t bj[kMaxSites * kMaxSites];
     int8_t bk[kMaxSites * kMaxSites];
@@ -88,6 +94,10 @@ struct ed_sector {
     bool u_uniform = true;
     double u_value = 0.0;
     ed::HeisTables heis;
+    // colex rank of an empty-site pattern h (bit j: site j+1 empty) in byte
+    // chunks, shared by every kernel that ranks strings on the fly:
+    // rank = sum_b lut[b][popcount(h & (2^(8b)-1))][byte b of h]
+    uint32_t *lut = nullptr;   // [4][33][256]
     double t_host[ed::kMaxSites * ed::kMaxSites];
     double j_host[ed::kMaxSites * ed::kMaxSites];
     int device = 0;
@@ -112,5 +122,27 @@ __device__ __forceinline__ float warp_sumf(float v)
 }
 
 int num_sms();
+
+// Empty-site pattern of a string of norb sites (site POS in bit norb-POS):
+// bit j set when site j+1 is empty.
+__device__ __forceinline__ uint32_t holes_dev(uint32_t s, int norb)
+{
+    const uint32_t full = (norb >= 32) ? 0xFFFFFFFFu : ((1u << norb) - 1u);
+    return __brev(~s & full) >> (32 - norb);
+}
+
+// Index of a string in the reference order from its empty-site pattern.
+__device__ __forceinline__ uint32_t rank_holes(const uint32_t *__restrict__ lut, uint32_t h)
+{
+    uint32_t r = 0;
+    int c = 0;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        const uint32_t byte = (h >> (8 * b)) & 255u;
+        r += __ldg(lut + (b * 33 + c) * 256 + byte);
+        c += __popc(byte);
+    }
+    return r;
+}
 
 }  // namespace ed

@@ -22,6 +22,8 @@ struct HubArgs {
     int64_t nsup, nsdn, ld;
     const uint32_t *ustr; const int32_t *uptr; const int32_t *usrc; const void *ucf; const double *uediag;
     const uint32_t *dstr; const int32_t *dptr; const int32_t *dsrc; const void *dcf; const double *dediag;
+    int64_t nslice;
+    const int32_t *ell_off; const int32_t *ell_src;
     double u_site[kMaxSites];
     int u_uniform;
     double u_value;
@@ -57,14 +59,17 @@ __device__ __forceinline__ void stage_row(T *dst, const T *__restrict__ src, int
     }
 }
 
-// Pass 1: diagonal + up hops, R rows per CTA iteration.
+// Pass 1: diagonal + up hops, R rows per CTA iteration.  Each warp owns one
+// 32-string slice at a time and walks its sliced-ELL slots (coalesced,
+// four slots in flight), gathering the sources from the staged rows.
 template <typename T, int R>
 __global__ void __launch_bounds__(512) hub_row_kernel(const T *__restrict__ x, T *__restrict__ y,
                                                       const HubArgs a, int64_t sld, int vec_ok)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *xs = reinterpret_cast<T *>(smem_raw);
-    const T *__restrict__ cf = static_cast<const T *>(a.ucf);
+    const T *__restrict__ ecf = static_cast<const T *>(a.ucf);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
     const int64_t nsup = a.nsup, ld = a.ld;
     for (int64_t d0 = (int64_t)blockIdx.x * R; d0 < a.nsdn; d0 += (int64_t)gridDim.x * R) {
         const int nr = (int)min((int64_t)R, a.nsdn - d0);
@@ -76,25 +81,43 @@ __global__ void __launch_bounds__(512) hub_row_kernel(const T *__restrict__ x, T
         T ed[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            sd[r] = (r < nr) ? a.dstr[d0 + r] : 0u;
-            ed[r] = (r < nr) ? (T)a.dediag[d0 + r] : (T)0;
+            sd[r] = (r < nr) ? __ldg(a.dstr + d0 + r) : 0u;
+            ed[r] = (r < nr) ? (T)__ldg(a.dediag + d0 + r) : (T)0;
         }
-        for (int64_t u = threadIdx.x; u < nsup; u += blockDim.x) {
-            const uint32_t su = __ldg(a.ustr + u);
-            const T eu = (T)__ldg(a.uediag + u);
+        for (int64_t sl = warp; sl < a.nslice; sl += nwarps) {
+            const int64_t u = sl * 32 + lane;
+            const bool ok = u < nsup;
+            const int64_t uu = ok ? u : nsup - 1;
+            const uint32_t su = __ldg(a.ustr + uu);
+            const T eu = (T)__ldg(a.uediag + uu);
             T acc[R];
 #pragma unroll
-            for (int r = 0; r < R; ++r) acc[r] = (eu + ed[r] + u_energy<T>(a, su & sd[r])) * xs[r * sld + u];
-            const int e0 = __ldg(a.uptr + u), e1 = __ldg(a.uptr + u + 1);
-            for (int e = e0; e < e1; ++e) {
-                const int q = __ldg(a.usrc + e);
-                const T c = __ldg(cf + e);
+            for (int r = 0; r < R; ++r) acc[r] = (eu + ed[r] + u_energy<T>(a, su & sd[r])) * xs[r * sld + uu];
+            const int s0 = __ldg(a.ell_off + sl), ns = __ldg(a.ell_off + sl + 1) - s0;
+            const int32_t *sp = a.ell_src + (int64_t)s0 * 32 + lane;
+            const T *cp = ecf + (int64_t)s0 * 32 + lane;
+            int k = 0;
+            for (; k + 4 <= ns; k += 4) {
+                int q[4];
+                T c[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) { q[i] = __ldg(sp + (k + i) * 32); c[i] = __ldg(cp + (k + i) * 32); }
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int r = 0; r < R; ++r) acc[r] += c[i] * xs[r * sld + q[i]];
+            }
+            for (; k < ns; ++k) {
+                const int q = __ldg(sp + k * 32);
+                const T c = __ldg(cp + k * 32);
 #pragma unroll
                 for (int r = 0; r < R; ++r) acc[r] += c * xs[r * sld + q];
             }
+            if (ok) {
 #pragma unroll
-            for (int r = 0; r < R; ++r)
-                if (r < nr) y[(d0 + r) * ld + u] = acc[r] * (T)a.scale;
+                for (int r = 0; r < R; ++r)
+                    if (r < nr) y[(d0 + r) * ld + u] = acc[r] * (T)a.scale;
+            }
         }
         __syncthreads();
     }
@@ -102,7 +125,9 @@ __global__ void __launch_bounds__(512) hub_row_kernel(const T *__restrict__ x, T
 
 // Pass 2: down hops, y[d][slab] += sum_e c_e x[src_e][slab]; optional dots.
 // Work items (slab, group of 8 rows) are visited slab-major by a persistent
-// grid so that the CTAs in flight share one or two slabs of x in L2.
+// grid so that the CTAs in flight share one or two slabs of x in L2.  A warp
+// holds its row's neighbour list in registers (one entry per lane) and issues
+// the neighbour loads of a chunk back to back.
 template <typename T, int VW>
 __global__ void __launch_bounds__(256) hub_slab_kernel(const T *__restrict__ x, T *__restrict__ y,
                                                        const HubArgs a, int64_t slab_w, int64_t ngroups,
@@ -118,50 +143,82 @@ __global__ void __launch_bounds__(256) hub_slab_kernel(const T *__restrict__ x, 
         const int64_t d = g * 8 + warp;
         if (d >= a.nsdn) continue;
         const int64_t c0 = slab * slab_w, c1 = min(c0 + slab_w, nsup);
-        const int e0 = __ldg(a.dptr + d), e1 = __ldg(a.dptr + d + 1);
+        const int e0 = __ldg(a.dptr + d), nn = __ldg(a.dptr + d + 1) - e0;
         T *yr = y + d * ld;
+        const T *xd = x + d * ld;
         float pxy = 0.f, pyy = 0.f;
         double qxy = 0.0, qyy = 0.0;
-        int64_t c = c0 + (int64_t)lane * VW;
-        for (; c + VW <= c1; c += 32 * VW) {
-            T acc[VW];
+        for (int b0 = 0; b0 < nn; b0 += 32) {
+            const int nb = min(32, nn - b0);
+            const int my_src = (lane < nb) ? __ldg(a.dsrc + e0 + b0 + lane) : 0;
+            const T my_cf = (lane < nb) ? __ldg(cf + e0 + b0 + lane) * sc : (T)0;
+            const bool last = (b0 + 32 >= nn);
+            // chunks of 32*VW columns; the loop is warp-uniform so every lane
+            // takes part in the shuffles, lanes past c1 are masked
+            for (int64_t cb = c0; cb < c1; cb += 32 * VW) {
+                const int64_t c = cb + (int64_t)lane * VW;
+                const bool full = c + VW <= c1;
+                const int nk = full ? VW : (c < c1 ? (int)(c1 - c) : 0);
+                T acc[VW];
 #pragma unroll
-            for (int k = 0; k < VW; ++k) acc[k] = yr[c + k];
-            for (int e = e0; e < e1; ++e) {
-                const T w = __ldg(cf + e) * sc;
-                const T *xr = x + (int64_t)__ldg(a.dsrc + e) * ld + c;
-                if constexpr (VW == 4 && sizeof(T) == 4) {
-                    const float4 v = __ldg(reinterpret_cast<const float4 *>(xr));
-                    acc[0] += w * v.x; acc[1] += w * v.y; acc[2] += w * v.z; acc[3] += w * v.w;
-                } else if constexpr (VW == 2 && sizeof(T) == 8) {
-                    const double2 v = __ldg(reinterpret_cast<const double2 *>(xr));
-                    acc[0] += w * v.x; acc[1] += w * v.y;
-                } else {
+                for (int k = 0; k < VW; ++k) acc[k] = (k < nk) ? yr[c + k] : (T)0;
+                int e = 0;
+                for (; e + 4 <= nb; e += 4) {
+                    T v[4][VW];
+                    T wgt[4];
 #pragma unroll
-                    for (int k = 0; k < VW; ++k) acc[k] += w * __ldg(xr + k);
+                    for (int i = 0; i < 4; ++i) {
+                        const int64_t sidx = __shfl_sync(0xffffffffu, my_src, e + i);
+                        wgt[i] = __shfl_sync(0xffffffffu, my_cf, e + i);
+                        const T *xr = x + sidx * ld + c;
+                        if (full) {
+                            if constexpr (VW == 4 && sizeof(T) == 4) {
+                                const float4 t4 = __ldg(reinterpret_cast<const float4 *>(xr));
+                                v[i][0] = t4.x; v[i][1] = t4.y; v[i][2] = t4.z; v[i][3] = t4.w;
+                            } else if constexpr (VW == 2 && sizeof(T) == 8) {
+                                const double2 t2 = __ldg(reinterpret_cast<const double2 *>(xr));
+                                v[i][0] = t2.x; v[i][1] = t2.y;
+                            } else {
+#pragma unroll
+                                for (int k = 0; k < VW; ++k) v[i][k] = __ldg(xr + k);
+                            }
+                        } else {
+#pragma unroll
+                            for (int k = 0; k < VW; ++k) v[i][k] = (k < nk) ? __ldg(xr + k) : (T)0;
+                        }
+                    }
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+#pragma unroll
+                        for (int k = 0; k < VW; ++k) acc[k] += wgt[i] * v[i][k];
                 }
-            }
+                for (; e < nb; ++e) {
+                    const int64_t sidx = __shfl_sync(0xffffffffu, my_src, e);
+                    const T wg = __shfl_sync(0xffffffffu, my_cf, e);
 #pragma unroll
-            for (int k = 0; k < VW; ++k) yr[c + k] = acc[k];
-            if (partials) {
+                    for (int k = 0; k < VW; ++k)
+                        if (k < nk) acc[k] += wg * __ldg(x + sidx * ld + c + k);
+                }
 #pragma unroll
-                for (int k = 0; k < VW; ++k) {
-                    const T xv = __ldg(x + d * ld + c + k);
-                    if constexpr (sizeof(T) == 4) { pxy += xv * acc[k]; pyy += acc[k] * acc[k]; }
-                    else { qxy += xv * acc[k]; qyy += acc[k] * acc[k]; }
+                for (int k = 0; k < VW; ++k)
+                    if (k < nk) yr[c + k] = acc[k];
+                if (partials && last) {
+#pragma unroll
+                    for (int k = 0; k < VW; ++k) {
+                        if (k >= nk) continue;
+                        const T xv = __ldg(xd + c + k);
+                        if constexpr (sizeof(T) == 4) { pxy += xv * acc[k]; pyy += acc[k] * acc[k]; }
+                        else { qxy += xv * acc[k]; qyy += acc[k] * acc[k]; }
+                    }
                 }
             }
         }
-        // ragged tail of the slab (scalar)
-        for (int64_t cc = c; cc < c1; ++cc) {
-            T acc = yr[cc];
-            for (int e = e0; e < e1; ++e)
-                acc += __ldg(cf + e) * sc * __ldg(x + (int64_t)__ldg(a.dsrc + e) * ld + cc);
-            yr[cc] = acc;
-            if (partials) {
-                const T xv = __ldg(x + d * ld + cc);
-                if constexpr (sizeof(T) == 4) { pxy += xv * acc; pyy += acc * acc; }
-                else { qxy += xv * acc; qyy += acc * acc; }
+        if (nn == 0 && partials) {
+            // no down hops: the dots still need this row's y
+            for (int64_t cc = c0 + lane; cc < c1; cc += 32) {
+                const T yv = yr[cc], xv = __ldg(xd + cc);
+                if constexpr (sizeof(T) == 4) { pxy += xv * yv; pyy += yv * yv; }
+                else { qxy += xv * yv; qyy += yv * yv; }
             }
         }
         dxy += (double)pxy + qxy;
@@ -223,19 +280,6 @@ struct HeisArgs {
     uint32_t binom[kMaxSites + 1][17];
 };
 
-__device__ __forceinline__ uint32_t heis_rank(const uint32_t *__restrict__ lut, uint32_t h)
-{
-    uint32_t r = 0;
-    int c = 0;
-#pragma unroll
-    for (int b = 0; b < 4; ++b) {
-        const uint32_t byte = (h >> (8 * b)) & 255u;
-        r += __ldg(lut + (b * 33 + c) * 256 + byte);
-        c += __popc(byte);
-    }
-    return r;
-}
-
 // colex unrank of an m-hole pattern among norb positions
 __device__ __forceinline__ uint32_t heis_unrank(const HeisArgs &a, uint32_t r)
 {
@@ -274,7 +318,7 @@ __global__ void __launch_bounds__(256) heis_kernel(const T *__restrict__ x, T *_
             const double c = hj ? a.flip_jk[b] : a.flip_kj[b];
             if (c == 0.0) continue;
             const uint32_t q = h ^ ((1u << (J - 1)) | (1u << (K - 1)));
-            acc += (T)c * __ldg(x + heis_rank(a.lut, q));
+            acc += (T)c * __ldg(x + rank_holes(a.lut, q));
         }
         (void)full;
         const T xv = x[p];
@@ -310,8 +354,11 @@ static int hub_hv(ed_sector *s, cudaStream_t st, int64_t ld, const T *x, T *y, d
     a.nsup = s->nsup; a.nsdn = s->nsdn; a.ld = ld;
     a.ustr = s->up.str; a.uptr = s->up.ptr; a.usrc = s->up.src; a.uediag = s->up.ediag;
     a.dstr = s->dn.str; a.dptr = s->dn.ptr; a.dsrc = s->dn.src; a.dediag = s->dn.ediag;
-    if (sizeof(T) == 4) { a.ucf = s->up.cf32; a.dcf = s->dn.cf32; }
-    else { a.ucf = s->up.cf64; a.dcf = s->dn.cf64; }
+    if (sizeof(T) == 4) { a.ucf = s->up.ell_cf32; a.dcf = s->dn.cf32; }
+    else { a.ucf = s->up.ell_cf64; a.dcf = s->dn.cf64; }
+    a.nslice = s->up.nslice;
+    a.ell_off = s->up.ell_off;
+    a.ell_src = s->up.ell_src;
     for (int b = 0; b < kMaxSites; ++b) a.u_site[b] = s->u_site[b];
     a.u_uniform = s->u_uniform ? 1 : 0;
     a.u_value = s->u_value;
@@ -386,7 +433,7 @@ static int heis_hv(ed_sector *s, cudaStream_t st, const T *x, T *y, double scale
     a.norb = s->norb;
     a.nholes = s->norb - s->nup;
     a.n = s->nsup;
-    a.lut = h.lut;
+    a.lut = s->lut;
     if (h.nbond > kMaxSites * kMaxSites / 2) { set_error("too many bonds"); return ED_ERR_RANGE; }
     a.nbond = h.nbond;
     for (int b = 0; b < h.nbond; ++b) {

@@ -8,6 +8,7 @@
 // (compute_solver.f90:39-179) for the parameter tables.
 #include "ed_common.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -194,6 +195,45 @@ static int upload(T **dst, const T *src, size_t count)
     return ED_OK;
 }
 
+static int upload_ell(const HostHop &h, HopTable &d)
+{
+    const int64_t n = (int64_t)h.str.size();
+    const int64_t ns = (n + 31) / 32;
+    std::vector<int32_t> off((size_t)ns + 1, 0);
+    for (int64_t sl = 0; sl < ns; ++sl) {
+        int32_t w = 0;
+        for (int64_t u = sl * 32; u < std::min(n, sl * 32 + 32); ++u) w = std::max(w, h.ptr[(size_t)u + 1] - h.ptr[(size_t)u]);
+        off[(size_t)sl + 1] = off[(size_t)sl] + w;
+    }
+    const int64_t slots = off[(size_t)ns];
+    std::vector<int32_t> src((size_t)std::max<int64_t>(slots * 32, 1));
+    std::vector<double> c64((size_t)std::max<int64_t>(slots * 32, 1), 0.0);
+    for (int64_t sl = 0; sl < ns; ++sl)
+        for (int64_t k = 0; k < off[(size_t)sl + 1] - off[(size_t)sl]; ++k)
+            for (int l = 0; l < 32; ++l) {
+                const int64_t u = sl * 32 + l;
+                const size_t at = (size_t)((off[(size_t)sl] + k) * 32 + l);
+                const int64_t uu = u < n ? u : n - 1;
+                const int32_t e0 = h.ptr[(size_t)uu], e1 = h.ptr[(size_t)uu + 1];
+                if (u < n && e0 + k < e1) {
+                    src[at] = h.src[(size_t)(e0 + k)];
+                    c64[at] = h.coef[(size_t)(e0 + k)];
+                } else {
+                    src[at] = (int32_t)uu;
+                    c64[at] = 0.0;
+                }
+            }
+    std::vector<float> c32(c64.begin(), c64.end());
+    d.nslice = ns;
+    d.ell_slots = slots;
+    int rc;
+    if ((rc = upload(&d.ell_off, off.data(), off.size()))) return rc;
+    if ((rc = upload(&d.ell_src, src.data(), src.size()))) return rc;
+    if ((rc = upload(&d.ell_cf32, c32.data(), c32.size()))) return rc;
+    if ((rc = upload(&d.ell_cf64, c64.data(), c64.size()))) return rc;
+    return ED_OK;
+}
+
 static int upload_hop(const HostHop &h, int norb, int ne, HopTable &d)
 {
     d.norb = norb;
@@ -208,6 +248,7 @@ static int upload_hop(const HostHop &h, int norb, int ne, HopTable &d)
     if ((rc = upload(&d.cf32, c32.data(), c32.size()))) return rc;
     if ((rc = upload(&d.cf64, h.coef.data(), h.coef.size()))) return rc;
     if ((rc = upload(&d.ediag, h.ediag.data(), h.ediag.size()))) return rc;
+    if ((rc = upload_ell(h, d))) return rc;
     d.owner = true;
     return ED_OK;
 }
@@ -217,17 +258,16 @@ static void free_hop(HopTable &d)
     if (!d.owner) { d = HopTable(); return; }
     cudaFree(d.str); cudaFree(d.ptr); cudaFree(d.src);
     cudaFree(d.cf32); cudaFree(d.cf64); cudaFree(d.ediag);
+    cudaFree(d.ell_off); cudaFree(d.ell_src); cudaFree(d.ell_cf32); cudaFree(d.ell_cf64);
     d = HopTable();
 }
 
 // ------------------------------------------------------------ Heisenberg
 
-static int build_heis(ed_sector *s, const double *J)
+static int build_lut(ed_sector *s)
 {
-    int norb = s->norb;
-    HeisTables &h = s->heis;
-    // byte-chunk colex tables: lut[b][c][x] = sum over set bits q of x, taken in
-    // increasing order with running index i = c+1, c+2, ..., of C(8b+q, i)
+    // lut[b][c][x] = sum over the set bits q of byte x, taken in increasing
+    // order with running index i = c+1, c+2, ..., of C(8b+q, i)
     std::vector<uint32_t> lut(4 * 33 * 256, 0u);
     for (int b = 0; b < 4; ++b)
         for (int c = 0; c <= 32; ++c)
@@ -238,8 +278,13 @@ static int build_heis(ed_sector *s, const double *J)
                     if ((x >> q) & 1) r += binom(8 * b + q, ++i);
                 lut[(b * 33 + c) * 256 + x] = (uint32_t)r;
             }
-    int rc = upload(&h.lut, lut.data(), lut.size());
-    if (rc) return rc;
+    return upload(&s->lut, lut.data(), lut.size());
+}
+
+static int build_heis(ed_sector *s, const double *J)
+{
+    int norb = s->norb;
+    HeisTables &h = s->heis;
     h.nbond = 0;
     h.dconst = 0.0;
     for (int a = 1; a <= norb; ++a) {
@@ -335,6 +380,17 @@ int ed_sector_create(int norb, int nup, int ndn, int kind, const double *t, cons
     } else {
         ED_REQUIRE(t != nullptr && U != nullptr, "Hubbard sector needs t and U");
     }
+    {
+        const double *m = (kind == ED_HUBBARD) ? t : J;
+        for (int i = 0; i < norb * norb; ++i)
+            if (!std::isfinite(m[i])) {
+                set_error("%s has a non-finite entry at %d", kind == ED_HUBBARD ? "t" : "J", i);
+                return ED_ERR_ARG;
+            }
+        if (kind == ED_HUBBARD)
+            for (int i = 0; i < norb; ++i)
+                if (!std::isfinite(U[i])) { set_error("U has a non-finite entry at %d", i); return ED_ERR_ARG; }
+    }
     ed_sector *s = new (std::nothrow) ed_sector();
     if (!s) { set_error("host allocation failed"); return ED_ERR_MEM; }
     s->kind = kind;
@@ -345,8 +401,8 @@ int ed_sector_create(int norb, int nup, int ndn, int kind, const double *t, cons
     s->nsdn = nsdn;
     s->dim = nsup * nsdn;
     cudaGetDevice(&s->device);
-    int rc = ED_OK;
-    if (kind == ED_HUBBARD) {
+    int rc = build_lut(s);
+    if (rc == ED_OK && kind == ED_HUBBARD) {
         for (int i = 0; i < norb * norb; ++i) {
             if (!std::isfinite(t[i])) { delete s; set_error("t has a non-finite entry at %d", i); return ED_ERR_ARG; }
             s->t_host[i] = t[i];
@@ -371,7 +427,7 @@ int ed_sector_create(int norb, int nup, int ndn, int kind, const double *t, cons
                 if (!rc) rc = upload_hop(hd, norb, ndn, s->dn);
             }
         }
-    } else {
+    } else if (rc == ED_OK) {
         for (int i = 0; i < norb * norb; ++i) {
             if (!std::isfinite(J[i])) { delete s; set_error("J has a non-finite entry at %d", i); return ED_ERR_ARG; }
             s->j_host[i] = J[i];
@@ -393,7 +449,7 @@ int ed_sector_destroy(ed_sector *s)
     if (!s) return ED_OK;
     free_hop(s->dn);
     free_hop(s->up);
-    if (s->heis.lut) cudaFree(s->heis.lut);
+    if (s->lut) cudaFree(s->lut);
     delete s;
     return ED_OK;
 }

@@ -7,7 +7,8 @@
 // loss).  FP32 vectors: products are formed and summed in FP32 over 16
 // elements per thread, every such partial is promoted to FP64 and all further
 // accumulation is FP64, so no FP64 multiply is spent per element.  FP64
-// vectors: FP64 throughout.
+// vectors: FP64 throughout.  (The FP32 multi-dot reduces each warp's 512
+// products in FP32 before the FP64 stage; see multidot_kernel.)
 #include "ed_common.cuh"
 
 namespace ed {
@@ -44,6 +45,10 @@ __device__ __forceinline__ void load_chunk(T (&r)[kEPT], const T *__restrict__ p
 
 // partials[block][j] (j < nvec) = sum over the block's chunks of <V_j, w>,
 // partials[block][nvec + j] the same with z (when z != NULL).
+// FP32 vectors: each warp forms its 512 products per chunk and reduces them in
+// FP32 (shuffles); only that warp partial is promoted and added in FP64, so
+// the FP64 work is one add per 512 elements and vector.  For random-sign
+// data the FP32 stage contributes an absolute error ~eps32 |V_j||w|/sqrt(n).
 template <typename T>
 __global__ void __launch_bounds__(kVecThreads) multidot_kernel(int64_t n, const T *__restrict__ V, int64_t ldv,
                                                                int nvec, const T *__restrict__ w,
@@ -61,19 +66,31 @@ __global__ void __launch_bounds__(kVecThreads) multidot_kernel(int64_t n, const 
         T rw[kEPT], rz[kEPT];
         load_chunk<T>(rw, w, base, n);
         if (z) load_chunk<T>(rz, z, base, n);
+#pragma unroll 2
         for (int j = 0; j < nvec; ++j) {
             T rv[kEPT];
             load_chunk<T>(rv, V + (int64_t)j * ldv, base, n);
             T pw = 0, pz = 0;
 #pragma unroll
             for (int k = 0; k < kEPT; ++k) pw += rv[k] * rw[k];
-            double sw = warp_sum((double)pw);
-            if (lane == 0) acc[warp * m + j] += sw;
             if (z) {
 #pragma unroll
                 for (int k = 0; k < kEPT; ++k) pz += rv[k] * rz[k];
-                double sz = warp_sum((double)pz);
-                if (lane == 0) acc[warp * m + nvec + j] += sz;
+            }
+            if constexpr (sizeof(T) == 4) {
+                pw = warp_sumf(pw);
+                if (z) pz = warp_sumf(pz);
+                if (lane == 0) {
+                    acc[warp * m + j] += (double)pw;
+                    if (z) acc[warp * m + nvec + j] += (double)pz;
+                }
+            } else {
+                const double sw = warp_sum((double)pw);
+                const double sz = z ? warp_sum((double)pz) : 0.0;
+                if (lane == 0) {
+                    acc[warp * m + j] += sw;
+                    if (z) acc[warp * m + nvec + j] += sz;
+                }
             }
         }
     }

@@ -1,0 +1,3 @@
+from .pole import Pole
+
+__all__ = ["Pole"]

@@ -184,7 +184,7 @@ def test_multidot_and_update(edlib, dt):
     refo = wd - coef @ Vd
     oo = o[:n].double().cpu().numpy()
     assert np.abs(oo - refo).max() <= (1e-5 if dt == "f32" else 1e-12) * np.abs(refo).max()
-    assert abs(nrm.item() - (oo @ oo)) <= 1e-10 * (oo @ oo)
+    assert abs(nrm.item() - (oo @ oo)) <= (1e-6 if dt == "f32" else 1e-12) * (oo @ oo)
     # Ritz-vector form: FP64 output from the basis alone
     o64 = torch.zeros(n_pad, dtype=torch.float64, device="cuda")
     edlib.update(V, nvec, cd, None, o64, n=n_pad)
