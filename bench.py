@@ -58,6 +58,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--small", action="store_true", help="3x3 cluster, for a quick functional run")
+    p.add_argument("--probe", action="store_true",
+                   help="a few launches of each solve kernel on 4x4-sized vectors (about 4 GB), for profilers")
     return p.parse_args()
 
 
@@ -196,6 +198,33 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def probe(sec, torch, LZ, capi):
+    """2 FP32 H*v, 2 FP64 H*v, 2 multidot and 2 update launches (4 vectors) on
+    vectors of the 4x4 sector: the launches profiled under ncu."""
+    x = LZ.start_vector(sec, 1, dtype=torch.float32)
+    y = torch.zeros_like(x)
+    for _ in range(2):
+        sec.hv(x, y)
+    x64, y64 = x.double(), torch.zeros(sec.n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        sec.hv(x64, y64)
+    del x64, y64
+    nv = 4
+    V = torch.zeros((nv, sec.n), dtype=torch.float32, device="cuda")
+    for j in range(nv):
+        V[j].copy_(LZ.start_vector(sec, 10 + j, dtype=torch.float32))
+    sc = torch.empty(capi.scratch_bytes(sec.n, nv) // 8 + 1, dtype=torch.float64, device="cuda")
+    out = torch.zeros(2 * nv, dtype=torch.float64, device="cuda")
+    coef = torch.full((nv,), 1e-3, dtype=torch.float64, device="cuda")
+    nrm = torch.zeros(1, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        capi.multidot(V, nv, y, out, sc, z=V[nv - 1])
+    for _ in range(2):
+        capi.update(V, nv, coef, y, y, norm2=nrm, scratch=sc)
+    torch.cuda.synchronize()
+    print(json.dumps({"probe": "ok", "dim": sec.dim, "dots": out.cpu().tolist()[:2]}))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -236,6 +265,9 @@ def main():
         norb, nup, ndn = 16, 8, 8
     sec = _capi.Sector(norb, nup, ndn, _capi.ED_HUBBARD, t=t, U=U)
     hbm, hbm_kind = peaks()
+    if args.probe:
+        probe(sec, torch, LZ, _capi)
+        return
 
     def solve(timer=None):
         return LZ.ground_state(sec, mode="mixed", steps=args.lanczos_steps, seed=0, timer=timer)

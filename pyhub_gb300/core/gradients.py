@@ -95,14 +95,15 @@ class Solution:
     gamma: dict          # {'up': NxN, 'down': NxN}
 
 
-def solve(params: HubbardParams, theta, nup: int, ndn: int, mode: str = "f64", steps: int = 300,
-          seed: int = 0, tol: float = 1e-13) -> Solution:
-    """Ground state and spin-resolved 1-RDM (computed, not copied, for both spins)."""
+def solve(params: HubbardParams, theta, nup: int, ndn: int, mode: str = "f64", steps: int = 400,
+          seed: int = 0, tol: float = 1e-11) -> Solution:
+    """Ground state (Lanczos until the Ritz residual |H psi - E0 psi| < tol) and
+    the spin-resolved 1-RDM (computed, not copied, for both spins)."""
     t, U = params.unpack(theta)
     sec = _capi.Sector(params.norb, nup, ndn, _capi.ED_HUBBARD, t=t, U=U)
-    rule = LZ.EnergyRule(tol * 10, min_steps=20)
+    rule = LZ.ResidualRule(tol, min_steps=10)
     gs = LZ.ground_state(sec, mode=mode, steps=steps, seed=seed, rule=rule if mode == "f64" else None,
-                         refine_tol=tol)
+                         refine_tol=1e-14)
     gamma = one_rdm(sec, gs.psi, params.norb)
     return Solution(e0=gs.e0, psi=gs.psi, sector=sec, gamma=gamma)
 

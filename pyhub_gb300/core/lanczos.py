@@ -84,6 +84,28 @@ class EnergyRule:
         return self.converged
 
 
+class ResidualRule:
+    """Stop when the residual norm of the lowest Ritz pair, |beta_k z_k|
+    (last component of its eigenvector of T times the last beta), falls
+    below tol.  Needs the eigenvectors of T, so the driver passes them."""
+
+    wants_vectors = True
+
+    def __init__(self, tol: float, min_steps: int = 0):
+        self.tol = float(tol)
+        self.min_steps = min_steps
+        self.converged = False
+        self.ndeg = 1
+        self.residual = float("inf")
+
+    def __call__(self, val, step: int = 1 << 30, vec=None, beta_last: float = 0.0) -> bool:
+        if vec is not None:
+            self.residual = abs(beta_last * vec[-1, 0])
+            if self.residual < self.tol and step >= self.min_steps:
+                self.converged = True
+        return self.converged
+
+
 @dataclass
 class KrylovResult:
     alpha: np.ndarray
@@ -223,7 +245,8 @@ def lanczos_full(sec, v0, max_steps: int, dtype=None, rule=None, check_every: in
     for k in range(m):
         if timer is not None:
             e = timer("hv", 2.0 * sec.dim * es)
-        sec.hv(V[k], w)
+        # w = H v_k = s_k H u_k: every stored u_j keeps a norm of order ||H||
+        sec.hv(V[k], w, scale=float(s[k]))
         if timer is not None:
             e.record()
             e = timer("multidot", (k + 2) * sec.dim * es)
@@ -242,9 +265,9 @@ def lanczos_full(sec, v0, max_steps: int, dtype=None, rule=None, check_every: in
             l = sla.solve_triangular(L[:k, :k], G[k, :k], lower=True, check_finite=False)
             L[k, :k] = l
             L[k, k] = math.sqrt(max(G[k, k] - float(l @ l), 1e-300))
-        c = sv * sv[k] * a
+        c = sv * a                      # v_j . H v_k
         y = sla.cho_solve((L[: k + 1, : k + 1], True), c, check_finite=False)
-        coef = y * sv / sv[k]
+        coef = y * sv                   # w - sum_j y_j v_j = w - sum_j (y_j s_j) u_j
         ws.coef[: k + 1].copy_(torch.from_numpy(coef))
         if timer is not None:
             e = timer("update", (k + 3) * sec.dim * es)
@@ -253,7 +276,7 @@ def lanczos_full(sec, v0, max_steps: int, dtype=None, rule=None, check_every: in
             e.record()
         nw2 = float(ws.nrm[0].item())
         alpha[k] = c[k]
-        bk = sv[k] * math.sqrt(max(nw2, 0.0))
+        bk = math.sqrt(max(nw2, 0.0))
         beta[k] = bk
         k_done = k + 1
         if not math.isfinite(nw2):
@@ -264,8 +287,13 @@ def lanczos_full(sec, v0, max_steps: int, dtype=None, rule=None, check_every: in
             s[k + 1] = 1.0 / math.sqrt(nw2)
             G[k + 1, k + 1] = 1.0
         if rule is not None and (k_done % check_every == 0 or breakdown) and k_done >= min_steps:
-            val = _tridiag_eigs(alpha, beta, k_done)
-            if rule(val, k_done):
+            if getattr(rule, "wants_vectors", False):
+                val, vecs_t = _tridiag_eigs(alpha, beta, k_done, vectors=True)
+                stop = rule(val, k_done, vec=vecs_t, beta_last=beta[k_done - 1])
+            else:
+                val = _tridiag_eigs(alpha, beta, k_done)
+                stop = rule(val, k_done)
+            if stop:
                 converged = True
                 break
         if breakdown:
@@ -338,16 +366,17 @@ def lanczos_plain(sec, v0, max_steps: int, rule=None, check_every: int = NADD, n
                 for j, p in enumerate(psis):
                     ws.coef[0] = -z[k, j] * s_cur
                     _capi.update(R[cur:cur + 1], 1, ws.coef, p, p)
-            sec.hv(R[cur], R[nxt], dots=ws.dots, scratch=ws.buf)
-            a = s_cur * s_cur * float(ws.dots[0].item())
+            # R[nxt] = H v_k with v_k = s_cur u_k; dots[0] = <u_k, H v_k>
+            sec.hv(R[cur], R[nxt], scale=s_cur, dots=ws.dots, scratch=ws.buf)
+            a = s_cur * float(ws.dots[0].item())
             coef = np.zeros(3)
-            coef[cur] = a
+            coef[cur] = a * s_cur
             if k > 0:
-                coef[prv] = bprev * s_prev / s_cur
+                coef[prv] = bprev * s_prev
             ws.coef[:3].copy_(torch.from_numpy(coef))
             _capi.update(R, 3, ws.coef, R[nxt], R[nxt], norm2=ws.nrm, scratch=ws.buf)
             nw2 = float(ws.nrm[0].item())
-            b = s_cur * math.sqrt(max(nw2, 0.0))
+            b = math.sqrt(max(nw2, 0.0))
             alpha.append(a)
             beta.append(b)
             done = k + 1

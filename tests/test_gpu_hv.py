@@ -205,3 +205,25 @@ def test_lanczos_c1_ring(edlib, mode):
     psi = sec.to_ref(gs.psi).cpu().numpy()
     r = H @ psi - gs.e0 * psi
     assert np.linalg.norm(r) < 1e-6
+
+
+@pytest.mark.parametrize("dt", ["f32", "f64"])
+def test_long_lanczos_stays_bounded(edlib, dt):
+    """300 full-reorth steps: stored vectors keep norms of order ||H|| (no
+    overflow of the unnormalised basis) and the Gram matrix stays the identity."""
+    import torch
+    from pyhub_gb300.core import lanczos as LZ
+    from pyhub_gb300.tools import lattices as LT
+    t = LT.square(3, 3, -1.0)
+    sec = edlib.Sector(9, 4, 5, edlib.ED_HUBBARD, t=t, U=np.full(9, 8.0))
+    td = torch.float32 if dt == "f32" else torch.float64
+    r = LZ.lanczos_full(sec, LZ.start_vector(sec, 0, dtype=td), 300, td, keep_basis=True, want_vector=False)
+    assert r.steps == 300 or r.breakdown
+    nrm = torch.linalg.vector_norm(r.basis[: r.steps].double(), dim=1).cpu().numpy()
+    assert np.all(np.isfinite(nrm)) and nrm.max() < 1e3
+    assert r.gram_offdiag < (1e-5 if dt == "f32" else 1e-12)
+    osec = O.Sector(9, 4, 5)
+    e = O.lanczos_ref(lambda v: O.hprod_hubbard(osec, t, 8.0, v, fast=True),
+                      np.random.default_rng(0).uniform(-0.5, 0.5, osec.dim), 600, 1e-12)["eigenvalues"][0]
+    assert abs(r.ritz[0] - e) < (1e-5 if dt == "f32" else 1e-10)
+    r.release()
