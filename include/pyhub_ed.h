@@ -141,6 +141,21 @@ int ed_rdm(ed_sector *s, void *stream, int dtype, int64_t ld, const void *bra, c
 int ed_gf_start(const ed_sector *src, const ed_sector *dst, void *stream, int kind, int site,
                 int dtype, int64_t ld0, const void *psi, int out_dtype, int64_t ld1, void *out);
 
+/* ed_multidot without a scratch buffer, for callers that cannot allocate
+ * device memory: a host that hands all GPU memory to another runtime's pool,
+ * or a plug-in whose host forbids it to call the CUDA allocator, has no way
+ * to provide the scratch that ed_multidot needs.  No counterpart in the
+ * reference (its dot products run on the CPU, lanczos.f90:53-55).
+ * Same arguments and results as ed_multidot.  The partial sums live in a fixed
+ * 1 MiB device array inside the library: nvec is limited to 64 (ED_ERR_RANGE
+ * beyond), every GPU that loads the library holds the array until the
+ * process exits, and calls that overlap on the GPU race because they share
+ * it.  The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * No call allocates or frees device memory. */
+int ed_multidot_noalloc(void *stream, int dtype, int64_t n, const void *V, int64_t ldv, int nvec,
+                        const void *w, const void *z, double *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -272,3 +272,99 @@ extern "C" int ed_update(void *stream, int dtype, int out_dtype, int64_t n, cons
     if (norm2) return launch_reduce(part, grid, 1, norm2, st);
     return ED_OK;
 }
+
+// ---------------------------------------------------------------------------
+// ed_multidot_noalloc: the multi-dot for callers that cannot allocate device
+// memory and so cannot hand ed_multidot a scratch buffer.  Its per-block
+// partial sums live in a fixed file-scope device array instead.
+
+#include <mutex>
+
+namespace ed {
+
+constexpr int kNoAllocMaxNvec = 64;
+constexpr int64_t kNoAllocDoubles = (int64_t)kMaxBlocks * 2 * kNoAllocMaxNvec;  // 131072 doubles = 1 MiB
+
+// Partial sums of ed_multidot_noalloc.  Every GPU on which this library's
+// kernels are loaded holds these 1 MiB until the process exits.  All calls on
+// a device share the array: calls that overlap on the GPU race.  The kernel
+// writes every partial before the reduction reads it, so nothing is cleared
+// between calls.
+static __device__ __align__(256) double g_noalloc_partials[kNoAllocDoubles];
+
+constexpr int kNoAllocMaxDevices = 64;
+static double *g_noalloc_addr[kNoAllocMaxDevices];
+static std::mutex g_noalloc_mu;
+
+// Device address of g_noalloc_partials on the current device.  In host code
+// the array's name is only a host-side stand-in, so the address is looked up
+// once per device (with that device current) and cached.
+static int noalloc_partials(double **out)
+{
+    int dev = 0;
+    ED_CHECK_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) {
+        set_error("device %d is beyond the %d devices ed_multidot_noalloc tracks", dev, kNoAllocMaxDevices);
+        return ED_ERR_RANGE;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (g_noalloc_addr[dev] == nullptr) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+        if (e != cudaSuccess) {
+            set_error("cudaGetSymbolAddress of the fixed scratch array failed: %s", cudaGetErrorString(e));
+            return ED_ERR_CUDA;
+        }
+        g_noalloc_addr[dev] = static_cast<double *>(p);
+    }
+    *out = g_noalloc_addr[dev];
+    return ED_OK;
+}
+
+}  // namespace ed
+
+extern "C" int ed_multidot_noalloc(void *stream, int dtype, int64_t n, const void *V, int64_t ldv, int nvec,
+                                   const void *w, const void *z, double *out)
+{
+    clear_error();
+    ED_REQUIRE(dtype == ED_F32 || dtype == ED_F64, "dtype must be ED_F32 or ED_F64");
+    ED_REQUIRE(n >= 0 && nvec >= 0, "negative size");
+    ED_REQUIRE(out != nullptr, "out is NULL");
+    if (nvec > kNoAllocMaxNvec) {
+        set_error("nvec=%d exceeds the %d vectors of ed_multidot_noalloc (its scratch is a fixed %lld-byte "
+                  "device array); use ed_multidot with a scratch buffer for more",
+                  nvec, kNoAllocMaxNvec, (long long)(kNoAllocDoubles * (int64_t)sizeof(double)));
+        return ED_ERR_RANGE;
+    }
+    if (nvec == 0 || n == 0) {
+        if (nvec > 0) ED_CHECK_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * (z ? 2 : 1) * nvec, (cudaStream_t)stream));
+        return ED_OK;
+    }
+    ED_REQUIRE(V != nullptr && w != nullptr, "V or w is NULL");
+    ED_REQUIRE(ldv >= n, "ldv=%lld below n=%lld", (long long)ldv, (long long)n);
+    const size_t esz = dtype == ED_F32 ? 4 : 8;
+    ED_REQUIRE((reinterpret_cast<uintptr_t>(V) % 16) == 0 && (reinterpret_cast<uintptr_t>(w) % 16) == 0 &&
+                   (!z || (reinterpret_cast<uintptr_t>(z) % 16) == 0) && ((ldv * esz) % 16) == 0,
+               "V, w, z and the vector stride must be 16-byte aligned");
+    const int m = z ? 2 * nvec : nvec;
+    const int grid = grid_for(n);
+    if ((int64_t)grid * m > kNoAllocDoubles) {
+        set_error("%d blocks x %d sums exceed the fixed scratch of %lld doubles", grid, m, (long long)kNoAllocDoubles);
+        return ED_ERR_RANGE;
+    }
+    double *part = nullptr;
+    const int rc = noalloc_partials(&part);
+    if (rc) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t smem = sizeof(double) * 8 * (size_t)m;  // at most 8 KiB: no opt-in needed
+    if (dtype == ED_F32)
+        multidot_kernel<float><<<grid, kVecThreads, smem, st>>>(n, static_cast<const float *>(V), ldv, nvec,
+                                                               static_cast<const float *>(w),
+                                                               static_cast<const float *>(z), part);
+    else
+        multidot_kernel<double><<<grid, kVecThreads, smem, st>>>(n, static_cast<const double *>(V), ldv, nvec,
+                                                                static_cast<const double *>(w),
+                                                                static_cast<const double *>(z), part);
+    ED_CHECK_LAUNCH();
+    return launch_reduce(part, grid, m, out, st);
+}
