@@ -141,6 +141,29 @@ int ed_rdm(ed_sector *s, void *stream, int dtype, int64_t ld, const void *bra, c
 int ed_gf_start(const ed_sector *src, const ed_sector *dst, void *stream, int kind, int site,
                 int dtype, int64_t ld0, const void *psi, int out_dtype, int64_t ld1, void *out);
 
+/* A batch of independent three-term Lanczos runs, one per instance, each on
+ * its own Hubbard sector (e.g. every particle/hole start vector of every
+ * cluster of a Green's-function sweep).  Replaces the per-start-block loops
+ * of GF_BANDLANCZOS (spgf_bandlanczos.f90:309-448, called from :63-288).
+ * Vectors of all instances are concatenated: instance i occupies elements
+ * [offsets[i], offsets[i] + nsdn_i*ld_i) with ld_i = nsup_i rounded up to 32
+ * (the engine's internal row stride). */
+typedef struct ed_batch ed_batch;
+int ed_batch_create(int ninst, ed_sector *const *secs, ed_batch **out);
+int ed_batch_destroy(ed_batch *b);
+/* total elements of one concatenated vector, per-instance offsets and sizes
+ * (nsdn_i*ld_i), and the CTA count of one step (scratch sizing). */
+int ed_batch_layout(const ed_batch *b, int64_t *total, int64_t *offsets, int64_t *sizes, int64_t *nblocks);
+int64_t ed_batch_scratch_bytes(const ed_batch *b);
+/* Run nsteps Lanczos steps of every instance from the start vectors x0
+ * (concatenated, zero padding).  work: 3*total elements (two Krylov vectors
+ * and H*v).  alpha: device FP64 [ninst][nsteps]; beta: device FP64
+ * [ninst][nsteps+1] with beta[i][0] = ||x0_i|| and beta[i][k] the coupling of
+ * steps k-1 and k.  Enqueues kernels only (no host synchronisation), so the
+ * call can be captured in a CUDA graph. */
+int ed_batch_lanczos(ed_batch *b, void *stream, int dtype, void *work, const void *x0, int nsteps,
+                     double *alpha, double *beta, void *scratch, int64_t scratch_bytes);
+
 /* ed_multidot without a scratch buffer, for callers that cannot allocate
  * device memory: a host that hands all GPU memory to another runtime's pool,
  * or a plug-in whose host forbids it to call the CUDA allocator, has no way

@@ -38,6 +38,11 @@ _SIGS = {
     "ed_rdm_scratch_bytes": (_I64, [_I]),
     "ed_rdm": (_I, [_P, _P, _I, _I64, _P, _P, _I, _P, _I, _P, _P, _I64]),
     "ed_gf_start": (_I, [_P, _P, _P, _I, _I, _I, _I64, _P, _I, _I64, _P]),
+    "ed_batch_create": (_I, [_I, ctypes.POINTER(_P), ctypes.POINTER(_P)]),
+    "ed_batch_destroy": (_I, [_P]),
+    "ed_batch_layout": (_I, [_P, ctypes.POINTER(_I64), _P, _P, ctypes.POINTER(_I64)]),
+    "ed_batch_scratch_bytes": (_I64, [_P]),
+    "ed_batch_lanczos": (_I, [_P, _P, _I, _P, _P, _I, _P, _P, _P, _I64]),
 }
 
 GF_KINDS = {"h_up": 0, "h_down": 1, "e_up": 2, "e_down": 3}
@@ -231,6 +236,47 @@ class Sector:
         sb = 0 if scratch is None else scratch.numel() * scratch.element_size()
         check("ed_hv", lib().ed_hv(self._h, _stream(stream), dtype_code(x.dtype), int(ld), _ptr(x), _ptr(y),
                                    float(scale), _ptr(dots), _ptr(scratch), int(sb)))
+
+
+class Batch:
+    """ed_batch: independent three-term Lanczos runs on their own sectors."""
+
+    def __init__(self, sectors):
+        self.sectors = list(sectors)
+        arr = (_P * len(self.sectors))(*[s.handle.value for s in self.sectors])
+        h = _P()
+        check("ed_batch_create", lib().ed_batch_create(len(self.sectors), arr, ctypes.byref(h)))
+        self._h = h
+        tot, nb = _I64(), _I64()
+        off = np.zeros(len(self.sectors), dtype=np.int64)
+        sz = np.zeros(len(self.sectors), dtype=np.int64)
+        check("ed_batch_layout", lib().ed_batch_layout(h, ctypes.byref(tot), off.ctypes.data, sz.ctypes.data,
+                                                       ctypes.byref(nb)))
+        self.total, self.offsets, self.sizes, self.nblocks = tot.value, off, sz, nb.value
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().ed_batch_destroy(self._h)
+            self._h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def view(self, vec, i):
+        """Instance i's slot of a concatenated vector (internal layout of its sector)."""
+        return vec[int(self.offsets[i]): int(self.offsets[i] + self.sizes[i])]
+
+    def scratch_bytes(self):
+        return int(lib().ed_batch_scratch_bytes(self._h))
+
+    def lanczos(self, work, x0, nsteps: int, alpha, beta, scratch, stream=None):
+        sb = scratch.numel() * scratch.element_size()
+        check("ed_batch_lanczos", lib().ed_batch_lanczos(self._h, _stream(stream), dtype_code(x0.dtype), _ptr(work),
+                                                         _ptr(x0), int(nsteps), _ptr(alpha), _ptr(beta), _ptr(scratch),
+                                                         int(sb)))
 
 
 def gf_start(src: "Sector", dst: "Sector", kind: str, site: int, psi, out, stream=None):

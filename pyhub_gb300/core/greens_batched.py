@@ -1,0 +1,226 @@
+"""Batched continued-fraction Green's functions.
+
+Every particle/hole start vector of every cluster is one Lanczos instance;
+all instances advance together through ed_batch_lanczos (two kernels per
+step over all instances).  The whole fixed-length run enqueues with no host
+synchronisation, so it is captured once in a CUDA graph and replayed.  The
+per-instance alternative, one three-term Lanczos driven from the host per
+start vector (``lanczos_plain``), is kept for comparison.
+
+G^>(w) = <phi|(w + E0 - H + i eta)^-1|phi>,  phi = c^+_i psi0   (poles at E_n - E0)
+G^<(w) = <phi|(w - E0 + H + i eta)^-1|phi>,  phi = c_i psi0     (poles at E0 - E_n)
+as the reference places them (reduced_quantities.py:84-92); the retarded G_ii
+is their sum.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+from .. import _capi
+from . import lanczos as LZ
+
+
+def _torch():
+    import torch
+    return torch
+
+
+class BatchedLanczos:
+    """Fixed-length three-term Lanczos of many instances in one enqueue."""
+
+    def __init__(self, sectors, nsteps: int, dtype=None, device="cuda"):
+        torch = _torch()
+        self.dtype = dtype or torch.float32
+        self.nsteps = int(nsteps)
+        self.batch = _capi.Batch(sectors)
+        self.sectors = list(sectors)
+        n = len(self.sectors)
+        tot = self.batch.total
+        self.work = torch.zeros(3 * tot, dtype=self.dtype, device=device)
+        self.x0 = torch.zeros(tot, dtype=self.dtype, device=device)
+        self.alpha = torch.zeros((n, self.nsteps), dtype=torch.float64, device=device)
+        self.beta = torch.zeros((n, self.nsteps + 1), dtype=torch.float64, device=device)
+        self.scratch = torch.empty(self.batch.scratch_bytes() // 8 + 1, dtype=torch.float64, device=device)
+        self.graph = None
+
+    def start(self, i: int):
+        return self.batch.view(self.x0, i)
+
+    def run(self):
+        self.batch.lanczos(self.work, self.x0, self.nsteps, self.alpha, self.beta, self.scratch)
+
+    def capture(self):
+        """Record run() in a CUDA graph (after one eager run that sets kernel attributes)."""
+        torch = _torch()
+        self.run()
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.run()
+        self.graph = g
+        return g
+
+    def replay(self):
+        if self.graph is None:
+            self.capture()
+        self.graph.replay()
+
+
+def continued_fraction(alpha, beta, z, sign: float = 1.0):
+    """beta_0^2 / (z - s a_0 - b_1^2 / (z - s a_1 - ...)) for every instance
+    (rows of alpha [n, m], beta [n, m+1]) at every z (1-D complex tensor);
+    sign=-1 evaluates <phi|(z + H)^-1|phi>.  Returns [n, len(z)]."""
+    torch = _torch()
+    a = alpha.to(torch.complex128)
+    b2 = (beta[:, 1:alpha.shape[1]] ** 2).to(torch.complex128)
+    zz = z.to(torch.complex128)[None, :]
+    g = torch.zeros((alpha.shape[0], zz.shape[1]), dtype=torch.complex128, device=alpha.device)
+    m = alpha.shape[1]
+    for k in range(m - 1, -1, -1):
+        tail = b2[:, k:k + 1] * g if k < m - 1 else 0.0
+        g = 1.0 / (zz - sign * a[:, k:k + 1] - tail)
+    return (beta[:, :1] ** 2).to(torch.complex128) * g
+
+
+def plain_coefficients(sec, phi, nsteps: int):
+    """alpha, beta of one start vector by the per-instance three-term Lanczos
+    (beta[0] = ||phi||, beta[k] couples steps k-1 and k)."""
+    torch = _torch()
+    nrm = math.sqrt(float((phi.double() ** 2).sum().item()))
+    r = LZ.lanczos_plain(sec, phi, nsteps, rule=None, want_vectors=False)
+    a = np.zeros(nsteps)
+    b = np.zeros(nsteps + 1)
+    a[: len(r.alpha)] = r.alpha
+    b[0] = nrm
+    b[1: len(r.beta) + 1] = r.beta
+    return a, b
+
+
+@dataclass
+class ClusterGF:
+    e0: float
+    nup: int
+    ndn: int
+    norb: int
+    # instance index ranges in the batch: [(spin, part, site) -> instance]
+    index: dict
+
+
+def build_start_vectors(solver_sectors, src_sector, psi0, bl: BatchedLanczos, inst_of: dict):
+    """Write c|psi0> / c^+|psi0> of every (spin, part, site) into the batch
+    start vectors (instance i's slot in its sector's internal layout)."""
+    for (spin, part, site), i in inst_of.items():
+        kind = ("e_" if part == "greater" else "h_") + spin
+        # ed_gf_start converts psi0's precision to the slot's on the fly
+        _capi.gf_start(src_sector, bl.sectors[i], kind, site, psi0, bl.start(i))
+
+
+def c4_clusters(n: int = 256, seed: int = 0):
+    """Seeded cluster set of the batched Green's-function workload: half 2x6,
+    half 3x4 open-boundary square clusters, nearest-neighbour t = 1
+    (t_ij = -1), next-nearest t' ~ U[-0.3, 0.3] on the plaquette diagonals,
+    uniform U ~ U[0, 8], N_up = N_down in {5, 6}."""
+    from ..tools import lattices as LT
+    rng = np.random.default_rng(seed)
+    out = []
+    for c in range(n):
+        lx, ly = (6, 2) if c < n // 2 else (4, 3)
+        tp = float(rng.uniform(-0.3, 0.3))
+        U = float(rng.uniform(0.0, 8.0))
+        N = int(rng.choice([5, 6]))
+        out.append({"t": LT.square(lx, ly, -1.0, periodic=False, tp=tp), "U": U, "N": N, "shape": (lx, ly),
+                    "tp": tp})
+    return out
+
+
+def sweep(clusters, nsteps: int = 150, chunk: int = 64, dtype=None, gs_steps: int = 200, gs_tol: float = 1e-10,
+          omega=None, eta: float = 0.05, graph: bool = True, timings: dict = None):
+    """Ground states, then G_ii^s(w) of every cluster from its 4*norb
+    particle/hole start vectors by continued fractions.  Returns
+    {cluster: {'e0': E0, 'G': complex tensor [2 spins, norb, len(w)]}}."""
+    torch = _torch()
+    import time
+    dtype = dtype or torch.float32
+    timings = {} if timings is None else timings
+    omega = omega if omega is not None else torch.linspace(-10.0, 10.0, 2048, dtype=torch.float64, device="cuda")
+    results = {}
+    t_gs = t_start = t_lz = t_cf = 0.0
+    n_inst = 0
+    for c0 in range(0, len(clusters), chunk):
+        cl = clusters[c0:c0 + chunk]
+        secs, inst, srcs, gss = [], [], [], []
+        cache = {}
+        t0 = time.perf_counter()
+        for ci, spec in enumerate(cl):
+            norb = spec["t"].shape[0]
+            N = spec["N"]
+            U = np.full(norb, spec["U"])
+            src = _capi.Sector(norb, N, N, _capi.ED_HUBBARD, t=spec["t"], U=U)
+            gs = LZ.ground_state(src, mode="f64", steps=gs_steps, rule=LZ.ResidualRule(gs_tol, 10))
+            srcs.append(src)
+            gss.append(gs)
+            for spin in ("up", "down"):
+                for part in ("greater", "lesser"):
+                    d = 1 if part == "greater" else -1
+                    key = (ci, (N + d, N) if spin == "up" else (N, N + d))
+                    if key not in cache:
+                        cache[key] = _capi.Sector(norb, key[1][0], key[1][1], _capi.ED_HUBBARD, t=spec["t"], U=U)
+                    for site in range(1, norb + 1):
+                        inst.append((ci, spin, part, site))
+                        secs.append(cache[key])
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        bl = BatchedLanczos(secs, nsteps, dtype=dtype)
+        for i, (ci, spin, part, site) in enumerate(inst):
+            build_start_vectors(None, srcs[ci], gss[ci].psi, bl, {(spin, part, site): i})
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        if graph:
+            bl.capture()          # one eager run (also the measured one when not replaying) + capture
+            torch.cuda.synchronize()
+            t2 = time.perf_counter()
+            bl.replay()
+        else:
+            bl.run()
+        torch.cuda.synchronize()
+        t3 = time.perf_counter()
+        e0s = torch.tensor([gss[ci].e0 for (ci, _, _, _) in inst], dtype=torch.float64, device="cuda")
+        greater = torch.tensor([p == "greater" for (_, _, p, _) in inst], device="cuda")
+        zg = omega[None, :] + e0s[:, None] + 1j * eta
+        zl = omega[None, :] - e0s[:, None] + 1j * eta
+        G = torch.where(greater[:, None], _cf_rows(bl.alpha, bl.beta, zg, 1.0), _cf_rows(bl.alpha, bl.beta, zl, -1.0))
+        torch.cuda.synchronize()
+        t4 = time.perf_counter()
+        for ci in range(len(cl)):
+            norb = cl[ci]["t"].shape[0]
+            out = torch.zeros((2, norb, omega.numel()), dtype=torch.complex128, device="cuda")
+            for i, (cj, spin, part, site) in enumerate(inst):
+                if cj == ci:
+                    out[0 if spin == "up" else 1, site - 1] += G[i]
+            results[c0 + ci] = {"e0": gss[ci].e0, "G": out}
+        t_gs += t1 - t0
+        t_start += t2 - t1
+        t_lz += t3 - t2
+        t_cf += t4 - t3
+        n_inst += len(inst)
+        del bl, secs, cache, srcs, gss
+        torch.cuda.empty_cache()
+    timings.update({"ground_states_s": t_gs, "start_vectors_s": t_start, "lanczos_s": t_lz, "cf_eval_s": t_cf,
+                    "instances": n_inst, "total_s": t_gs + t_start + t_lz + t_cf})
+    return results
+
+
+def _cf_rows(alpha, beta, z, sign):
+    """continued_fraction with one z row per instance ([n, nw] complex)."""
+    torch = _torch()
+    a = alpha.to(torch.complex128)
+    b2 = (beta[:, 1:alpha.shape[1]] ** 2).to(torch.complex128)
+    g = torch.zeros_like(z, dtype=torch.complex128)
+    m = alpha.shape[1]
+    for k in range(m - 1, -1, -1):
+        tail = b2[:, k:k + 1] * g if k < m - 1 else 0.0
+        g = 1.0 / (z - sign * a[:, k:k + 1] - tail)
+    return (beta[:, :1] ** 2).to(torch.complex128) * g

@@ -1,0 +1,140 @@
+"""Batched Lanczos / continued-fraction Green's functions.
+
+Tolerances: batched FP64 alpha/beta vs the per-instance three-term Lanczos
+1e-9 relative over 30 steps; batched continued fraction vs the oracle's FP64
+full-reorthogonalisation Lanczos of the same length (25 steps) 1e-8; G_ii(w)
+(eta = 0.1) of a 6-site open cluster after 200 steps vs the exact Lehmann sum
+1e-4 (convergence of the fraction); CUDA-graph replay bit-identical to the
+eager run; FP32 vectors after 200 steps within 1e-3 of the Lehmann sum."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(edlib, norb=6, nup=3, ndn=3, nsteps=30, dtype="f64"):
+    import torch
+    from pyhub_gb300.core import greens_batched as GB
+    from pyhub_gb300.core import lanczos as LZ
+    from pyhub_gb300.tools import lattices as LT
+    t = LT.square(3, 2, -1.0, periodic=False, tp=0.2)
+    U = np.full(norb, 3.0)
+    src = edlib.Sector(norb, nup, ndn, edlib.ED_HUBBARD, t=t, U=U)
+    gs = LZ.ground_state(src, mode="f64", steps=120, rule=LZ.ResidualRule(1e-12, 10))
+    secs, inst = [], {}
+    cache = {}
+    for spin in ("up", "down"):
+        for part in ("greater", "lesser"):
+            d = 1 if part == "greater" else -1
+            key = (nup + d, ndn) if spin == "up" else (nup, ndn + d)
+            if key not in cache:
+                cache[key] = edlib.Sector(norb, key[0], key[1], edlib.ED_HUBBARD, t=t, U=U)
+            for site in range(1, norb + 1):
+                inst[(spin, part, site)] = len(secs)
+                secs.append(cache[key])
+    td = torch.float64 if dtype == "f64" else torch.float32
+    bl = GB.BatchedLanczos(secs, nsteps, dtype=td)
+    GB.build_start_vectors(secs, src, gs.psi, bl, inst)
+    return t, U, src, gs, secs, inst, bl
+
+
+def test_batched_matches_per_instance(edlib):
+    import torch
+    from pyhub_gb300.core import greens_batched as GB
+    t, U, src, gs, secs, inst, bl = _setup(edlib)
+    bl.run()
+    torch.cuda.synchronize()
+    A, B = bl.alpha.cpu().numpy(), bl.beta.cpu().numpy()
+    for key in [("up", "greater", 1), ("down", "lesser", 4), ("up", "lesser", 6)]:
+        i = inst[key]
+        phi = bl.start(i).clone()
+        a, b = GB.plain_coefficients(secs[i], phi, bl.nsteps)
+        n = np.count_nonzero(b[1:] > 1e-8)
+        assert np.allclose(A[i, :n], a[:n], rtol=1e-9, atol=1e-9), key
+        assert np.allclose(B[i, :n + 1], b[:n + 1], rtol=1e-9, atol=1e-9), key
+
+
+def test_batched_graph_replay_is_identical(edlib):
+    import torch
+    t, U, src, gs, secs, inst, bl = _setup(edlib, nsteps=40)
+    bl.run()
+    torch.cuda.synchronize()
+    a0, b0 = bl.alpha.clone(), bl.beta.clone()
+    bl.capture()
+    bl.alpha.zero_()
+    bl.beta.zero_()
+    bl.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(bl.alpha, a0) and torch.equal(bl.beta, b0)
+
+
+def test_batched_cf_matches_oracle_lanczos(edlib):
+    """25 steps (before any loss of orthogonality): the batched continued
+    fraction equals the oracle's FP64 full-reorthogonalisation Lanczos
+    continued fraction of the same start vector, to 1e-8."""
+    import torch
+    from pyhub_gb300.core import greens_batched as GB
+    t, U, src, gs, secs, inst, bl = _setup(edlib, nsteps=25)
+    bl.run()
+    w = np.linspace(-8, 8, 201)
+    z = torch.tensor(w + gs.e0 + 0.1j, device="cuda")
+    g = GB.continued_fraction(bl.alpha, bl.beta, z).cpu().numpy()
+    for key in [("up", "greater", 2), ("down", "greater", 5)]:
+        i = inst[key]
+        osec = O.Sector(6, secs[i].nup, secs[i].ndn)
+        phi = secs[i].to_ref(bl.start(i)).cpu().numpy()
+        a, b, n2 = O.lanczos_tridiag(lambda v: O.hprod_hubbard(osec, t, U, v, fast=True), phi, 25)
+        ref = O.continued_fraction(a, b, n2, w + gs.e0 + 0.1j)
+        assert np.abs(g[i] - ref).max() < 1e-8 * max(1.0, np.abs(ref).max()), key
+
+
+def test_batched_gf_converges_to_lehmann(edlib):
+    """200 steps: G_ii(w) at eta = 0.1 within 1e-4 of the exact Lehmann sum."""
+    import torch
+    from pyhub_gb300.core import greens_batched as GB
+    t, U, src, gs, secs, inst, bl = _setup(edlib, nsteps=200)
+    bl.run()
+    w = torch.linspace(-8, 8, 401, dtype=torch.float64, device="cuda")
+    eta = 0.1
+    gr = GB.continued_fraction(bl.alpha, bl.beta, w + gs.e0 + 1j * eta, sign=1.0)
+    le = GB.continued_fraction(bl.alpha, bl.beta, w - gs.e0 + 1j * eta, sign=-1.0)
+    osec = O.Sector(6, 3, 3)
+    psi = src.to_ref(gs.psi).cpu().numpy()
+    ref = O.lehmann_gf_diag(osec, t, U, psi, gs.e0, 6)
+    wn = w.cpu().numpy()
+    for spin in ("up", "down"):
+        for site in range(1, 7):
+            got = (gr[inst[(spin, "greater", site)]] + le[inst[(spin, "lesser", site)]]).cpu().numpy()
+            exact = 0
+            for part in ("greater", "lesser"):
+                pos, Q = ref[spin][part]
+                exact = exact + O.poles_eval(pos, Q[site - 1] ** 2, wn, eta)
+            assert np.abs(got - exact).max() < 1e-4, (spin, site, np.abs(got - exact).max())
+
+
+def test_batched_fp32_converges_to_lehmann(edlib):
+    """FP32 vectors (FP64 scalars), 200 steps: G_ii(w) at eta = 0.1 within 1e-3
+    of the exact Lehmann sum."""
+    import torch
+    from pyhub_gb300.core import greens_batched as GB
+    t, U, src, gs, secs, inst, bl = _setup(edlib, nsteps=200, dtype="f32")
+    bl.run()
+    w = torch.linspace(-8, 8, 401, dtype=torch.float64, device="cuda")
+    eta = 0.1
+    gr = GB.continued_fraction(bl.alpha, bl.beta, w + gs.e0 + 1j * eta, sign=1.0)
+    le = GB.continued_fraction(bl.alpha, bl.beta, w - gs.e0 + 1j * eta, sign=-1.0)
+    osec = O.Sector(6, 3, 3)
+    ref = O.lehmann_gf_diag(osec, t, U, src.to_ref(gs.psi).cpu().numpy(), gs.e0, 6)
+    wn = w.cpu().numpy()
+    worst = 0.0
+    for spin in ("up", "down"):
+        for site in range(1, 7):
+            got = (gr[inst[(spin, "greater", site)]] + le[inst[(spin, "lesser", site)]]).cpu().numpy()
+            exact = 0
+            for part in ("greater", "lesser"):
+                pos, Q = ref[spin][part]
+                exact = exact + O.poles_eval(pos, Q[site - 1] ** 2, wn, eta)
+            worst = max(worst, np.abs(got - exact).max())
+    assert worst < 1e-3, worst
