@@ -163,6 +163,17 @@ int64_t ed_batch_scratch_bytes(const ed_batch *b);
  * call can be captured in a CUDA graph. */
 int ed_batch_lanczos(ed_batch *b, void *stream, int dtype, void *work, const void *x0, int nsteps,
                      double *alpha, double *beta, void *scratch, int64_t scratch_bytes);
+/* Replay of ed_batch_lanczos from the same x0 that also accumulates, per
+ * instance, the Ritz vector out_i += sum_k coef[i][k] q_k (q_k the
+ * normalised Lanczos vectors; coef device FP64 [ninst][nsteps], typically the
+ * eigenvector of the instance's tridiagonal matrix for its lowest Ritz
+ * value).  out: concatenated, same dtype and layout as x0, accumulated into
+ * (zero it first).  The replay recomputes bit-identical q_k, so the pair
+ * ed_batch_lanczos + ed_batch_ritz is the batched two-pass ground-state
+ * Lanczos of LANCZOS/READ_PSI (lanczos.f90:17-86, compute_solver.f90:270-290). */
+int ed_batch_ritz(ed_batch *b, void *stream, int dtype, void *work, const void *x0, int nsteps,
+                  double *alpha, double *beta, const double *coef, void *out, void *scratch,
+                  int64_t scratch_bytes);
 
 /* ed_multidot without a scratch buffer, for callers that cannot allocate
  * device memory: a host that hands all GPU memory to another runtime's pool,

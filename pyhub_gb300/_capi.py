@@ -43,6 +43,7 @@ _SIGS = {
     "ed_batch_layout": (_I, [_P, ctypes.POINTER(_I64), _P, _P, ctypes.POINTER(_I64)]),
     "ed_batch_scratch_bytes": (_I64, [_P]),
     "ed_batch_lanczos": (_I, [_P, _P, _I, _P, _P, _I, _P, _P, _P, _I64]),
+    "ed_batch_ritz": (_I, [_P, _P, _I, _P, _P, _I, _P, _P, _P, _P, _P, _I64]),
 }
 
 GF_KINDS = {"h_up": 0, "h_down": 1, "e_up": 2, "e_down": 3}
@@ -277,6 +278,13 @@ class Batch:
         check("ed_batch_lanczos", lib().ed_batch_lanczos(self._h, _stream(stream), dtype_code(x0.dtype), _ptr(work),
                                                          _ptr(x0), int(nsteps), _ptr(alpha), _ptr(beta), _ptr(scratch),
                                                          int(sb)))
+
+    def ritz(self, work, x0, nsteps: int, alpha, beta, coef, out, scratch, stream=None):
+        """Replay of lanczos() accumulating out_i += sum_k coef[i, k] q_k."""
+        sb = scratch.numel() * scratch.element_size()
+        check("ed_batch_ritz", lib().ed_batch_ritz(self._h, _stream(stream), dtype_code(x0.dtype), _ptr(work),
+                                                   _ptr(x0), int(nsteps), _ptr(alpha), _ptr(beta), _ptr(coef),
+                                                   _ptr(out), _ptr(scratch), int(sb)))
 
 
 def gf_start(src: "Sector", dst: "Sector", kind: str, site: int, psi, out, stream=None):

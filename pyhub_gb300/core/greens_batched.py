@@ -69,6 +69,75 @@ class BatchedLanczos:
         self.graph.replay()
 
 
+@dataclass
+class BatchedGroundStates:
+    e0: np.ndarray          # [n] lowest Ritz values
+    residual: np.ndarray    # [n] beta_m |y_m| of the lowest Ritz pair
+    psi: list               # [n] normalised ground states (views into one device vector)
+    restarts: int
+
+
+def _lowest_ritz(a, b, tol_break: float = 1e-12):
+    """Lowest eigenpair of one instance's tridiagonal matrix, cut at the first
+    vanishing beta (an exhausted Krylov space); returns (theta, y, residual, m)."""
+    import scipy.linalg as sla
+    scale = max(1.0, float(np.abs(a).max()) if a.size else 1.0)
+    m = len(a)
+    for k in range(1, len(a)):
+        if b[k] <= tol_break * scale:
+            m = k
+            break
+    if m == 1:
+        return float(a[0]), np.ones(1), float(b[1]), 1
+    w, y = sla.eigh_tridiagonal(a[:m], b[1:m], select="i", select_range=(0, 0))
+    return float(w[0]), y[:, 0], float(b[m] * abs(y[m - 1, 0])), m
+
+
+def batched_ground_states(sectors, nsteps: int = 120, tol: float = 1e-10, max_restarts: int = 6, seed: int = 0,
+                          dtype=None) -> BatchedGroundStates:
+    """Ground states of many sectors at once: every sector is an instance of
+    the batched three-term Lanczos (ed_batch_lanczos), the lowest Ritz pair of
+    each tridiagonal matrix is found on the host, and a replay of the same
+    run (ed_batch_ritz) accumulates the Ritz vectors -- the two-pass scheme of
+    the reference's ground-state solve (lanczos.f90:17-86 for the
+    coefficients, compute_solver.f90:270-290 for V*c).  Instances whose
+    residual beta_m |y_m| is above tol * max(1, |E0|) restart from their Ritz
+    vector (all instances are re-run; converged ones keep converging)."""
+    torch = _torch()
+    dtype = dtype or torch.float64
+    bl = BatchedLanczos(sectors, nsteps, dtype=dtype)
+    n = len(bl.sectors)
+    for i, sec in enumerate(bl.sectors):
+        bl.start(i).copy_(LZ.start_vector(sec, seed + i, dtype=dtype))
+    out = torch.zeros_like(bl.x0)
+    coef = torch.zeros((n, nsteps), dtype=torch.float64, device=bl.x0.device)
+    e0 = np.zeros(n)
+    res = np.full(n, np.inf)
+    it = 0
+    while True:
+        bl.run()
+        A = bl.alpha.cpu().numpy()
+        B = bl.beta.cpu().numpy()
+        C = np.zeros((n, nsteps))
+        for i in range(n):
+            theta, y, r, m = _lowest_ritz(A[i], B[i])
+            e0[i], res[i] = theta, r
+            C[i, :m] = y
+        coef.copy_(torch.from_numpy(C))
+        out.zero_()
+        bl.batch.ritz(bl.work, bl.x0, nsteps, bl.alpha, bl.beta, coef, out, bl.scratch)
+        for i in range(n):
+            v = bl.batch.view(out, i)
+            v /= torch.linalg.vector_norm(v)
+        done = res <= tol * np.maximum(1.0, np.abs(e0))
+        if done.all() or it >= max_restarts:
+            break
+        bl.x0.copy_(out)
+        it += 1
+    psi = [bl.batch.view(out, i) for i in range(n)]
+    return BatchedGroundStates(e0=e0.copy(), residual=res.copy(), psi=psi, restarts=it)
+
+
 def continued_fraction(alpha, beta, z, sign: float = 1.0):
     """beta_0^2 / (z - s a_0 - b_1^2 / (z - s a_1 - ...)) for every instance
     (rows of alpha [n, m], beta [n, m+1]) at every z (1-D complex tensor);
@@ -136,11 +205,12 @@ def c4_clusters(n: int = 256, seed: int = 0):
     return out
 
 
-def sweep(clusters, nsteps: int = 150, chunk: int = 64, dtype=None, gs_steps: int = 200, gs_tol: float = 1e-10,
+def sweep(clusters, nsteps: int = 150, chunk: int = 64, dtype=None, gs_steps: int = 120, gs_tol: float = 1e-10,
           omega=None, eta: float = 0.05, graph: bool = True, timings: dict = None):
-    """Ground states, then G_ii^s(w) of every cluster from its 4*norb
-    particle/hole start vectors by continued fractions.  Returns
-    {cluster: {'e0': E0, 'G': complex tensor [2 spins, norb, len(w)]}}."""
+    """Ground states (batched over the clusters of a chunk), then G_ii^s(w)
+    of every cluster from its 4*norb particle/hole start vectors by
+    continued fractions (batched over all start vectors of the chunk).
+    Returns {cluster: {'e0': E0, 'G': complex tensor [2 spins, norb, len(w)]}}."""
     torch = _torch()
     import time
     dtype = dtype or torch.float32
@@ -149,37 +219,41 @@ def sweep(clusters, nsteps: int = 150, chunk: int = 64, dtype=None, gs_steps: in
     results = {}
     t_gs = t_start = t_lz = t_cf = 0.0
     n_inst = 0
+    restarts = 0
     for c0 in range(0, len(clusters), chunk):
         cl = clusters[c0:c0 + chunk]
-        secs, inst, srcs, gss = [], [], [], []
-        cache = {}
+        secs, inst, srcs = [], [], []
+        base = []
         t0 = time.perf_counter()
         for ci, spec in enumerate(cl):
             norb = spec["t"].shape[0]
             N = spec["N"]
             U = np.full(norb, spec["U"])
-            src = _capi.Sector(norb, N, N, _capi.ED_HUBBARD, t=spec["t"], U=U)
-            gs = LZ.ground_state(src, mode="f64", steps=gs_steps, rule=LZ.ResidualRule(gs_tol, 10))
-            srcs.append(src)
-            gss.append(gs)
+            srcs.append(_capi.Sector(norb, N, N, _capi.ED_HUBBARD, t=spec["t"], U=U))
+            cache = {}
+            base.append(len(inst))
+            # instance order inside a cluster: spin (up, down) x part (greater, lesser) x site
             for spin in ("up", "down"):
                 for part in ("greater", "lesser"):
                     d = 1 if part == "greater" else -1
-                    key = (ci, (N + d, N) if spin == "up" else (N, N + d))
+                    key = (N + d, N) if spin == "up" else (N, N + d)
                     if key not in cache:
-                        cache[key] = _capi.Sector(norb, key[1][0], key[1][1], _capi.ED_HUBBARD, t=spec["t"], U=U)
+                        cache[key] = _capi.Sector(norb, key[0], key[1], _capi.ED_HUBBARD, t=spec["t"], U=U)
                     for site in range(1, norb + 1):
                         inst.append((ci, spin, part, site))
                         secs.append(cache[key])
+        gsb = batched_ground_states(srcs, nsteps=gs_steps, tol=gs_tol, seed=c0)
+        restarts = max(restarts, gsb.restarts)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         bl = BatchedLanczos(secs, nsteps, dtype=dtype)
         for i, (ci, spin, part, site) in enumerate(inst):
-            build_start_vectors(None, srcs[ci], gss[ci].psi, bl, {(spin, part, site): i})
+            kind = ("e_" if part == "greater" else "h_") + spin
+            _capi.gf_start(srcs[ci], secs[i], kind, site, gsb.psi[ci], bl.start(i))
         torch.cuda.synchronize()
         t2 = time.perf_counter()
         if graph:
-            bl.capture()          # one eager run (also the measured one when not replaying) + capture
+            bl.capture()          # one eager run (sets kernel attributes) + capture
             torch.cuda.synchronize()
             t2 = time.perf_counter()
             bl.replay()
@@ -187,29 +261,26 @@ def sweep(clusters, nsteps: int = 150, chunk: int = 64, dtype=None, gs_steps: in
             bl.run()
         torch.cuda.synchronize()
         t3 = time.perf_counter()
-        e0s = torch.tensor([gss[ci].e0 for (ci, _, _, _) in inst], dtype=torch.float64, device="cuda")
+        e0s = torch.tensor([gsb.e0[ci] for (ci, _, _, _) in inst], dtype=torch.float64, device="cuda")
         greater = torch.tensor([p == "greater" for (_, _, p, _) in inst], device="cuda")
         zg = omega[None, :] + e0s[:, None] + 1j * eta
         zl = omega[None, :] - e0s[:, None] + 1j * eta
         G = torch.where(greater[:, None], _cf_rows(bl.alpha, bl.beta, zg, 1.0), _cf_rows(bl.alpha, bl.beta, zl, -1.0))
-        torch.cuda.synchronize()
-        t4 = time.perf_counter()
         for ci in range(len(cl)):
             norb = cl[ci]["t"].shape[0]
-            out = torch.zeros((2, norb, omega.numel()), dtype=torch.complex128, device="cuda")
-            for i, (cj, spin, part, site) in enumerate(inst):
-                if cj == ci:
-                    out[0 if spin == "up" else 1, site - 1] += G[i]
-            results[c0 + ci] = {"e0": gss[ci].e0, "G": out}
+            g = G[base[ci]: base[ci] + 4 * norb].view(2, 2, norb, -1).sum(dim=1)
+            results[c0 + ci] = {"e0": float(gsb.e0[ci]), "G": g}
+        torch.cuda.synchronize()
+        t4 = time.perf_counter()
         t_gs += t1 - t0
         t_start += t2 - t1
         t_lz += t3 - t2
         t_cf += t4 - t3
         n_inst += len(inst)
-        del bl, secs, cache, srcs, gss
+        del bl, secs, srcs, gsb
         torch.cuda.empty_cache()
     timings.update({"ground_states_s": t_gs, "start_vectors_s": t_start, "lanczos_s": t_lz, "cf_eval_s": t_cf,
-                    "instances": n_inst, "total_s": t_gs + t_start + t_lz + t_cf})
+                    "instances": n_inst, "total_s": t_gs + t_start + t_lz + t_cf, "gs_restarts": restarts})
     return results
 
 

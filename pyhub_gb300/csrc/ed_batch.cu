@@ -53,34 +53,24 @@ struct ed_batch {
     int64_t total = 0;                 // elements of one concatenated vector
     int64_t nblocks = 0;
     ed::BatchInst *dev = nullptr;      // [ninst]
-    int64_t *blk_start = nullptr;      // [ninst+1] device
-    double **u_site_bufs = nullptr;
+    int32_t *blk_inst = nullptr;       // [nblocks] device: instance of every CTA
+    double *u_site_all = nullptr;      // [ninst][kMaxSites] device
     std::vector<int64_t> offsets, dims;
-    std::vector<double *> u_site_dev;
     int max_nsup = 0;
     int max_ld = 0;
 };
 
 namespace ed {
 
-__device__ __forceinline__ int find_inst(const int64_t *__restrict__ blk_start, int ninst, int64_t b)
-{
-    int lo = 0, hi = ninst - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (__ldg(blk_start + mid) <= b) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
+// Per-instance scalars, kept on the device between the kernels of a step.
+enum { kS = 0, kSPrev = 1, kBeta = 2, kCCur = 3, kCPrev = 4, kScal = 8 };
 
-template <typename T>
-__device__ __forceinline__ double inst_reduce(const double *__restrict__ part, int64_t b0, int n)
+__device__ __forceinline__ double sum_partials_warp(const double *__restrict__ part, int64_t b0, int n)
 {
-    // every CTA of an instance sums its partials in the same order: identical values
+    // fixed lane/order pattern: the same partials always give the same sum
     double s = 0.0;
-    for (int i = 0; i < n; ++i) s += part[b0 + i];
-    return s;
+    for (int q = threadIdx.x & 31; q < n; q += 32) s += part[b0 + q];
+    return warp_sum(s);
 }
 
 template <typename T>
@@ -96,207 +86,232 @@ __device__ __forceinline__ T u_energy_b(const BatchInst &a, uint32_t both)
     return e;
 }
 
+__device__ __forceinline__ void block_partial(double v, double *__restrict__ out)
+{
+    __shared__ double red[kBatchThreads / 32];
+    v = warp_sum(v);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < kBatchThreads / 32; ++w) t += red[w];
+        *out = t;
+    }
+}
+
 // Norms of the start vectors: partial ||x0||^2 per CTA.
 template <typename T>
 __global__ void __launch_bounds__(kBatchThreads) batch_norm_kernel(const BatchInst *__restrict__ inst,
-                                                                   const int64_t *__restrict__ blk_start, int ninst,
+                                                                   const int32_t *__restrict__ blk_inst,
                                                                    const T *__restrict__ x, double *__restrict__ part)
 {
     const int64_t b = blockIdx.x;
-    const int i = find_inst(blk_start, ninst, b);
-    const BatchInst a = inst[i];
+    const BatchInst &a = inst[__ldg(blk_inst + b)];
     const int64_t r0 = (b - a.blk0) * kRows;
+    const int nr = (int)min((int64_t)kRows, a.nsdn - r0);
     double s = 0.0;
-    for (int r = 0; r < kRows; ++r) {
-        const int64_t d = r0 + r;
-        if (d >= a.nsdn) break;
-        const T *row = x + a.off + d * a.ld;
-        for (int64_t u = threadIdx.x; u < a.nsup; u += blockDim.x) s += (double)row[u] * (double)row[u];
+    for (int r = 0; r < nr; ++r) {
+        const T *row = x + a.off + (r0 + r) * a.ld;
+        for (int64_t c = threadIdx.x; c < a.nsup; c += blockDim.x) s += (double)row[c] * (double)row[c];
     }
-    __shared__ double red[kBatchThreads / 32];
-    s = warp_sum(s);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int w = 0; w < kBatchThreads / 32; ++w) t += red[w];
-        part[b] = t;
+    block_partial(s, part + b);
+}
+
+// One warp per instance.  mode 0 (after a norm / update pass):
+//   beta_k = sqrt(sum), s_{k-1} <- s_k, s_k = 1/beta_k; beta[i][k] written.
+// mode 1 (after the H*v pass of step k):
+//   alpha_k = s_k sum <u_k, y>; c_cur = alpha_k s_k, c_prev = beta_k s_{k-1}.
+__global__ void batch_scalar_kernel(const BatchInst *__restrict__ inst, int ninst, const double *__restrict__ part,
+                                    double *__restrict__ scal, double *__restrict__ alpha,
+                                    double *__restrict__ beta, int k, int nsteps, int mode)
+{
+    const int i = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (i >= ninst) return;
+    const BatchInst &a = inst[i];
+    const double sum = sum_partials_warp(part, a.blk0, a.nblk);
+    if ((threadIdx.x & 31) != 0) return;
+    double *sc = scal + (int64_t)i * kScal;
+    if (mode == 0) {
+        const double bk = sqrt(fmax(sum, 0.0));
+        sc[kSPrev] = (k == 0) ? 0.0 : sc[kS];
+        sc[kS] = (bk > 1e-150) ? 1.0 / bk : 0.0;
+        sc[kBeta] = bk;
+        beta[(int64_t)i * (nsteps + 1) + k] = bk;
+    } else {
+        const double al = sc[kS] * sum;
+        alpha[(int64_t)i * nsteps + k] = al;
+        sc[kCCur] = al * sc[kS];
+        sc[kCPrev] = sc[kBeta] * sc[kSPrev];
     }
 }
 
-// y = s_k H u_k and partial <u_k, y>; s_k from the partials of the previous
-// update (or of the start-vector norms at k = 0).  kRows rows of u_k are
-// staged in shared memory; each warp takes 32-string slices of a row: the up
-// hops walk the sector's sliced-ELL slots (coalesced) and gather from the
-// staged row, the down hops read the neighbour rows' slice from L2 with the
-// row's neighbour list held one entry per lane.
+constexpr int kMaxNb = 48;   // down-hop neighbours of a row staged in shared memory
+
+// y = s_k H u_k and partial <u_k, y>.  kRows rows of u_k are staged in shared
+// memory.  A warp owns 32-string slices and computes all kRows rows of its
+// slice at once: each up-hop slot (sector's sliced-ELL table, coalesced) is
+// loaded once and applied to every staged row; the down hops read the
+// neighbour rows' slice from L2 (the instances in flight keep their vectors
+// there), with the CTA's neighbour lists staged in shared memory.
 template <typename T>
 __global__ void __launch_bounds__(kBatchThreads) batch_hv_kernel(const BatchInst *__restrict__ inst,
-                                                                 const int64_t *__restrict__ blk_start, int ninst,
+                                                                 const int32_t *__restrict__ blk_inst,
                                                                  const T *__restrict__ u, T *__restrict__ y,
-                                                                 const double *__restrict__ part_in,
-                                                                 double *__restrict__ part_out,
-                                                                 double *__restrict__ beta, int k, int nsteps)
+                                                                 const double *__restrict__ scal,
+                                                                 double *__restrict__ part_out)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *xs = reinterpret_cast<T *>(smem_raw);
-    __shared__ double red[kBatchThreads / 32];
-    __shared__ double s_k;
+    __shared__ int nb_src[kRows][kMaxNb];
+    __shared__ T nb_cf[kRows][kMaxNb];
+    __shared__ int nb_n[kRows], nb_e0[kRows];
+    __shared__ uint32_t row_str[kRows];
+    __shared__ T row_ed[kRows];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = kBatchThreads / 32;
     const int64_t b = blockIdx.x;
-    const int i = find_inst(blk_start, ninst, b);
-    const BatchInst a = inst[i];
-    if (threadIdx.x == 0) {
-        const double nb = inst_reduce<T>(part_in, a.blk0, a.nblk);
-        const double bk = sqrt(fmax(nb, 0.0));
-        s_k = (bk > 1e-150) ? 1.0 / bk : 0.0;
-        if (b == a.blk0) beta[(int64_t)i * (nsteps + 1) + k] = bk;
-    }
+    const int i = __ldg(blk_inst + b);
+    const BatchInst &a = inst[i];
     const int64_t r0 = (b - a.blk0) * kRows;
     const int nr = (int)min((int64_t)kRows, a.nsdn - r0);
-    const int64_t sld = a.ld;
+    const int64_t nsup = a.nsup, ld = a.ld;
     const T *ub = u + a.off;
-    for (int r = 0; r < nr; ++r)
-        for (int64_t c = threadIdx.x; c < a.nsup; c += blockDim.x) xs[r * sld + c] = ub[(r0 + r) * a.ld + c];
-    __syncthreads();
-    const T sc = (T)s_k;
-    const T *ecf = (sizeof(T) == 4) ? reinterpret_cast<const T *>(a.ell_cf32) : reinterpret_cast<const T *>(a.ell_cf64);
     const T *dcf = (sizeof(T) == 4) ? reinterpret_cast<const T *>(a.dcf32) : reinterpret_cast<const T *>(a.dcf64);
+    // stage rows (zeros past the instance's last row) and the rows' down-hop lists
+    for (int r = 0; r < kRows; ++r) {
+        const T *src = ub + (r0 + r) * ld;
+        for (int64_t c = threadIdx.x; c < ld; c += blockDim.x) xs[r * ld + c] = (r < nr) ? src[c] : (T)0;
+    }
+    if (warp < kRows) {
+        const int r = warp;
+        int e0 = 0, nn = 0;
+        if (r < nr) {
+            e0 = __ldg(a.dptr + r0 + r);
+            nn = __ldg(a.dptr + r0 + r + 1) - e0;
+        }
+        for (int e = lane; e < min(nn, kMaxNb); e += 32) {
+            nb_src[r][e] = __ldg(a.dsrc + e0 + e);
+            nb_cf[r][e] = __ldg(dcf + e0 + e);
+        }
+        if (lane == 0) {
+            nb_n[r] = nn;
+            nb_e0[r] = e0;
+            row_str[r] = (r < nr) ? __ldg(a.dstr + r0 + r) : 0u;
+            row_ed[r] = (r < nr) ? (T)__ldg(a.dediag + r0 + r) : (T)0;
+        }
+    }
+    __syncthreads();
+    const T sc = (T)scal[(int64_t)i * kScal + kS];
+    const T *ecf = (sizeof(T) == 4) ? reinterpret_cast<const T *>(a.ell_cf32) : reinterpret_cast<const T *>(a.ell_cf64);
     T dotp = 0;
-    for (int r = 0; r < nr; ++r) {
-        const int64_t d = r0 + r;
-        const uint32_t sd = __ldg(a.dstr + d);
-        const T ed = (T)__ldg(a.dediag + d);
-        const int e0 = __ldg(a.dptr + d), nn = __ldg(a.dptr + d + 1) - e0;
-        const int my_src = (lane < nn) ? __ldg(a.dsrc + e0 + lane) : 0;
-        const T my_cf = (lane < nn) ? __ldg(dcf + e0 + lane) : (T)0;
-        for (int sl = warp; sl < a.nslice; sl += nwarps) {
-            const int64_t c = (int64_t)sl * 32 + lane;
-            const bool ok = c < a.nsup;
-            const int64_t cc = ok ? c : a.nsup - 1;
-            const uint32_t su = __ldg(a.ustr + cc);
-            const T xv = xs[r * sld + cc];
-            T acc = ((T)__ldg(a.uediag + cc) + ed + u_energy_b<T>(a, su & sd)) * xv;
-            const int s0 = __ldg(a.ell_off + sl), ns = __ldg(a.ell_off + sl + 1) - s0;
-            const int32_t *sp = a.ell_src + (int64_t)s0 * 32 + lane;
-            const T *cp = ecf + (int64_t)s0 * 32 + lane;
-            for (int q = 0; q < ns; ++q) acc += __ldg(cp + q * 32) * xs[r * sld + __ldg(sp + q * 32)];
-            // down hops: the row's neighbour list (<= 32 entries) is spread over the lanes
-            for (int e = 0; e < min(nn, 32); ++e) {
-                const int src = __shfl_sync(0xffffffffu, my_src, e);
-                const T wgt = __shfl_sync(0xffffffffu, my_cf, e);
-                acc += wgt * ub[(int64_t)src * a.ld + cc];
-            }
-            for (int e = 32; e < nn; ++e) acc += __ldg(dcf + e0 + e) * ub[(int64_t)__ldg(a.dsrc + e0 + e) * a.ld + cc];
-            acc *= sc;
+    for (int sl = warp; sl < a.nslice; sl += nwarps) {
+        const int64_t c = (int64_t)sl * 32 + lane;
+        const bool ok = c < nsup;
+        const int64_t cc = ok ? c : nsup - 1;
+        const uint32_t su = __ldg(a.ustr + cc);
+        const T ued = (T)__ldg(a.uediag + cc);
+        T acc[kRows];
+#pragma unroll
+        for (int r = 0; r < kRows; ++r) acc[r] = (ued + row_ed[r] + u_energy_b<T>(a, su & row_str[r])) * xs[r * ld + cc];
+        const int s0 = __ldg(a.ell_off + sl), ns = __ldg(a.ell_off + sl + 1) - s0;
+        const int32_t *sp = a.ell_src + (int64_t)s0 * 32 + lane;
+        const T *cp = ecf + (int64_t)s0 * 32 + lane;
+#pragma unroll 2
+        for (int q = 0; q < ns; ++q) {
+            const int src = __ldg(sp + q * 32);
+            const T w = __ldg(cp + q * 32);
+#pragma unroll
+            for (int r = 0; r < kRows; ++r) acc[r] += w * xs[r * ld + src];
+        }
+#pragma unroll
+        for (int r = 0; r < kRows; ++r) {
+            if (r >= nr) break;
+            const int nn = nb_n[r];
+            const int nl = min(nn, kMaxNb);
+            T ar = 0;
+#pragma unroll 4
+            for (int e = 0; e < nl; ++e) ar += nb_cf[r][e] * ub[(int64_t)nb_src[r][e] * ld + cc];
+            for (int e = kMaxNb; e < nn; ++e)
+                ar += __ldg(dcf + nb_e0[r] + e) * ub[(int64_t)__ldg(a.dsrc + nb_e0[r] + e) * ld + cc];
+            const T v = (acc[r] + ar) * sc;
             if (ok) {
-                y[a.off + d * a.ld + c] = acc;
-                dotp += xv * acc;
+                y[a.off + (r0 + r) * ld + c] = v;
+                dotp += xs[r * ld + cc] * v;
             }
         }
     }
-    double dot = warp_sum((double)dotp);
-    if (lane == 0) red[warp] = dot;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int w = 0; w < kBatchThreads / 32; ++w) t += red[w];
-        part_out[b] = t;
-    }
+    block_partial((double)dotp, part_out + b);
 }
 
-// u_next = y - alpha_k s_k u_k - beta_k s_{k-1} u_prev (written over u_prev),
-// partial ||u_next||^2; alpha_k = s_k sum <u_k,y> partials.
+// u_next = y - c_cur u_k - c_prev u_prev (written over u_prev), partial
+// ||u_next||^2.  With ritz_coef, also out += ritz_coef[i][k] s_k u_k (the
+// Ritz vector sum_k y_k q_k of a replayed run).
 template <typename T>
 __global__ void __launch_bounds__(kBatchThreads) batch_update_kernel(const BatchInst *__restrict__ inst,
-                                                                     const int64_t *__restrict__ blk_start, int ninst,
+                                                                     const int32_t *__restrict__ blk_inst,
                                                                      const T *__restrict__ y, const T *__restrict__ u,
-                                                                     T *__restrict__ up,
-                                                                     const double *__restrict__ part_dot,
+                                                                     T *__restrict__ up, const double *__restrict__ scal,
                                                                      double *__restrict__ part_nrm,
-                                                                     const double *__restrict__ beta,
-                                                                     double *__restrict__ alpha, int k, int nsteps)
+                                                                     const double *__restrict__ ritz_coef,
+                                                                     T *__restrict__ ritz_out, int k, int nsteps)
 {
-    __shared__ double red[kBatchThreads / 32];
-    __shared__ double c_cur, c_prev;
     const int64_t b = blockIdx.x;
-    const int i = find_inst(blk_start, ninst, b);
-    const BatchInst a = inst[i];
-    if (threadIdx.x == 0) {
-        const double bk = beta[(int64_t)i * (nsteps + 1) + k];
-        const double sk = (bk > 1e-150) ? 1.0 / bk : 0.0;
-        const double al = sk * inst_reduce<T>(part_dot, a.blk0, a.nblk);
-        if (b == a.blk0) alpha[(int64_t)i * nsteps + k] = al;
-        c_cur = al * sk;
-        if (k > 0) {
-            const double bp = beta[(int64_t)i * (nsteps + 1) + k - 1];
-            const double sp = (bp > 1e-150) ? 1.0 / bp : 0.0;
-            c_prev = bk * sp;
-        } else {
-            c_prev = 0.0;
-        }
-    }
-    __syncthreads();
-    const T cc = (T)c_cur, cp = (T)c_prev;
+    const int i = __ldg(blk_inst + b);
+    const BatchInst &a = inst[i];
+    const double *sc = scal + (int64_t)i * kScal;
+    const T cc = (T)sc[kCCur], cp = (T)sc[kCPrev];
+    const T cr = ritz_coef ? (T)(ritz_coef[(int64_t)i * nsteps + k] * sc[kS]) : (T)0;
     const int64_t r0 = (b - a.blk0) * kRows;
     const int nr = (int)min((int64_t)kRows, a.nsdn - r0);
     T sp = 0;
     for (int r = 0; r < nr; ++r) {
         const int64_t base = a.off + (r0 + r) * a.ld;
         for (int64_t c = threadIdx.x; c < a.nsup; c += blockDim.x) {
-            const T v = y[base + c] - cc * u[base + c] - cp * up[base + c];
+            const T uk = u[base + c];
+            const T v = y[base + c] - cc * uk - cp * up[base + c];
             up[base + c] = v;
             sp += v * v;
+            if (ritz_out) ritz_out[base + c] += cr * uk;
         }
     }
-    double s = warp_sum((double)sp);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int w = 0; w < kBatchThreads / 32; ++w) t += red[w];
-        part_nrm[b] = t;
-    }
-}
-
-// beta of the last step from the last update's partials.
-__global__ void batch_last_beta_kernel(const ed::BatchInst *__restrict__ inst, int ninst,
-                                       const double *__restrict__ part, double *__restrict__ beta, int nsteps)
-{
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ninst; i += gridDim.x * blockDim.x) {
-        const BatchInst a = inst[i];
-        double s = 0.0;
-        for (int q = 0; q < a.nblk; ++q) s += part[a.blk0 + q];
-        beta[(int64_t)i * (nsteps + 1) + nsteps] = sqrt(fmax(s, 0.0));
-    }
+    block_partial((double)sp, part_nrm + b);
 }
 
 template <typename T>
 static int run_batch(ed_batch *bt, cudaStream_t st, T *work, const T *x0, int nsteps, double *alpha, double *beta,
-                     double *scratch)
+                     double *scratch, const double *ritz_coef, T *ritz_out)
 {
     const int64_t tot = bt->total;
     T *U[2] = {work, work + tot};
     T *Y = work + 2 * tot;
-    double *pa = scratch, *pb = scratch + bt->nblocks;
+    double *pa = scratch, *pb = scratch + bt->nblocks, *scal = scratch + 2 * bt->nblocks;
     const size_t smem = (size_t)kRows * bt->max_ld * sizeof(T);
     const unsigned nb = (unsigned)bt->nblocks;
+    const unsigned ns = (unsigned)((bt->ninst * 32 + 255) / 256);
     // u_{k+1} overwrites u_{k-1} in place, so u_k lives in slot k % 2
     ED_CHECK_CUDA(cudaMemcpyAsync(U[0], x0, sizeof(T) * tot, cudaMemcpyDeviceToDevice, st));
     ED_CHECK_CUDA(cudaMemsetAsync(U[1], 0, sizeof(T) * tot, st));
-    batch_norm_kernel<T><<<nb, kBatchThreads, 0, st>>>(bt->dev, bt->blk_start, bt->ninst, U[0], pb);
+    if (nb > 0) {
+        batch_norm_kernel<T><<<nb, kBatchThreads, 0, st>>>(bt->dev, bt->blk_inst, U[0], pb);
+        ED_CHECK_LAUNCH();
+    }
+    batch_scalar_kernel<<<ns, 256, 0, st>>>(bt->dev, bt->ninst, pb, scal, alpha, beta, 0, nsteps, 0);
     ED_CHECK_LAUNCH();
     for (int k = 0; k < nsteps; ++k) {
         T *uk = U[k % 2], *uprev = U[(k + 1) % 2];
-        batch_hv_kernel<T><<<nb, kBatchThreads, smem, st>>>(bt->dev, bt->blk_start, bt->ninst, uk, Y, pb, pa, beta,
-                                                             k, nsteps);
+        if (nb > 0) {
+            batch_hv_kernel<T><<<nb, kBatchThreads, smem, st>>>(bt->dev, bt->blk_inst, uk, Y, scal, pa);
+            ED_CHECK_LAUNCH();
+        }
+        batch_scalar_kernel<<<ns, 256, 0, st>>>(bt->dev, bt->ninst, pa, scal, alpha, beta, k, nsteps, 1);
         ED_CHECK_LAUNCH();
-        batch_update_kernel<T><<<nb, kBatchThreads, 0, st>>>(bt->dev, bt->blk_start, bt->ninst, Y, uk, uprev, pa, pb,
-                                                             beta, alpha, k, nsteps);
+        if (nb > 0) {
+            batch_update_kernel<T><<<nb, kBatchThreads, 0, st>>>(bt->dev, bt->blk_inst, Y, uk, uprev, scal, pb,
+                                                                 ritz_coef, ritz_out, k, nsteps);
+            ED_CHECK_LAUNCH();
+        }
+        batch_scalar_kernel<<<ns, 256, 0, st>>>(bt->dev, bt->ninst, pb, scal, alpha, beta, k + 1, nsteps, 0);
         ED_CHECK_LAUNCH();
     }
-    batch_last_beta_kernel<<<(bt->ninst + 127) / 128, 128, 0, st>>>(bt->dev, bt->ninst, pb, beta, nsteps);
-    ED_CHECK_LAUNCH();
     return ED_OK;
 }
 
@@ -310,26 +325,23 @@ extern "C" int ed_batch_create(int ninst, ed_sector *const *secs, ed_batch **out
     ED_REQUIRE(out != nullptr, "out is NULL");
     *out = nullptr;
     ED_REQUIRE(ninst >= 1 && secs != nullptr, "need at least one instance");
-    ed_batch *bt = new ed_batch();
-    bt->ninst = ninst;
     std::vector<BatchInst> host((size_t)ninst);
-    std::vector<int64_t> bstart((size_t)ninst + 1);
+    std::vector<double> usite((size_t)ninst * kMaxSites);
+    std::vector<int32_t> binst;
+    std::vector<int64_t> offsets, dims;
     int64_t off = 0, blk = 0;
+    int max_nsup = 0, max_ld = 0;
     for (int i = 0; i < ninst; ++i) {
         const ed_sector *s = secs[i];
-        if (!s || s->kind != ED_HUBBARD) {
-            delete bt;
-            set_error("instance %d is not a Hubbard sector", i);
-            return ED_ERR_ARG;
-        }
-        if ((size_t)kRows * ((s->nsup + 31) / 32 * 32) * sizeof(double) > 200 * 1024) {
-            delete bt;
+        ED_REQUIRE(s != nullptr && s->kind == ED_HUBBARD, "instance %d is not a Hubbard sector", i);
+        const int64_t ld = (s->nsup + 31) / 32 * 32;   // the internal row stride of pyhub_gb300 vectors
+        if ((size_t)kRows * ld * sizeof(double) > 200 * 1024) {
             set_error("instance %d: rows of %lld strings are too long for the batched kernel", i, (long long)s->nsup);
             return ED_ERR_RANGE;
         }
         BatchInst &a = host[(size_t)i];
         a.nsup = s->nsup; a.nsdn = s->nsdn;
-        a.ld = (s->nsup + 31) / 32 * 32;   // the internal row stride of pyhub_gb300 vectors
+        a.ld = ld;
         a.off = off;
         a.ustr = s->up.str; a.dstr = s->dn.str;
         a.uptr = s->up.ptr; a.usrc = s->up.src; a.dptr = s->dn.ptr; a.dsrc = s->dn.src;
@@ -338,39 +350,49 @@ extern "C" int ed_batch_create(int ninst, ed_sector *const *secs, ed_batch **out
         a.ell_off = s->up.ell_off; a.ell_src = s->up.ell_src;
         a.ell_cf32 = s->up.ell_cf32; a.ell_cf64 = s->up.ell_cf64;
         a.nslice = (int)s->up.nslice;
-        double *us = nullptr;
-        if (cudaMalloc(&us, sizeof(double) * kMaxSites) != cudaSuccess ||
-            cudaMemcpy(us, s->u_site, sizeof(double) * kMaxSites, cudaMemcpyHostToDevice) != cudaSuccess) {
-            set_error("allocation of batch parameters failed");
-            ed_batch_destroy(bt);
-            return ED_ERR_MEM;
-        }
-        bt->u_site_dev.push_back(us);
-        a.u_site = us;
+        for (int q = 0; q < kMaxSites; ++q) usite[(size_t)i * kMaxSites + q] = s->u_site[q];
+        a.u_site = nullptr;   // set after the upload below
         a.u_value = s->u_value;
         a.u_uniform = s->u_uniform ? 1 : 0;
         a.blk0 = blk;
         a.nblk = (int)((s->nsdn + kRows - 1) / kRows);
-        bstart[(size_t)i] = blk;
+        for (int q = 0; q < a.nblk; ++q) binst.push_back(i);
         blk += a.nblk;
-        bt->offsets.push_back(off);
-        bt->dims.push_back(s->nsdn * a.ld);
-        off += s->nsdn * a.ld;
+        offsets.push_back(off);
+        dims.push_back(s->nsdn * ld);
+        off += s->nsdn * ld;
         off = (off + 31) / 32 * 32;  // keep every instance 128-byte aligned
-        bt->max_nsup = std::max(bt->max_nsup, (int)s->nsup);
-        bt->max_ld = std::max(bt->max_ld, (int)a.ld);
+        max_nsup = std::max(max_nsup, (int)s->nsup);
+        max_ld = std::max(max_ld, (int)ld);
     }
-    bstart[(size_t)ninst] = blk;
+    ED_REQUIRE(blk < (int64_t)INT32_MAX, "batch of %lld CTAs is too large", (long long)blk);
+    ed_batch *bt = new ed_batch();
+    bt->ninst = ninst;
     bt->total = off;
     bt->nblocks = blk;
+    bt->offsets = std::move(offsets);
+    bt->dims = std::move(dims);
+    bt->max_nsup = max_nsup;
+    bt->max_ld = max_ld;
+    // one allocation per table: creating a batch of thousands of instances costs a few copies
     if (cudaMalloc(&bt->dev, sizeof(BatchInst) * ninst) != cudaSuccess ||
-        cudaMalloc(&bt->blk_start, sizeof(int64_t) * (ninst + 1)) != cudaSuccess) {
+        cudaMalloc(&bt->u_site_all, sizeof(double) * usite.size()) != cudaSuccess ||
+        (blk > 0 && cudaMalloc(&bt->blk_inst, sizeof(int32_t) * (size_t)blk) != cudaSuccess)) {
+        cudaGetLastError();
         set_error("allocation of batch descriptors failed");
         ed_batch_destroy(bt);
         return ED_ERR_MEM;
     }
-    ED_CHECK_CUDA(cudaMemcpy(bt->dev, host.data(), sizeof(BatchInst) * ninst, cudaMemcpyHostToDevice));
-    ED_CHECK_CUDA(cudaMemcpy(bt->blk_start, bstart.data(), sizeof(int64_t) * (ninst + 1), cudaMemcpyHostToDevice));
+    for (int i = 0; i < ninst; ++i) host[(size_t)i].u_site = bt->u_site_all + (size_t)i * kMaxSites;
+    if (cudaMemcpy(bt->dev, host.data(), sizeof(BatchInst) * ninst, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(bt->u_site_all, usite.data(), sizeof(double) * usite.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+        (blk > 0 && cudaMemcpy(bt->blk_inst, binst.data(), sizeof(int32_t) * (size_t)blk, cudaMemcpyHostToDevice) !=
+                        cudaSuccess)) {
+        const cudaError_t e = cudaGetLastError();
+        set_error("upload of batch descriptors failed: %s", cudaGetErrorString(e));
+        ed_batch_destroy(bt);
+        return ED_ERR_CUDA;
+    }
     *out = bt;
     return ED_OK;
 }
@@ -378,9 +400,9 @@ extern "C" int ed_batch_create(int ninst, ed_sector *const *secs, ed_batch **out
 extern "C" int ed_batch_destroy(ed_batch *bt)
 {
     if (!bt) return ED_OK;
-    for (double *p : bt->u_site_dev) cudaFree(p);
     if (bt->dev) cudaFree(bt->dev);
-    if (bt->blk_start) cudaFree(bt->blk_start);
+    if (bt->blk_inst) cudaFree(bt->blk_inst);
+    if (bt->u_site_all) cudaFree(bt->u_site_all);
     delete bt;
     return ED_OK;
 }
@@ -401,13 +423,12 @@ extern "C" int ed_batch_layout(const ed_batch *bt, int64_t *total, int64_t *offs
 extern "C" int64_t ed_batch_scratch_bytes(const ed_batch *bt)
 {
     if (!bt) return -1;
-    return 2 * bt->nblocks * (int64_t)sizeof(double) + 256;
+    return (2 * bt->nblocks + (int64_t)kScal * bt->ninst) * (int64_t)sizeof(double) + 256;
 }
 
-extern "C" int ed_batch_lanczos(ed_batch *bt, void *stream, int dtype, void *work, const void *x0, int nsteps,
-                                double *alpha, double *beta, void *scratch, int64_t scratch_bytes)
+static int batch_launch(ed_batch *bt, void *stream, int dtype, void *work, const void *x0, int nsteps, double *alpha,
+                        double *beta, const double *ritz_coef, void *ritz_out, void *scratch, int64_t scratch_bytes)
 {
-    clear_error();
     ED_REQUIRE(bt != nullptr && work != nullptr && x0 != nullptr && alpha != nullptr && beta != nullptr,
                "NULL argument");
     ED_REQUIRE(dtype == ED_F32 || dtype == ED_F64, "dtype must be ED_F32 or ED_F64");
@@ -418,9 +439,27 @@ extern "C" int ed_batch_lanczos(ed_batch *bt, void *stream, int dtype, void *wor
     if (dtype == ED_F32) {
         const size_t smem = (size_t)kRows * bt->max_ld * sizeof(float);
         ED_CHECK_CUDA(cudaFuncSetAttribute(batch_hv_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        return run_batch<float>(bt, st, (float *)work, (const float *)x0, nsteps, alpha, beta, (double *)scratch);
+        return run_batch<float>(bt, st, (float *)work, (const float *)x0, nsteps, alpha, beta, (double *)scratch,
+                                ritz_coef, (float *)ritz_out);
     }
     const size_t smem = (size_t)kRows * bt->max_ld * sizeof(double);
     ED_CHECK_CUDA(cudaFuncSetAttribute(batch_hv_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    return run_batch<double>(bt, st, (double *)work, (const double *)x0, nsteps, alpha, beta, (double *)scratch);
+    return run_batch<double>(bt, st, (double *)work, (const double *)x0, nsteps, alpha, beta, (double *)scratch,
+                             ritz_coef, (double *)ritz_out);
+}
+
+extern "C" int ed_batch_lanczos(ed_batch *bt, void *stream, int dtype, void *work, const void *x0, int nsteps,
+                                double *alpha, double *beta, void *scratch, int64_t scratch_bytes)
+{
+    clear_error();
+    return batch_launch(bt, stream, dtype, work, x0, nsteps, alpha, beta, nullptr, nullptr, scratch, scratch_bytes);
+}
+
+extern "C" int ed_batch_ritz(ed_batch *bt, void *stream, int dtype, void *work, const void *x0, int nsteps,
+                             double *alpha, double *beta, const double *coef, void *out, void *scratch,
+                             int64_t scratch_bytes)
+{
+    clear_error();
+    ED_REQUIRE(coef != nullptr && out != nullptr, "NULL argument");
+    return batch_launch(bt, stream, dtype, work, x0, nsteps, alpha, beta, coef, out, scratch, scratch_bytes);
 }
