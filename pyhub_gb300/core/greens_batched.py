@@ -53,9 +53,9 @@ class BatchedLanczos:
         self.batch.lanczos(self.work, self.x0, self.nsteps, self.alpha, self.beta, self.scratch)
 
     def capture(self):
-        """Record run() in a CUDA graph (after one eager run that sets kernel attributes)."""
+        """Record run() in a CUDA graph (the batch set its kernels' attributes
+        when it was created, so nothing but stream work is captured)."""
         torch = _torch()
-        self.run()
         torch.cuda.synchronize()
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
@@ -72,14 +72,15 @@ class BatchedLanczos:
 @dataclass
 class BatchedGroundStates:
     e0: np.ndarray          # [n] lowest Ritz values
-    residual: np.ndarray    # [n] beta_m |y_m| of the lowest Ritz pair
-    psi: list               # [n] normalised ground states (views into one device vector)
-    restarts: int
+    residual: np.ndarray    # [n] ||H psi - E0 psi|| of the returned (normalised) vectors
+    psi: list               # [n] normalised FP64 ground states (views into one device vector)
+    restarts: int           # FP64 cycles after the first
 
 
 def _lowest_ritz(a, b, tol_break: float = 1e-12):
     """Lowest eigenpair of one instance's tridiagonal matrix, cut at the first
-    vanishing beta (an exhausted Krylov space); returns (theta, y, residual, m)."""
+    vanishing beta (an exhausted Krylov space); returns (theta, y, estimate, m)
+    with the usual estimate beta_m |y_m| of the residual."""
     import scipy.linalg as sla
     scale = max(1.0, float(np.abs(a).max()) if a.size else 1.0)
     m = len(a)
@@ -93,49 +94,82 @@ def _lowest_ritz(a, b, tol_break: float = 1e-12):
     return float(w[0]), y[:, 0], float(b[m] * abs(y[m - 1, 0])), m
 
 
-def batched_ground_states(sectors, nsteps: int = 120, tol: float = 1e-10, max_restarts: int = 6, seed: int = 0,
-                          dtype=None) -> BatchedGroundStates:
-    """Ground states of many sectors at once: every sector is an instance of
-    the batched three-term Lanczos (ed_batch_lanczos), the lowest Ritz pair of
-    each tridiagonal matrix is found on the host, and a replay of the same
-    run (ed_batch_ritz) accumulates the Ritz vectors -- the two-pass scheme of
-    the reference's ground-state solve (lanczos.f90:17-86 for the
-    coefficients, compute_solver.f90:270-290 for V*c).  Instances whose
-    residual beta_m |y_m| is above tol * max(1, |E0|) restart from their Ritz
-    vector (all instances are re-run; converged ones keep converging)."""
+def _ritz_cycle(bl, out):
+    """One batched Lanczos run, the lowest Ritz pair of every instance, and
+    the replay that accumulates the Ritz vectors into `out` (normalised)."""
     torch = _torch()
-    dtype = dtype or torch.float64
-    bl = BatchedLanczos(sectors, nsteps, dtype=dtype)
-    n = len(bl.sectors)
-    for i, sec in enumerate(bl.sectors):
-        bl.start(i).copy_(LZ.start_vector(sec, seed + i, dtype=dtype))
-    out = torch.zeros_like(bl.x0)
-    coef = torch.zeros((n, nsteps), dtype=torch.float64, device=bl.x0.device)
+    n, nsteps = len(bl.sectors), bl.nsteps
+    bl.run()
+    A = bl.alpha.cpu().numpy()
+    B = bl.beta.cpu().numpy()
+    C = np.zeros((n, nsteps))
     e0 = np.zeros(n)
-    res = np.full(n, np.inf)
+    for i in range(n):
+        theta, y, _, m = _lowest_ritz(A[i], B[i])
+        e0[i] = theta
+        C[i, :m] = y
+    coef = torch.from_numpy(C).to(bl.x0.device)
+    out.zero_()
+    bl.batch.ritz(bl.work, bl.x0, nsteps, bl.alpha, bl.beta, coef, out, bl.scratch)
+    for i in range(n):
+        v = bl.batch.view(out, i)
+        v /= torch.linalg.vector_norm(v)
+    return e0
+
+
+def _true_residuals(bl, out, e0):
+    """||H psi_i - E0_i psi_i|| of every instance (per-sector FP64 H*v)."""
+    torch = _torch()
+    res = torch.empty(len(bl.sectors), dtype=torch.float64, device=out.device)
+    for i, sec in enumerate(bl.sectors):
+        v = bl.batch.view(out, i)
+        y = torch.zeros_like(v)       # ed_hv leaves the row padding untouched
+        sec.hv(v, y)
+        res[i] = torch.linalg.vector_norm(y - e0[i] * v)
+    return res.cpu().numpy()
+
+
+def batched_ground_states(sectors, nsteps: int = 120, tol: float = 1e-10, max_restarts: int = 8, seed: int = 0,
+                          mixed: bool = True, refine_steps: int = 60) -> BatchedGroundStates:
+    """Ground states of many sectors at once.  Every sector is an instance of
+    the batched three-term Lanczos (ed_batch_lanczos); the lowest Ritz pair
+    of each tridiagonal matrix is found on the host and a replay of the same
+    run (ed_batch_ritz) accumulates the Ritz vectors -- the two-pass scheme
+    of the reference's ground-state solve (lanczos.f90:17-86 for the
+    coefficients, compute_solver.f90:270-290 for V*c).
+
+    mixed=True: a first cycle of nsteps with FP32 vectors, then FP64 cycles
+    of refine_steps restarted from the previous Ritz vector; mixed=False:
+    FP64 cycles of nsteps from the start.  Cycles repeat (all instances; the
+    converged ones keep improving) until every true residual
+    ||H psi - E0 psi|| is below tol, at most max_restarts FP64 cycles after
+    the first."""
+    torch = _torch()
+    starts = [LZ.start_vector(sec, seed + i, dtype=torch.float64) for i, sec in enumerate(sectors)]
+    if mixed:
+        b32 = BatchedLanczos(sectors, nsteps, dtype=torch.float32)
+        for i, v in enumerate(starts):
+            b32.start(i).copy_(v)
+        out32 = torch.zeros_like(b32.x0)
+        _ritz_cycle(b32, out32)
+        bl = BatchedLanczos(sectors, refine_steps, dtype=torch.float64)
+        bl.x0.copy_(out32)
+        del b32, out32
+    else:
+        bl = BatchedLanczos(sectors, nsteps, dtype=torch.float64)
+        for i, v in enumerate(starts):
+            bl.start(i).copy_(v)
+    out = torch.zeros_like(bl.x0)
     it = 0
     while True:
-        bl.run()
-        A = bl.alpha.cpu().numpy()
-        B = bl.beta.cpu().numpy()
-        C = np.zeros((n, nsteps))
-        for i in range(n):
-            theta, y, r, m = _lowest_ritz(A[i], B[i])
-            e0[i], res[i] = theta, r
-            C[i, :m] = y
-        coef.copy_(torch.from_numpy(C))
-        out.zero_()
-        bl.batch.ritz(bl.work, bl.x0, nsteps, bl.alpha, bl.beta, coef, out, bl.scratch)
-        for i in range(n):
-            v = bl.batch.view(out, i)
-            v /= torch.linalg.vector_norm(v)
-        done = res <= tol * np.maximum(1.0, np.abs(e0))
-        if done.all() or it >= max_restarts:
+        e0 = _ritz_cycle(bl, out)
+        res = _true_residuals(bl, out, e0)
+        if (res <= tol).all() or it >= max_restarts:
             break
         bl.x0.copy_(out)
         it += 1
-    psi = [bl.batch.view(out, i) for i in range(n)]
-    return BatchedGroundStates(e0=e0.copy(), residual=res.copy(), psi=psi, restarts=it)
+    psi = [bl.batch.view(out, i) for i in range(len(bl.sectors))]
+    return BatchedGroundStates(e0=e0, residual=res, psi=psi, restarts=it)
 
 
 def continued_fraction(alpha, beta, z, sign: float = 1.0):
@@ -253,9 +287,7 @@ def sweep(clusters, nsteps: int = 150, chunk: int = 64, dtype=None, gs_steps: in
         torch.cuda.synchronize()
         t2 = time.perf_counter()
         if graph:
-            bl.capture()          # one eager run (sets kernel attributes) + capture
-            torch.cuda.synchronize()
-            t2 = time.perf_counter()
+            bl.capture()
             bl.replay()
         else:
             bl.run()

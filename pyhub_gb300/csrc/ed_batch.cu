@@ -21,6 +21,7 @@
 #include "ed_common.cuh"
 
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 namespace ed {
@@ -39,6 +40,7 @@ struct BatchInst {
     const int32_t *ell_off, *ell_src; // sliced-ELL up-hop table of the sector
     const float *ell_cf32;
     const double *ell_cf64;
+    const int2 *ell_pk32;
     int nslice;
     double u_value;
     int u_uniform;
@@ -145,14 +147,99 @@ __global__ void batch_scalar_kernel(const BatchInst *__restrict__ inst, int nins
     }
 }
 
-constexpr int kMaxNb = 48;   // down-hop neighbours of a row staged in shared memory
+constexpr int kMaxNb = 48;      // down-hop neighbours of a row staged in shared memory
 
-// y = s_k H u_k and partial <u_k, y>.  kRows rows of u_k are staged in shared
-// memory.  A warp owns 32-string slices and computes all kRows rows of its
-// slice at once: each up-hop slot (sector's sliced-ELL table, coalesced) is
-// loaded once and applied to every staged row; the down hops read the
-// neighbour rows' slice from L2 (the instances in flight keep their vectors
-// there), with the CTA's neighbour lists staged in shared memory.
+// 16-byte vectors: float4 / double2.
+template <typename T> struct V16;
+template <> struct V16<float> {
+    using type = float4;
+    static constexpr int n = 4;
+};
+template <> struct V16<double> {
+    using type = double2;
+    static constexpr int n = 2;
+};
+__device__ __forceinline__ float &vat(float4 &v, int k) { return reinterpret_cast<float *>(&v)[k]; }
+__device__ __forceinline__ double &vat(double2 &v, int k) { return reinterpret_cast<double *>(&v)[k]; }
+
+// A down-hop neighbour: element offset of the source row and its coefficient.
+template <typename T> struct alignas(sizeof(T) == 4 ? 8 : 16) NbEnt {
+    int off;
+    T cf;
+};
+
+// Column c of the staged block: rows 0..kRows-1 of string c, padded to a
+// 16-byte multiple that spreads consecutive columns over all bank groups
+// (48 B for FP32, 80 B for FP64).
+template <typename T> __host__ __device__ constexpr int staged_stride() { return kRows + 16 / (int)sizeof(T); }
+
+template <typename T>
+__device__ __forceinline__ void load_column(const T *p, T (&v)[kRows])
+{
+    using V = typename V16<T>::type;
+#pragma unroll
+    for (int q = 0; q < kRows / V16<T>::n; ++q) {
+        const V w = reinterpret_cast<const V *>(p)[q];
+#pragma unroll
+        for (int k = 0; k < V16<T>::n; ++k) v[q * V16<T>::n + k] = reinterpret_cast<const T *>(&w)[k];
+    }
+}
+
+// G up-hop slots of one lane (table entries at `at`, `at`+32, ...): the G
+// table loads are issued before the first gather.
+template <typename T, int G>
+__device__ __forceinline__ void up_group(const BatchInst &a, const T *xs, int at, T (&acc)[kRows])
+{
+    constexpr int S = staged_stride<T>();
+    int src[G];
+    T w[G];
+#pragma unroll
+    for (int j = 0; j < G; ++j) {
+        if (sizeof(T) == 4) {
+            const int2 pk = __ldg(a.ell_pk32 + at + 32 * j);
+            src[j] = pk.x;
+            w[j] = (T)__int_as_float(pk.y);
+        } else {
+            src[j] = __ldg(a.ell_src + at + 32 * j);
+            w[j] = (T)__ldg(a.ell_cf64 + at + 32 * j);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < G; ++j) {
+        T xv[kRows];
+        load_column(xs + src[j] * S, xv);
+#pragma unroll
+        for (int r = 0; r < kRows; ++r) acc[r] += w[j] * xv[r];
+    }
+}
+
+// G down-hop neighbour rows (16-byte vector v of each): loads issued together.
+template <typename T, int G>
+__device__ __forceinline__ void down_group(const NbEnt<T> *en, const T *__restrict__ ub, int v,
+                                           typename V16<T>::type &acc)
+{
+    using V = typename V16<T>::type;
+    V xn[G];
+    T cf[G];
+#pragma unroll
+    for (int j = 0; j < G; ++j) {
+        const NbEnt<T> e = en[j];
+        cf[j] = e.cf;
+        xn[j] = __ldg(reinterpret_cast<const V *>(ub + e.off) + v);
+    }
+#pragma unroll
+    for (int j = 0; j < G; ++j)
+#pragma unroll
+        for (int k = 0; k < V16<T>::n; ++k) vat(acc, k) += cf[j] * reinterpret_cast<const T *>(&xn[j])[k];
+}
+
+// y = s_k H u_k and partial <u_k, y> over kRows rows of one instance.
+// Phase A (diagonal + up hops): the rows are staged in shared memory one
+// column per string; a warp owns 32-string slices, loads each sliced-ELL
+// slot once and applies it to all rows with 16-byte shared loads; the sums
+// go to y.  Phase B (down hops): each row adds its neighbour rows as
+// 16-byte-vector axpys read from L2 (the instances in flight keep their
+// vectors there), then scales, stores and forms the dot product.
 template <typename T>
 __global__ void __launch_bounds__(kBatchThreads) batch_hv_kernel(const BatchInst *__restrict__ inst,
                                                                  const int32_t *__restrict__ blk_inst,
@@ -160,10 +247,12 @@ __global__ void __launch_bounds__(kBatchThreads) batch_hv_kernel(const BatchInst
                                                                  const double *__restrict__ scal,
                                                                  double *__restrict__ part_out)
 {
+    using V = typename V16<T>::type;
+    constexpr int VN = V16<T>::n;
+    constexpr int S = staged_stride<T>();
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *xs = reinterpret_cast<T *>(smem_raw);
-    __shared__ int nb_src[kRows][kMaxNb];
-    __shared__ T nb_cf[kRows][kMaxNb];
+    T *xs = reinterpret_cast<T *>(smem_raw);   // [nsup][S]
+    __shared__ NbEnt<T> nb[kRows][kMaxNb];
     __shared__ int nb_n[kRows], nb_e0[kRows];
     __shared__ uint32_t row_str[kRows];
     __shared__ T row_ed[kRows];
@@ -171,15 +260,15 @@ __global__ void __launch_bounds__(kBatchThreads) batch_hv_kernel(const BatchInst
     const int64_t b = blockIdx.x;
     const int i = __ldg(blk_inst + b);
     const BatchInst &a = inst[i];
-    const int64_t r0 = (b - a.blk0) * kRows;
+    const int r0 = (int)((b - a.blk0) * kRows);
     const int nr = (int)min((int64_t)kRows, a.nsdn - r0);
-    const int64_t nsup = a.nsup, ld = a.ld;
+    const int nsup = (int)a.nsup, ld = (int)a.ld;
     const T *ub = u + a.off;
+    T *yb = y + a.off + (int64_t)r0 * ld;
     const T *dcf = (sizeof(T) == 4) ? reinterpret_cast<const T *>(a.dcf32) : reinterpret_cast<const T *>(a.dcf64);
-    // stage rows (zeros past the instance's last row) and the rows' down-hop lists
     for (int r = 0; r < kRows; ++r) {
-        const T *src = ub + (r0 + r) * ld;
-        for (int64_t c = threadIdx.x; c < ld; c += blockDim.x) xs[r * ld + c] = (r < nr) ? src[c] : (T)0;
+        const T *src = ub + (int64_t)(r0 + r) * ld;
+        for (int c = threadIdx.x; c < nsup; c += blockDim.x) xs[c * S + r] = (r < nr) ? src[c] : (T)0;
     }
     if (warp < kRows) {
         const int r = warp;
@@ -189,8 +278,8 @@ __global__ void __launch_bounds__(kBatchThreads) batch_hv_kernel(const BatchInst
             nn = __ldg(a.dptr + r0 + r + 1) - e0;
         }
         for (int e = lane; e < min(nn, kMaxNb); e += 32) {
-            nb_src[r][e] = __ldg(a.dsrc + e0 + e);
-            nb_cf[r][e] = __ldg(dcf + e0 + e);
+            nb[r][e].off = __ldg(a.dsrc + e0 + e) * ld;
+            nb[r][e].cf = __ldg(dcf + e0 + e);
         }
         if (lane == 0) {
             nb_n[r] = nn;
@@ -200,51 +289,74 @@ __global__ void __launch_bounds__(kBatchThreads) batch_hv_kernel(const BatchInst
         }
     }
     __syncthreads();
-    const T sc = (T)scal[(int64_t)i * kScal + kS];
-    const T *ecf = (sizeof(T) == 4) ? reinterpret_cast<const T *>(a.ell_cf32) : reinterpret_cast<const T *>(a.ell_cf64);
-    T dotp = 0;
+    // ---- phase A
     for (int sl = warp; sl < a.nslice; sl += nwarps) {
-        const int64_t c = (int64_t)sl * 32 + lane;
+        const int c = sl * 32 + lane;
         const bool ok = c < nsup;
-        const int64_t cc = ok ? c : nsup - 1;
+        const int cc = ok ? c : nsup - 1;
         const uint32_t su = __ldg(a.ustr + cc);
         const T ued = (T)__ldg(a.uediag + cc);
-        T acc[kRows];
+        T acc[kRows], xv[kRows];
+        load_column(xs + cc * S, xv);
 #pragma unroll
-        for (int r = 0; r < kRows; ++r) acc[r] = (ued + row_ed[r] + u_energy_b<T>(a, su & row_str[r])) * xs[r * ld + cc];
+        for (int r = 0; r < kRows; ++r) acc[r] = (ued + row_ed[r] + u_energy_b<T>(a, su & row_str[r])) * xv[r];
         const int s0 = __ldg(a.ell_off + sl), ns = __ldg(a.ell_off + sl + 1) - s0;
-        const int32_t *sp = a.ell_src + (int64_t)s0 * 32 + lane;
-        const T *cp = ecf + (int64_t)s0 * 32 + lane;
-#pragma unroll 2
-        for (int q = 0; q < ns; ++q) {
-            const int src = __ldg(sp + q * 32);
-            const T w = __ldg(cp + q * 32);
-#pragma unroll
-            for (int r = 0; r < kRows; ++r) acc[r] += w * xs[r * ld + src];
+        // slots in groups: all table loads of a group are in flight before
+        // its first gather
+        int q = 0;
+        for (; q + 8 <= ns; q += 8) up_group<T, 8>(a, xs, (s0 + q) * 32 + lane, acc);
+        if (q + 4 <= ns) {
+            up_group<T, 4>(a, xs, (s0 + q) * 32 + lane, acc);
+            q += 4;
         }
+        for (; q < ns; ++q) up_group<T, 1>(a, xs, (s0 + q) * 32 + lane, acc);
+        if (ok) {
 #pragma unroll
-        for (int r = 0; r < kRows; ++r) {
-            if (r >= nr) break;
-            const int nn = nb_n[r];
-            const int nl = min(nn, kMaxNb);
-            T ar = 0;
-#pragma unroll 4
-            for (int e = 0; e < nl; ++e) ar += nb_cf[r][e] * ub[(int64_t)nb_src[r][e] * ld + cc];
-            for (int e = kMaxNb; e < nn; ++e)
-                ar += __ldg(dcf + nb_e0[r] + e) * ub[(int64_t)__ldg(a.dsrc + nb_e0[r] + e) * ld + cc];
-            const T v = (acc[r] + ar) * sc;
-            if (ok) {
-                y[a.off + (r0 + r) * ld + c] = v;
-                dotp += xs[r * ld + cc] * v;
-            }
+            for (int r = 0; r < kRows; ++r)
+                if (r < nr) yb[r * ld + c] = acc[r];
         }
+    }
+    __syncthreads();   // phase A's rows of y are visible to the whole CTA
+    // ---- phase B
+    const T sc = (T)scal[(int64_t)i * kScal + kS];
+    const int nvec = ld / VN, chunks = (nvec + 31) / 32;
+    T dotp = 0;
+    for (int task = warp; task < nr * chunks; task += nwarps) {
+        const int r = task / chunks, v = (task - r * chunks) * 32 + lane;
+        if (v >= nvec) continue;
+        V acc = reinterpret_cast<const V *>(yb + r * ld)[v];
+        const int nn = nb_n[r], nl = min(nn, kMaxNb);
+        // neighbour rows in groups of loads in flight
+        int e = 0;
+        for (; e + 8 <= nl; e += 8) down_group<T, 8>(&nb[r][e], ub, v, acc);
+        if (e + 4 <= nl) {
+            down_group<T, 4>(&nb[r][e], ub, v, acc);
+            e += 4;
+        }
+        for (; e < nl; ++e) down_group<T, 1>(&nb[r][e], ub, v, acc);
+        for (int e = kMaxNb; e < nn; ++e) {
+            const T cf = __ldg(dcf + nb_e0[r] + e);
+            const V xn = __ldg(reinterpret_cast<const V *>(ub + (int64_t)__ldg(a.dsrc + nb_e0[r] + e) * ld) + v);
+#pragma unroll
+            for (int k = 0; k < VN; ++k) vat(acc, k) += cf * reinterpret_cast<const T *>(&xn)[k];
+        }
+        const V xo = __ldg(reinterpret_cast<const V *>(ub + (int64_t)(r0 + r) * ld) + v);
+#pragma unroll
+        for (int k = 0; k < VN; ++k) {
+            T val = vat(acc, k) * sc;
+            if (v * VN + k >= nsup) val = (T)0;   // the row padding stays zero
+            vat(acc, k) = val;
+            dotp += reinterpret_cast<const T *>(&xo)[k] * val;
+        }
+        reinterpret_cast<V *>(yb + r * ld)[v] = acc;
     }
     block_partial((double)dotp, part_out + b);
 }
 
 // u_next = y - c_cur u_k - c_prev u_prev (written over u_prev), partial
-// ||u_next||^2.  With ritz_coef, also out += ritz_coef[i][k] s_k u_k (the
-// Ritz vector sum_k y_k q_k of a replayed run).
+// ||u_next||^2, in 16-byte vectors over the CTA's rows (padding is zero in
+// all three inputs, so it stays zero).  With ritz_coef, also
+// out += ritz_coef[i][k] s_k u_k (the Ritz vector sum_k y_k q_k of a replay).
 template <typename T>
 __global__ void __launch_bounds__(kBatchThreads) batch_update_kernel(const BatchInst *__restrict__ inst,
                                                                      const int32_t *__restrict__ blk_inst,
@@ -254,6 +366,8 @@ __global__ void __launch_bounds__(kBatchThreads) batch_update_kernel(const Batch
                                                                      const double *__restrict__ ritz_coef,
                                                                      T *__restrict__ ritz_out, int k, int nsteps)
 {
+    using V = typename V16<T>::type;
+    constexpr int VN = V16<T>::n;
     const int64_t b = blockIdx.x;
     const int i = __ldg(blk_inst + b);
     const BatchInst &a = inst[i];
@@ -262,15 +376,30 @@ __global__ void __launch_bounds__(kBatchThreads) batch_update_kernel(const Batch
     const T cr = ritz_coef ? (T)(ritz_coef[(int64_t)i * nsteps + k] * sc[kS]) : (T)0;
     const int64_t r0 = (b - a.blk0) * kRows;
     const int nr = (int)min((int64_t)kRows, a.nsdn - r0);
+    const int64_t base = a.off + r0 * a.ld;
+    const int nv = nr * (int)(a.ld / VN);
+    const V *yv = reinterpret_cast<const V *>(y + base);
+    const V *uv = reinterpret_cast<const V *>(u + base);
+    V *pv = reinterpret_cast<V *>(up + base);
+    V *ov = ritz_out ? reinterpret_cast<V *>(ritz_out + base) : nullptr;
     T sp = 0;
-    for (int r = 0; r < nr; ++r) {
-        const int64_t base = a.off + (r0 + r) * a.ld;
-        for (int64_t c = threadIdx.x; c < a.nsup; c += blockDim.x) {
-            const T uk = u[base + c];
-            const T v = y[base + c] - cc * uk - cp * up[base + c];
-            up[base + c] = v;
-            sp += v * v;
-            if (ritz_out) ritz_out[base + c] += cr * uk;
+    for (int q = threadIdx.x; q < nv; q += blockDim.x) {
+        const V yy = __ldg(yv + q), uk = __ldg(uv + q);
+        V pp = pv[q];
+        V nv_;
+#pragma unroll
+        for (int e = 0; e < VN; ++e) {
+            const T t = reinterpret_cast<const T *>(&yy)[e] - cc * reinterpret_cast<const T *>(&uk)[e] -
+                        cp * reinterpret_cast<const T *>(&pp)[e];
+            vat(nv_, e) = t;
+            sp += t * t;
+        }
+        pv[q] = nv_;
+        if (ov) {
+            V o = ov[q];
+#pragma unroll
+            for (int e = 0; e < VN; ++e) vat(o, e) += cr * reinterpret_cast<const T *>(&uk)[e];
+            ov[q] = o;
         }
     }
     block_partial((double)sp, part_nrm + b);
@@ -284,7 +413,7 @@ static int run_batch(ed_batch *bt, cudaStream_t st, T *work, const T *x0, int ns
     T *U[2] = {work, work + tot};
     T *Y = work + 2 * tot;
     double *pa = scratch, *pb = scratch + bt->nblocks, *scal = scratch + 2 * bt->nblocks;
-    const size_t smem = (size_t)kRows * bt->max_ld * sizeof(T);
+    const size_t smem = (size_t)bt->max_ld * staged_stride<T>() * sizeof(T);
     const unsigned nb = (unsigned)bt->nblocks;
     const unsigned ns = (unsigned)((bt->ninst * 32 + 255) / 256);
     // u_{k+1} overwrites u_{k-1} in place, so u_k lives in slot k % 2
@@ -319,6 +448,35 @@ static int run_batch(ed_batch *bt, cudaStream_t st, T *work, const T *x0, int ns
 
 using namespace ed;
 
+static size_t hv_smem_bytes(int dtype, int64_t ld)
+{
+    return (dtype == ED_F32) ? (size_t)ld * staged_stride<float>() * sizeof(float)
+                             : (size_t)ld * staged_stride<double>() * sizeof(double);
+}
+
+// Dynamic shared memory of the H*v kernels: raised once to the largest need
+// (at batch creation, so a later launch inside a stream capture only launches).
+static std::mutex g_smem_mu;
+static size_t g_smem_set[2] = {0, 0};
+
+static int ensure_hv_smem(int dtype, size_t bytes)
+{
+    std::lock_guard<std::mutex> lk(g_smem_mu);
+    const int k = (dtype == ED_F32) ? 0 : 1;
+    if (bytes <= g_smem_set[k]) return ED_OK;
+    const cudaError_t e = (dtype == ED_F32)
+                              ? cudaFuncSetAttribute(batch_hv_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)bytes)
+                              : cudaFuncSetAttribute(batch_hv_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)bytes);
+    if (e != cudaSuccess) {
+        set_error("cudaFuncSetAttribute: %s", cudaGetErrorString(e));
+        return ED_ERR_CUDA;
+    }
+    g_smem_set[k] = bytes;
+    return ED_OK;
+}
+
 extern "C" int ed_batch_create(int ninst, ed_sector *const *secs, ed_batch **out)
 {
     clear_error();
@@ -335,7 +493,7 @@ extern "C" int ed_batch_create(int ninst, ed_sector *const *secs, ed_batch **out
         const ed_sector *s = secs[i];
         ED_REQUIRE(s != nullptr && s->kind == ED_HUBBARD, "instance %d is not a Hubbard sector", i);
         const int64_t ld = (s->nsup + 31) / 32 * 32;   // the internal row stride of pyhub_gb300 vectors
-        if ((size_t)kRows * ld * sizeof(double) > 200 * 1024) {
+        if (hv_smem_bytes(ED_F64, ld) > 200 * 1024) {
             set_error("instance %d: rows of %lld strings are too long for the batched kernel", i, (long long)s->nsup);
             return ED_ERR_RANGE;
         }
@@ -349,6 +507,7 @@ extern "C" int ed_batch_create(int ninst, ed_sector *const *secs, ed_batch **out
         a.uediag = s->up.ediag; a.dediag = s->dn.ediag;
         a.ell_off = s->up.ell_off; a.ell_src = s->up.ell_src;
         a.ell_cf32 = s->up.ell_cf32; a.ell_cf64 = s->up.ell_cf64;
+        a.ell_pk32 = s->up.ell_pk32;
         a.nslice = (int)s->up.nslice;
         for (int q = 0; q < kMaxSites; ++q) usite[(size_t)i * kMaxSites + q] = s->u_site[q];
         a.u_site = nullptr;   // set after the upload below
@@ -382,6 +541,11 @@ extern "C" int ed_batch_create(int ninst, ed_sector *const *secs, ed_batch **out
         set_error("allocation of batch descriptors failed");
         ed_batch_destroy(bt);
         return ED_ERR_MEM;
+    }
+    if (ensure_hv_smem(ED_F32, hv_smem_bytes(ED_F32, max_ld)) != ED_OK ||
+        ensure_hv_smem(ED_F64, hv_smem_bytes(ED_F64, max_ld)) != ED_OK) {
+        ed_batch_destroy(bt);
+        return ED_ERR_CUDA;
     }
     for (int i = 0; i < ninst; ++i) host[(size_t)i].u_site = bt->u_site_all + (size_t)i * kMaxSites;
     if (cudaMemcpy(bt->dev, host.data(), sizeof(BatchInst) * ninst, cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -436,14 +600,12 @@ static int batch_launch(ed_batch *bt, void *stream, int dtype, void *work, const
     ED_REQUIRE(scratch != nullptr && scratch_bytes >= ed_batch_scratch_bytes(bt), "scratch of %lld bytes is below %lld",
                (long long)scratch_bytes, (long long)ed_batch_scratch_bytes(bt));
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int rc = ensure_hv_smem(dtype, hv_smem_bytes(dtype, bt->max_ld));
+    if (rc != ED_OK) return rc;
     if (dtype == ED_F32) {
-        const size_t smem = (size_t)kRows * bt->max_ld * sizeof(float);
-        ED_CHECK_CUDA(cudaFuncSetAttribute(batch_hv_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         return run_batch<float>(bt, st, (float *)work, (const float *)x0, nsteps, alpha, beta, (double *)scratch,
                                 ritz_coef, (float *)ritz_out);
     }
-    const size_t smem = (size_t)kRows * bt->max_ld * sizeof(double);
-    ED_CHECK_CUDA(cudaFuncSetAttribute(batch_hv_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     return run_batch<double>(bt, st, (double *)work, (const double *)x0, nsteps, alpha, beta, (double *)scratch,
                              ritz_coef, (double *)ritz_out);
 }

@@ -70,6 +70,7 @@ struct HopTable {
     int32_t *ell_src = nullptr;    // [ell_slots*32]
     float *ell_cf32 = nullptr;
     double *ell_cf64 = nullptr;
+    int2 *ell_pk32 = nullptr;      // [ell_slots*32] {src, FP32 coefficient bits}: one 8-byte load per slot
     bool owner = true;
 };
 

@@ -208,22 +208,58 @@ static int upload_ell(const HostHop &h, HopTable &d)
     const int64_t slots = off[(size_t)ns];
     std::vector<int32_t> src((size_t)std::max<int64_t>(slots * 32, 1));
     std::vector<double> c64((size_t)std::max<int64_t>(slots * 32, 1), 0.0);
-    for (int64_t sl = 0; sl < ns; ++sl)
-        for (int64_t k = 0; k < off[(size_t)sl + 1] - off[(size_t)sl]; ++k)
-            for (int l = 0; l < 32; ++l) {
-                const int64_t u = sl * 32 + l;
-                const size_t at = (size_t)((off[(size_t)sl] + k) * 32 + l);
-                const int64_t uu = u < n ? u : n - 1;
-                const int32_t e0 = h.ptr[(size_t)uu], e1 = h.ptr[(size_t)uu + 1];
-                if (u < n && e0 + k < e1) {
-                    src[at] = h.src[(size_t)(e0 + k)];
-                    c64[at] = h.coef[(size_t)(e0 + k)];
-                } else {
-                    src[at] = (int32_t)uu;
-                    c64[at] = 0.0;
+    // Slot order within a lane is free.  The batched kernel gathers 16-byte
+    // column pieces for 8 lanes at a time (one quarter warp), and a column's
+    // bank group is (source string mod 8); so each quarter's lanes take, slot
+    // by slot, neighbours of pairwise different groups where they can (greedy,
+    // lanes with the most neighbours left first).  Padding slots read the
+    // lane's own string (consecutive strings: distinct groups) with weight 0.
+    for (int64_t sl = 0; sl < ns; ++sl) {
+        const int64_t w = off[(size_t)sl + 1] - off[(size_t)sl];
+        for (int qw = 0; qw < 4; ++qw) {
+            std::vector<std::vector<int32_t>> left(8);   // remaining neighbour entries (hop-table positions)
+            for (int l = 0; l < 8; ++l) {
+                const int64_t u = sl * 32 + qw * 8 + l;
+                if (u >= n) continue;
+                for (int32_t e = h.ptr[(size_t)u]; e < h.ptr[(size_t)u + 1]; ++e) left[(size_t)l].push_back(e);
+            }
+            for (int64_t k = 0; k < w; ++k) {
+                bool used[8] = {false, false, false, false, false, false, false, false};
+                int order[8] = {0, 1, 2, 3, 4, 5, 6, 7};
+                std::stable_sort(order, order + 8, [&](int x, int y) { return left[(size_t)x].size() > left[(size_t)y].size(); });
+                for (int oi = 0; oi < 8; ++oi) {
+                    const int l = order[oi];
+                    const int64_t u = sl * 32 + qw * 8 + l;
+                    const size_t at = (size_t)((off[(size_t)sl] + k) * 32 + qw * 8 + l);
+                    const int64_t uu = u < n ? u : n - 1;
+                    std::vector<int32_t> &L = left[(size_t)l];
+                    const bool must = (int64_t)L.size() >= w - k;   // no spare slot left for this lane
+                    int pick = -1;
+                    for (size_t j = 0; j < L.size(); ++j)
+                        if (!used[h.src[(size_t)L[j]] & 7]) { pick = (int)j; break; }
+                    if (pick < 0 && must) pick = 0;
+                    if (pick < 0 && !L.empty() && used[uu & 7]) pick = 0;   // padding would conflict too
+                    if (pick >= 0) {
+                        const int32_t e = L[(size_t)pick];
+                        L.erase(L.begin() + pick);
+                        src[at] = h.src[(size_t)e];
+                        c64[at] = h.coef[(size_t)e];
+                    } else {
+                        src[at] = (int32_t)uu;
+                        c64[at] = 0.0;
+                    }
+                    used[src[at] & 7] = true;
                 }
             }
+        }
+    }
     std::vector<float> c32(c64.begin(), c64.end());
+    std::vector<int2> pk(src.size());
+    for (size_t q = 0; q < src.size(); ++q) {
+        int32_t bits;
+        std::memcpy(&bits, &c32[q], sizeof(bits));
+        pk[q] = make_int2(src[q], bits);
+    }
     d.nslice = ns;
     d.ell_slots = slots;
     int rc;
@@ -231,6 +267,7 @@ static int upload_ell(const HostHop &h, HopTable &d)
     if ((rc = upload(&d.ell_src, src.data(), src.size()))) return rc;
     if ((rc = upload(&d.ell_cf32, c32.data(), c32.size()))) return rc;
     if ((rc = upload(&d.ell_cf64, c64.data(), c64.size()))) return rc;
+    if ((rc = upload(&d.ell_pk32, pk.data(), pk.size()))) return rc;
     return ED_OK;
 }
 
@@ -259,6 +296,7 @@ static void free_hop(HopTable &d)
     cudaFree(d.str); cudaFree(d.ptr); cudaFree(d.src);
     cudaFree(d.cf32); cudaFree(d.cf64); cudaFree(d.ediag);
     cudaFree(d.ell_off); cudaFree(d.ell_src); cudaFree(d.ell_cf32); cudaFree(d.ell_cf64);
+    cudaFree(d.ell_pk32);
     d = HopTable();
 }
 
