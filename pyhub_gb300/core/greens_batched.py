@@ -74,7 +74,7 @@ class BatchedGroundStates:
     e0: np.ndarray          # [n] lowest Ritz values
     residual: np.ndarray    # [n] ||H psi - E0 psi|| of the returned (normalised) vectors
     psi: list               # [n] normalised FP64 ground states (views into one device vector)
-    restarts: int           # FP64 cycles after the first
+    restarts: int           # FP64 cycles after the first (on the unconverged instances only)
 
 
 def _lowest_ritz(a, b, tol_break: float = 1e-12):
@@ -160,14 +160,26 @@ def batched_ground_states(sectors, nsteps: int = 120, tol: float = 1e-10, max_re
         for i, v in enumerate(starts):
             bl.start(i).copy_(v)
     out = torch.zeros_like(bl.x0)
+    e0 = _ritz_cycle(bl, out)
+    res = _true_residuals(bl, out, e0)
+    # further FP64 cycles only for the instances still above tol, each
+    # restarted from its Ritz vector in a batch of their own
     it = 0
-    while True:
-        e0 = _ritz_cycle(bl, out)
-        res = _true_residuals(bl, out, e0)
-        if (res <= tol).all() or it >= max_restarts:
-            break
-        bl.x0.copy_(out)
+    todo = np.nonzero(res > tol)[0]
+    while todo.size and it < max_restarts:
         it += 1
+        sub = BatchedLanczos([bl.sectors[i] for i in todo], refine_steps, dtype=torch.float64)
+        for j, i in enumerate(todo):
+            sub.start(j).copy_(bl.batch.view(out, int(i)))
+        sout = torch.zeros_like(sub.x0)
+        e_sub = _ritz_cycle(sub, sout)
+        r_sub = _true_residuals(sub, sout, e_sub)
+        for j, i in enumerate(todo):
+            if r_sub[j] < res[i]:
+                bl.batch.view(out, int(i)).copy_(sub.batch.view(sout, j))
+                e0[i], res[i] = e_sub[j], r_sub[j]
+        del sub, sout
+        todo = np.nonzero(res > tol)[0]
     psi = [bl.batch.view(out, i) for i in range(len(bl.sectors))]
     return BatchedGroundStates(e0=e0, residual=res, psi=psi, restarts=it)
 

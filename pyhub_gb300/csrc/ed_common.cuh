@@ -84,6 +84,42 @@ struct HeisTables {
     double dconst = 0.0;                     // 0.5*sum J(J,J) (|.|>tol) + 0.25*sum J(J,J)
 };
 
+constexpr int kMaxHalf = 16;    // sites in one half of a Heisenberg sector
+constexpr int kMaxAB = 256;     // bonds between the two halves
+
+// Row tables of a Heisenberg sector (see ed_heis.cu): the vector, in the
+// reference order, is one row per B-half hole pattern; the row's entries are
+// the A-half hole patterns with m holes in colex order.
+struct HeisStruct {
+    int nA = 0, nB = 0, H = 0, mlo = 0, mhi = 0;
+    int64_t nrows = 0, max_len = 0;
+    int64_t col_base[kMaxHalf + 2] = {}, ncol[kMaxHalf + 1] = {}, slice_base[kMaxHalf + 2] = {};
+    int64_t row_base[kMaxHalf + 2] = {};
+    uint32_t *col_pat = nullptr;     // A patterns, concatenated over m
+    int32_t *rankA = nullptr;        // [2^nA] colex rank among the patterns of equal popcount
+    double *diagA = nullptr;         // A-A zz energy per column
+    int32_t *aa_off = nullptr, *aa_src = nullptr;   // sliced ELL of the A-A flips per m
+    float *aa_cf32 = nullptr;
+    double *aa_cf64 = nullptr;
+    uint32_t *row_pat = nullptr;     // B pattern per row (rows in offset order)
+    int32_t *row_m = nullptr, *rowidx = nullptr;    // holes in A per row; [2^nB] row of a pattern or -1
+    int64_t *row_off = nullptr;
+    double *diagB = nullptr;         // B-B zz energy + constant diagonal per row
+    int32_t *bb_ptr = nullptr, *bb_src = nullptr;   // B-B flips: neighbour rows per row (CSR)
+    float *bb_cf32 = nullptr;
+    double *bb_cf64 = nullptr;
+    int32_t *rows_of_m = nullptr;    // rows grouped by m
+    int nab = 0;
+    int8_t ab_pa[kMaxAB] = {}, ab_pb[kMaxAB] = {};  // A bit, B bit (relative to nA)
+    double ab_fjk[kMaxAB] = {}, ab_fkj[kMaxAB] = {}, ab_zz[kMaxAB] = {};
+};
+
+int heis_struct_build(ed_sector *s);
+void heis_struct_free(HeisStruct *hs);
+int heis_struct_hv(ed_sector *s, cudaStream_t st, int dtype, const void *x, void *y, double scale, double *dots,
+                   double *partials);
+int launch_reduce(const double *partials, int nblocks, int m, double *out, cudaStream_t st);
+
 }  // namespace ed
 
 struct ed_sector {
@@ -95,6 +131,7 @@ struct ed_sector {
     bool u_uniform = true;
     double u_value = 0.0;
     ed::HeisTables heis;
+    ed::HeisStruct *hs = nullptr;  // Heisenberg row tables
     // colex rank of an empty-site pattern h (bit j: site j+1 empty) in byte
     // chunks, shared by every kernel that ranks strings on the fly:
     // rank = sum_b lut[b][popcount(h & (2^(8b)-1))][byte b of h]

@@ -1,0 +1,503 @@
+// ed_heis.cu -- structured H*v of the Heisenberg sector.
+//
+// Replaces HPROD of hprod_heis.f90:1-61 (the same Hamiltonian as heis_kernel
+// of ed_hv.cu, element for element) with a product that never ranks a full
+// 32-bit state.  A state is its empty-site (down-spin) pattern h, bit j for
+// site j+1.  Split the sites into A = 1..nA (bits 0..nA-1) and B = the rest.
+// The reference order is colex order of h, and colex order keeps all states
+// that share their B part contiguous, ordered by the colex rank of their A
+// part.  So the sector vector IS a set of rows: one row per B pattern hB
+// (row offset = the colex contribution of hB's bits), and the row's entries
+// are the A patterns with m = H - popcount(hB) holes in colex order (the
+// 16-site combination order for a 4x8 lattice cut in two 4x4 halves).
+// With that layout
+//   A-A bonds flip within a row     -> gathers from the row staged in shared memory,
+//   B-B bonds flip between rows     -> row axpys at equal column (coalesced),
+//   A-B bonds flip both             -> a gather from ONE other row per bond; the
+//                                      column map (add/remove one fixed bit) is
+//                                      monotone, so the gathers stay local.
+// Pass R (one CTA per row): diagonal + A-A + A-B, y = s*(...).
+// Pass S (column slabs that keep the x slab of one m-block in L2): y += s*B-B,
+// with the fused <x,y>, <y,y> partials.
+#include "ed_common.cuh"
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+namespace ed {
+
+namespace {
+
+int64_t hbinom(int n, int k)
+{
+    if (k < 0 || n < 0 || k > n) return 0;
+    int64_t r = 1;
+    for (int i = 1; i <= k; ++i) r = r * (n - k + i) / i;
+    return r;
+}
+
+// colex rank of a hole pattern: sum over its set bits p (ascending, i = 1..) of C(p, i)
+int64_t colex_rank(uint32_t h, int base_i = 0, int shift = 0)
+{
+    int64_t r = 0;
+    int i = base_i;
+    while (h) {
+        const int p = __builtin_ctz(h);
+        r += hbinom(p + shift, ++i);
+        h &= h - 1;
+    }
+    return r;
+}
+
+template <typename T>
+int up(T **dst, const std::vector<T> &v)
+{
+    *dst = nullptr;
+    if (v.empty()) return ED_OK;
+    if (cudaMalloc(dst, sizeof(T) * v.size()) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("device allocation of %zu bytes failed", sizeof(T) * v.size());
+        return ED_ERR_MEM;
+    }
+    if (cudaMemcpy(*dst, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        set_error("upload failed");
+        return ED_ERR_CUDA;
+    }
+    return ED_OK;
+}
+
+}  // namespace
+
+int heis_struct_build(ed_sector *s)
+{
+    const HeisTables &ht = s->heis;
+    HeisStruct *hs = new HeisStruct();
+    s->hs = hs;
+    const int norb = s->norb;
+    const int nA = norb / 2, nB = norb - nA, H = norb - s->nup;
+    hs->nA = nA;
+    hs->nB = nB;
+    hs->H = H;
+    hs->mlo = std::max(0, H - nB);
+    hs->mhi = std::min(nA, H);
+    // ---- columns: A patterns by hole count m, colex order
+    std::vector<uint32_t> col_pat;
+    std::vector<int32_t> rankA((size_t)1 << nA, -1);
+    std::vector<double> diagA;
+    for (int m = 0; m <= kMaxHalf + 1; ++m) hs->col_base[m] = 0;
+    for (int m = 0; m <= nA; ++m) {
+        hs->col_base[m] = (int64_t)col_pat.size();
+        hs->ncol[m] = hbinom(nA, m);
+        std::vector<uint32_t> pats;
+        for (uint32_t h = 0; h < (1u << nA); ++h)
+            if (__builtin_popcount(h) == m) pats.push_back(h);
+        std::sort(pats.begin(), pats.end(), [](uint32_t x, uint32_t y) { return colex_rank(x) < colex_rank(y); });
+        for (size_t r = 0; r < pats.size(); ++r) {
+            rankA[pats[r]] = (int32_t)r;
+            col_pat.push_back(pats[r]);
+        }
+    }
+    hs->col_base[nA + 1] = (int64_t)col_pat.size();
+    // bonds by class
+    std::vector<int> aa, bb, ab;
+    for (int b = 0; b < ht.nbond; ++b) {
+        const int pj = ht.bj[b] - 1, pk = ht.bk[b] - 1;   // pj < pk
+        if (pk < nA) aa.push_back(b);
+        else if (pj >= nA) bb.push_back(b);
+        else ab.push_back(b);
+    }
+    if ((int)ab.size() > kMaxAB) {
+        set_error("%zu bonds cross the two halves (at most %d)", ab.size(), kMaxAB);
+        return ED_ERR_RANGE;
+    }
+    // A-A zz energy and hop lists per column, sliced ELL per m (32 columns per slice)
+    diagA.resize(col_pat.size());
+    std::vector<int32_t> aa_off(1, 0), aa_src;
+    std::vector<double> aa_cf;
+    int64_t nslices = 0;
+    for (int m = 0; m <= nA; ++m) {
+        hs->slice_base[m] = nslices;
+        const int64_t n = hs->ncol[m], base = hs->col_base[m];
+        std::vector<std::vector<std::pair<int32_t, double>>> lists((size_t)n);
+        for (int64_t r = 0; r < n; ++r) {
+            const uint32_t h = col_pat[(size_t)(base + r)];
+            double d = 0.0;
+            for (int b : aa) {
+                const int pj = ht.bj[b] - 1, pk = ht.bk[b] - 1;
+                const uint32_t hj = (h >> pj) & 1u, hk = (h >> pk) & 1u;
+                d += (hj == hk ? 0.25 : -0.25) * ht.zz[b];
+                if (hj == hk) continue;
+                const double c = hj ? ht.flip_jk[b] : ht.flip_kj[b];
+                if (c == 0.0) continue;
+                lists[(size_t)r].push_back({rankA[h ^ ((1u << pj) | (1u << pk))], c});
+            }
+            diagA[(size_t)(base + r)] = d;
+        }
+        const int64_t ns = (n + 31) / 32;
+        for (int64_t sl = 0; sl < ns; ++sl) {
+            size_t w = 0;
+            for (int64_t r = sl * 32; r < std::min(n, sl * 32 + 32); ++r) w = std::max(w, lists[(size_t)r].size());
+            for (size_t k = 0; k < w; ++k)
+                for (int l = 0; l < 32; ++l) {
+                    const int64_t r = sl * 32 + l;
+                    if (r < n && k < lists[(size_t)r].size()) {
+                        aa_src.push_back(lists[(size_t)r][k].first);
+                        aa_cf.push_back(lists[(size_t)r][k].second);
+                    } else {
+                        aa_src.push_back((int32_t)std::min(r, n - 1));   // own column, weight 0
+                        aa_cf.push_back(0.0);
+                    }
+                }
+            aa_off.push_back(aa_off.back() + (int32_t)w);
+        }
+        nslices += ns;
+    }
+    hs->slice_base[nA + 1] = nslices;
+    // ---- rows: B patterns with H - m holes, m in [mlo, mhi], sorted by offset
+    struct Row {
+        uint32_t hb;
+        int m;
+        int64_t off;
+    };
+    std::vector<Row> rows;
+    for (uint32_t hb = 0; hb < (1u << nB); ++hb) {
+        const int m = H - __builtin_popcount(hb);
+        if (m < hs->mlo || m > hs->mhi) continue;
+        // colex contribution of the B holes: running index continues after the m A holes
+        rows.push_back({hb, m, colex_rank(hb, m, nA)});
+    }
+    std::sort(rows.begin(), rows.end(), [](const Row &x, const Row &y) { return x.off < y.off; });
+    const int64_t nrows = (int64_t)rows.size();
+    hs->nrows = nrows;
+    std::vector<uint32_t> row_pat((size_t)nrows);
+    std::vector<int32_t> row_m((size_t)nrows), rowidx((size_t)1 << nB, -1);
+    std::vector<int64_t> row_off((size_t)nrows);
+    std::vector<double> diagB((size_t)nrows);
+    int64_t expect = 0;
+    hs->max_len = 0;
+    for (int64_t r = 0; r < nrows; ++r) {
+        const Row &w = rows[(size_t)r];
+        if (w.off != expect) {
+            set_error("internal: row offsets are not contiguous at row %lld", (long long)r);
+            return ED_ERR_ARG;
+        }
+        expect += hs->ncol[w.m];
+        row_pat[(size_t)r] = w.hb;
+        row_m[(size_t)r] = w.m;
+        row_off[(size_t)r] = w.off;
+        rowidx[w.hb] = (int32_t)r;
+        hs->max_len = std::max<int64_t>(hs->max_len, hs->ncol[w.m]);
+    }
+    if (expect != s->nsup) {
+        set_error("internal: rows cover %lld of %lld states", (long long)expect, (long long)s->nsup);
+        return ED_ERR_ARG;
+    }
+    // B-B zz energy (+ the constant diagonal) and neighbour rows per row
+    std::vector<int32_t> bb_ptr(1, 0), bb_src;
+    std::vector<double> bb_cf;
+    for (int64_t r = 0; r < nrows; ++r) {
+        const uint32_t h = row_pat[(size_t)r];
+        double d = ht.dconst;
+        for (int b : bb) {
+            const int pj = ht.bj[b] - 1 - nA, pk = ht.bk[b] - 1 - nA;
+            const uint32_t hj = (h >> pj) & 1u, hk = (h >> pk) & 1u;
+            d += (hj == hk ? 0.25 : -0.25) * ht.zz[b];
+            if (hj == hk) continue;
+            const double c = hj ? ht.flip_jk[b] : ht.flip_kj[b];
+            if (c == 0.0) continue;
+            bb_src.push_back(rowidx[h ^ ((1u << pj) | (1u << pk))]);
+            bb_cf.push_back(c);
+        }
+        diagB[(size_t)r] = d;
+        bb_ptr.push_back((int32_t)bb_src.size());
+    }
+    // rows grouped by m (offset order within each m) for the slab pass
+    std::vector<int32_t> rows_of_m;
+    for (int m = 0; m <= kMaxHalf + 1; ++m) hs->row_base[m] = 0;
+    for (int m = 0; m <= nA; ++m) {
+        hs->row_base[m] = (int64_t)rows_of_m.size();
+        for (int64_t r = 0; r < nrows; ++r)
+            if (row_m[(size_t)r] == m) rows_of_m.push_back((int32_t)r);
+    }
+    hs->row_base[nA + 1] = (int64_t)rows_of_m.size();
+    // A-B bonds
+    hs->nab = (int)ab.size();
+    for (int q = 0; q < hs->nab; ++q) {
+        const int b = ab[(size_t)q];
+        hs->ab_pa[q] = (int8_t)(ht.bj[b] - 1);
+        hs->ab_pb[q] = (int8_t)(ht.bk[b] - 1 - nA);
+        hs->ab_fjk[q] = ht.flip_jk[b];
+        hs->ab_fkj[q] = ht.flip_kj[b];
+        hs->ab_zz[q] = 0.25 * ht.zz[b];
+    }
+    std::vector<float> aa_cf32(aa_cf.begin(), aa_cf.end()), bb_cf32(bb_cf.begin(), bb_cf.end());
+    int rc;
+    if ((rc = up(&hs->col_pat, col_pat)) || (rc = up(&hs->rankA, rankA)) || (rc = up(&hs->diagA, diagA)) ||
+        (rc = up(&hs->aa_off, aa_off)) || (rc = up(&hs->aa_src, aa_src)) || (rc = up(&hs->aa_cf32, aa_cf32)) ||
+        (rc = up(&hs->aa_cf64, aa_cf)) || (rc = up(&hs->row_pat, row_pat)) || (rc = up(&hs->row_m, row_m)) ||
+        (rc = up(&hs->row_off, row_off)) || (rc = up(&hs->rowidx, rowidx)) || (rc = up(&hs->diagB, diagB)) ||
+        (rc = up(&hs->bb_ptr, bb_ptr)) || (rc = up(&hs->bb_src, bb_src)) || (rc = up(&hs->bb_cf32, bb_cf32)) ||
+        (rc = up(&hs->bb_cf64, bb_cf)) || (rc = up(&hs->rows_of_m, rows_of_m)))
+        return rc;
+    return ED_OK;
+}
+
+void heis_struct_free(HeisStruct *hs)
+{
+    if (!hs) return;
+    void *ptrs[] = {hs->col_pat, hs->rankA, hs->diagA, hs->aa_off, hs->aa_src, hs->aa_cf32,
+                    hs->aa_cf64, hs->row_pat, hs->row_m, hs->row_off, hs->rowidx, hs->diagB,
+                    hs->bb_ptr, hs->bb_src, hs->bb_cf32, hs->bb_cf64, hs->rows_of_m};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    delete hs;
+}
+
+// ------------------------------------------------------------ kernels
+
+struct HsArgs {
+    int nA, nB, nab;
+    int64_t nrows;
+    int64_t col_base[kMaxHalf + 2], ncol[kMaxHalf + 1], slice_base[kMaxHalf + 2], row_base[kMaxHalf + 2];
+    const uint32_t *col_pat, *row_pat;
+    const int32_t *rankA, *aa_off, *aa_src, *row_m, *rowidx, *bb_ptr, *bb_src, *rows_of_m;
+    const int64_t *row_off;
+    const double *diagA, *diagB;
+    const void *aa_cf, *bb_cf;     // float or double
+    int8_t ab_pa[kMaxAB], ab_pb[kMaxAB];
+    double ab_fjk[kMaxAB], ab_fkj[kMaxAB], ab_zz[kMaxAB];
+    double scale;
+};
+
+constexpr int kHeisRowThreads = 512;
+constexpr int64_t kMaxPartialBlocksHeis = 1024;   // the partials that ed_scratch_bytes provides for
+
+// Pass R: y[row] = s * (diag + A-A flips + A-B flips) of every row.
+template <typename T>
+__global__ void __launch_bounds__(kHeisRowThreads) heis_row_kernel(const T *__restrict__ x, T *__restrict__ y,
+                                                                    const HsArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *xs = reinterpret_cast<T *>(smem_raw);
+    __shared__ int64_t ab_src[kMaxAB];   // element offset of the bond's source row, -1 if the flip is impossible
+    __shared__ T ab_c[kMaxAB];           // flip element when the A site is in the required state
+    __shared__ uint32_t ab_need[kMaxAB]; // required A bit (1: A site down) for the flip
+    __shared__ T ab_dsame[kMaxAB];       // +-zz/4 when the two sites are equal
+    const T *acf = reinterpret_cast<const T *>(a.aa_cf);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = kHeisRowThreads / 32;
+    const T sc = (T)a.scale;
+    for (int64_t row = blockIdx.x; row < a.nrows; row += gridDim.x) {
+        const uint32_t hb = __ldg(a.row_pat + row);
+        const int m = __ldg(a.row_m + row);
+        const int64_t off = __ldg(a.row_off + row);
+        const int len = (int)a.ncol[m];
+        const int64_t cbase = a.col_base[m];
+        const int64_t sbase = a.slice_base[m];
+        const T db = (T)__ldg(a.diagB + row);
+        __syncthreads();   // the previous row's readers are done with xs / ab_*
+        for (int c = threadIdx.x; c < len; c += blockDim.x) xs[c] = x[off + c];
+        for (int q = threadIdx.x; q < a.nab; q += blockDim.x) {
+            const uint32_t hk = (hb >> a.ab_pb[q]) & 1u;
+            // the flip needs the A site opposite to the B site: hj = 1 - hk
+            const int32_t r2 = __ldg(a.rowidx + (hb ^ (1u << a.ab_pb[q])));
+            ab_src[q] = (r2 >= 0) ? __ldg(a.row_off + r2) : (int64_t)-1;
+            ab_need[q] = 1u - hk;
+            ab_c[q] = (T)(hk ? a.ab_fkj[q] : a.ab_fjk[q]);   // target hj = 1-hk: hj ? fjk : fkj
+            ab_dsame[q] = (T)a.ab_zz[q];
+        }
+        __syncthreads();
+        const int nsl = (len + 31) / 32;
+        for (int sl = warp; sl < nsl; sl += nwarps) {
+            const int c = sl * 32 + lane;
+            const bool ok = c < len;
+            const int cc = ok ? c : len - 1;
+            const uint32_t ha = __ldg(a.col_pat + cbase + cc);
+            T d = (T)__ldg(a.diagA + cbase + cc) + db;
+            T acc = 0;
+            const int s0 = __ldg(a.aa_off + sbase + sl), ns = __ldg(a.aa_off + sbase + sl + 1) - s0;
+#pragma unroll 4
+            for (int q = 0; q < ns; ++q) {
+                const int at = (s0 + q) * 32 + lane;
+                acc += __ldg(acf + at) * xs[__ldg(a.aa_src + at)];
+            }
+            for (int q = 0; q < a.nab; ++q) {
+                const uint32_t hj = (ha >> a.ab_pa[q]) & 1u;
+                if (hj != ab_need[q]) {
+                    d += ab_dsame[q];          // equal sites
+                    continue;
+                }
+                d -= ab_dsame[q];
+                const int64_t src = ab_src[q];
+                if (src >= 0) acc += ab_c[q] * __ldg(x + src + __ldg(a.rankA + (ha ^ (1u << a.ab_pa[q]))));
+            }
+            if (ok) y[off + c] = (d * xs[cc] + acc) * sc;
+        }
+    }
+}
+
+// Pass S: y += s * (B-B flips), fused <x,y>, <y,y>.  Work items run block
+// (m) by block, slab by slab: all row groups of a block read one column slab
+// of x while it sits in L2.
+struct SlabPlan {
+    int nblk;
+    int m[kMaxHalf + 1];
+    int64_t item_base[kMaxHalf + 2];
+    int64_t slab_w[kMaxHalf + 1], ngroups[kMaxHalf + 1];
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) heis_slab_kernel(const T *__restrict__ x, T *__restrict__ y, const HsArgs a,
+                                                        const SlabPlan p, double *__restrict__ partials)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const T *bcf = reinterpret_cast<const T *>(a.bb_cf);
+    const T sc = (T)a.scale;
+    double dxy = 0.0, dyy = 0.0;
+    const int64_t nitems = p.item_base[p.nblk];
+    for (int64_t it = blockIdx.x; it < nitems; it += gridDim.x) {
+        int bi = 0;
+        while (bi + 1 < p.nblk && p.item_base[bi + 1] <= it) ++bi;
+        const int m = p.m[bi];
+        const int64_t li = it - p.item_base[bi];
+        const int64_t slab = li / p.ngroups[bi], g = li - slab * p.ngroups[bi];
+        const int len = (int)a.ncol[m];
+        const int64_t nr_m = a.row_base[m + 1] - a.row_base[m];
+        const int64_t rr = g * 8 + warp;
+        if (rr >= nr_m) continue;   // warp-uniform
+        const int32_t row = __ldg(a.rows_of_m + a.row_base[m] + rr);
+        const int64_t off = __ldg(a.row_off + row);
+        const int e0 = __ldg(a.bb_ptr + row), nn = __ldg(a.bb_ptr + row + 1) - e0;
+        const int64_t c0 = slab * p.slab_w[bi];
+        const int64_t c1 = min((int64_t)len, c0 + p.slab_w[bi]);
+        for (int eb = 0; eb < nn || eb == 0; eb += 32) {
+            // neighbour rows of this chunk, one per lane
+            const int ne = min(32, nn - eb);
+            int64_t my_off = 0;
+            T my_cf = 0;
+            if (lane < ne) {
+                my_off = __ldg(a.row_off + __ldg(a.bb_src + e0 + eb + lane));
+                my_cf = __ldg(bcf + e0 + eb + lane);
+            }
+            const bool last = eb + 32 >= nn;
+            for (int64_t cb = c0; cb < c1; cb += 32) {
+                const int64_t c = cb + lane;
+                const bool ok = c < c1;
+                T acc = 0;
+#pragma unroll 4
+                for (int e = 0; e < ne; ++e) {
+                    const int64_t so = __shfl_sync(0xffffffffu, my_off, e);
+                    const T w = __shfl_sync(0xffffffffu, my_cf, e);
+                    if (ok) acc += w * __ldg(x + so + c);
+                }
+                if (ok) {
+                    const T yv = y[off + c] + acc * sc;
+                    y[off + c] = yv;
+                    if (last) {
+                        dxy += (double)x[off + c] * (double)yv;
+                        dyy += (double)yv * (double)yv;
+                    }
+                }
+            }
+        }
+    }
+    if (partials) {
+        __shared__ double red[2][8];
+        dxy = warp_sum(dxy);
+        dyy = warp_sum(dyy);
+        if (lane == 0) {
+            red[0][warp] = dxy;
+            red[1][warp] = dyy;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double sxy = 0.0, syy = 0.0;
+            for (int w = 0; w < 8; ++w) {
+                sxy += red[0][w];
+                syy += red[1][w];
+            }
+            partials[2 * blockIdx.x] = sxy;
+            partials[2 * blockIdx.x + 1] = syy;
+        }
+    }
+}
+
+template <typename T>
+static int heis_struct_run(ed_sector *s, cudaStream_t st, const T *x, T *y, double scale, double *dots,
+                           double *partials)
+{
+    const HeisStruct &h = *s->hs;
+    HsArgs a;
+    a.nA = h.nA;
+    a.nB = h.nB;
+    a.nab = h.nab;
+    a.nrows = h.nrows;
+    for (int m = 0; m <= kMaxHalf + 1; ++m) {
+        a.col_base[m] = h.col_base[m];
+        a.slice_base[m] = h.slice_base[m];
+        a.row_base[m] = h.row_base[m];
+        if (m <= kMaxHalf) a.ncol[m] = h.ncol[m];
+    }
+    a.col_pat = h.col_pat; a.row_pat = h.row_pat;
+    a.rankA = h.rankA; a.aa_off = h.aa_off; a.aa_src = h.aa_src; a.row_m = h.row_m;
+    a.rowidx = h.rowidx; a.bb_ptr = h.bb_ptr; a.bb_src = h.bb_src; a.rows_of_m = h.rows_of_m;
+    a.row_off = h.row_off;
+    a.diagA = h.diagA; a.diagB = h.diagB;
+    a.aa_cf = (sizeof(T) == 4) ? (const void *)h.aa_cf32 : (const void *)h.aa_cf64;
+    a.bb_cf = (sizeof(T) == 4) ? (const void *)h.bb_cf32 : (const void *)h.bb_cf64;
+    for (int q = 0; q < h.nab; ++q) {
+        a.ab_pa[q] = h.ab_pa[q]; a.ab_pb[q] = h.ab_pb[q];
+        a.ab_fjk[q] = h.ab_fjk[q]; a.ab_fkj[q] = h.ab_fkj[q]; a.ab_zz[q] = h.ab_zz[q];
+    }
+    a.scale = scale;
+    const int nsm = num_sms();
+    // ---- pass R
+    const size_t smem = (size_t)std::max<int64_t>(h.max_len, 1) * sizeof(T);
+    ED_CHECK_CUDA(cudaFuncSetAttribute(heis_row_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int64_t blocks = std::min<int64_t>(h.nrows, (int64_t)nsm * 4);
+    if (blocks < 1) blocks = 1;
+    heis_row_kernel<T><<<(unsigned)blocks, kHeisRowThreads, smem, st>>>(x, y, a);
+    ED_CHECK_LAUNCH();
+    // ---- pass S
+    SlabPlan p;
+    p.nblk = 0;
+    p.item_base[0] = 0;
+    for (int m = 0; m <= h.nA; ++m) {
+        const int64_t nr = h.row_base[m + 1] - h.row_base[m];
+        if (nr == 0) continue;
+        const int64_t len = h.ncol[m];
+        // the x slab of the block (nr rows x w) should take at most ~48 MB of L2
+        int64_t w = (int64_t)(48.0e6 / ((double)nr * sizeof(T)));
+        w = w / 32 * 32;
+        if (w < 256) w = 256;
+        if (w > len) w = len;
+        const int b = p.nblk++;
+        p.m[b] = m;
+        p.slab_w[b] = w;
+        p.ngroups[b] = (nr + 7) / 8;
+        p.item_base[b + 1] = p.item_base[b] + ((len + w - 1) / w) * p.ngroups[b];
+    }
+    int64_t blocks2 = std::min<int64_t>((int64_t)nsm * 8, kMaxPartialBlocksHeis);
+    if (blocks2 > p.item_base[p.nblk]) blocks2 = p.item_base[p.nblk];
+    if (blocks2 < 1) blocks2 = 1;
+    heis_slab_kernel<T><<<(unsigned)blocks2, 256, 0, st>>>(x, y, a, p, dots ? partials : nullptr);
+    ED_CHECK_LAUNCH();
+    if (dots) return launch_reduce(partials, (int)blocks2, 2, dots, st);
+    return ED_OK;
+}
+
+int heis_struct_hv(ed_sector *s, cudaStream_t st, int dtype, const void *x, void *y, double scale, double *dots,
+                   double *partials)
+{
+    if (!s->hs) {
+        set_error("Heisenberg sector without its row tables");
+        return ED_ERR_ARG;
+    }
+    if (dtype == ED_F32)
+        return heis_struct_run<float>(s, st, static_cast<const float *>(x), static_cast<float *>(y), scale, dots,
+                                      partials);
+    return heis_struct_run<double>(s, st, static_cast<const double *>(x), static_cast<double *>(y), scale, dots,
+                                   partials);
+}
+
+}  // namespace ed

@@ -490,9 +490,5 @@ extern "C" int ed_hv(ed_sector *s, void *stream, int dtype, int64_t ld, const vo
         return hub_hv<double>(s, st, ld, static_cast<const double *>(x), static_cast<double *>(y), scale, dots,
                               static_cast<double *>(scratch));
     }
-    if (dtype == ED_F32)
-        return heis_hv<float>(s, st, static_cast<const float *>(x), static_cast<float *>(y), scale, dots,
-                              static_cast<double *>(scratch));
-    return heis_hv<double>(s, st, static_cast<const double *>(x), static_cast<double *>(y), scale, dots,
-                           static_cast<double *>(scratch));
+    return heis_struct_hv(s, st, dtype, x, y, scale, dots, static_cast<double *>(scratch));
 }

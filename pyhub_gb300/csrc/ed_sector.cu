@@ -471,6 +471,7 @@ int ed_sector_create(int norb, int nup, int ndn, int kind, const double *t, cons
             s->j_host[i] = J[i];
         }
         rc = build_heis(s, J);
+        if (!rc) rc = heis_struct_build(s);
     }
     if (rc) {
         std::string keep = g_err;
@@ -488,6 +489,7 @@ int ed_sector_destroy(ed_sector *s)
     free_hop(s->dn);
     free_hop(s->up);
     if (s->lut) cudaFree(s->lut);
+    heis_struct_free(s->hs);
     delete s;
     return ED_OK;
 }
