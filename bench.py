@@ -58,9 +58,11 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--small", action="store_true", help="3x3 cluster, for a quick functional run")
-    p.add_argument("--config", default="c2", choices=["c2", "c4"],
-                   help="c2: 4x4 ground-state solve (default); c4: batched Green's functions of 256 clusters")
+    p.add_argument("--config", default="c2", choices=["c2", "c3", "c4"],
+                   help="c2: 4x4 Hubbard ground-state solve (default); c3: 4x8 Heisenberg ground state and "
+                        "nearest-neighbour spin correlations; c4: batched Green's functions of 256 clusters")
     p.add_argument("--clusters", type=int, default=256)
+    p.add_argument("--lattice", default="4x8", help="c3: periodic LXxLY lattice (default 4x8)")
     p.add_argument("--probe", action="store_true",
                    help="a few launches of each solve kernel on 4x4-sized vectors (about 4 GB), for profilers")
     return p.parse_args()
@@ -294,6 +296,88 @@ def run_c4(args):
         print(json.dumps(line), flush=True)
 
 
+def run_c3(args):
+    """4x8 periodic Heisenberg antiferromagnet (J=1 on the 64 bonds, S_z=0,
+    dim C(32,16) = 601,080,390): mixed-precision ground state by the
+    three-term Lanczos (FP32 vectors, FP64 scalars, 200 steps) with an FP64
+    three-term refinement, then the 64 nearest-neighbour <S_i.S_j>.  The
+    timed step is the whole solve; the H*v line is the structured product
+    alone (FP32 and FP64, CUDA events)."""
+    import numpy as np
+    import torch
+    from pyhub_gb300 import _build, _capi
+    from pyhub_gb300.core import lanczos as LZ
+    from pyhub_gb300.tools import lattices as LT
+    _build.build()
+    ws, rank, local = dist()
+    torch.cuda.set_device(local)
+    lx, ly = (4, 4) if args.small else tuple(int(v) for v in args.lattice.lower().split("x"))
+    J = LT.square(lx, ly, 1.0, periodic=True)
+    norb = lx * ly
+    t0 = time.perf_counter()
+    sec = _capi.Sector(norb, norb // 2, 0, _capi.ED_HEISENBERG, J=J)
+    t_sector = time.perf_counter() - t0
+    bonds = [(i + 1, j + 1) for i in range(norb) for j in range(i + 1, norb) if J[i, j] != 0.0]
+    scratch = torch.empty(_capi.scratch_bytes(sec.n, 1) // 8 + 1, dtype=torch.float64, device="cuda")
+    dots = torch.zeros(2, dtype=torch.float64, device="cuda")
+    hv_ms = {}
+    for dt in (torch.float32, torch.float64):
+        x = LZ.start_vector(sec, 0, dtype=dt)
+        y = torch.zeros_like(x)
+        for _ in range(2):
+            sec.hv(x, y, dots=dots, scratch=scratch)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(5):
+            sec.hv(x, y, dots=dots, scratch=scratch)
+        e1.record()
+        torch.cuda.synchronize()
+        hv_ms["f32" if dt == torch.float32 else "f64"] = e0.elapsed_time(e1) / 5
+        del x, y
+    torch.cuda.empty_cache()
+    clocks = ClockSampler(local)
+    clocks.start()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    # FP32 stage until E0 stalls at FP32 resolution; FP64 stage until the residual estimate is below 1e-9
+    gs = LZ.ground_state(sec, mode="mixed", steps=args.lanczos_steps, reorth="none", refine_steps=150,
+                         rule=LZ.EnergyRule(1e-7, min_steps=20), refine_rule=LZ.ResidualRule(1e-9, 10))
+    raw, _ = sec.rdm_raw(gs.psi, pairs=bonds)
+    torch.cuda.synchronize()
+    t_solve = time.perf_counter() - t0
+    clk = clocks.stop()
+    sij = raw[:, 0] + raw[:, 1]          # SMATRIX(J,K) as J_SPIN forms it (static_rq_heis.f90:66-114)
+    # The product's flip element is -(-1)^(J+K) J (hprod_heis.f90:39-45) while J_SPIN's transverse sum
+    # carries +(-1)^(J+K), so the energy is sum_{J!=K} J_JK (q1 - q0) = 2 sum_bonds (q1 - q0).
+    e_bonds = 2.0 * float(np.sum(raw[:, 1] - raw[:, 0]))
+    # residual ||H psi - E0 psi|| in FP64
+    y = torch.zeros_like(gs.psi)
+    sec.hv(gs.psi, y)
+    res = float(torch.linalg.vector_norm(y - gs.e0 * gs.psi))
+    peak, src = peaks()
+    gbs = 2 * sec.dim * 4 / (hv_ms["f32"] * 1e-3) / 1e9
+    if rank == 0:
+        line = {"metric": METRIC, "value": 1.0 / t_solve, "unit": "solve/s", "n_gpus": ws, "steps": 1, "warmup": 1,
+                "ms_per_step": t_solve * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32 vectors / f64 scalars + f64 refinement", "data": "synthetic (seeded start vector)",
+                "config": {"workload": f"Heisenberg {lx}x{ly} PBC, J=1, Sz=0, dim {sec.dim}; three-term Lanczos "
+                                       f"(FP32 to E0 stall, at most {args.lanczos_steps} steps) + FP64 three-term "
+                                       f"refinement to residual estimate 1e-9; nn <S.S>",
+                           "parallelism": "replicas"},
+                "e0": gs.e0, "e0_per_site": gs.e0 / norb, "e0_unrefined_fp32": gs.e0_unrefined,
+                "residual_fp64": res, "fp32_steps": int(gs.steps), "refine_steps": int(gs.refine_steps),
+                "nn_smatrix_mean": float(np.mean(sij)), "nn_sisj_energy_gauge_mean": float(np.mean(raw[:, 1] - raw[:, 0])),
+                "bond_energy_identity_err": gs.e0 - e_bonds,
+                "times_s": {k: float(v) for k, v in gs.times.items()}, "sector_create_s": t_sector,
+                "hv_ms": hv_ms,
+                "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                             "traffic": None, "kernel": "structured Heisenberg H*v (FP32), x read + y written",
+                             "peak_source": src},
+                "clocks": clk}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -301,6 +385,9 @@ def main():
         return
     if args.config == "c4":
         run_c4(args)
+        return
+    if args.config == "c3":
+        run_c3(args)
         return
     import numpy as np
     import torch

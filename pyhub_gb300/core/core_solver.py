@@ -186,6 +186,12 @@ class CoreSolver(Basis, GreenFunction, StaticQuantities):
             r = LZ.lanczos_plain(sec, v0.to(vt), steps, rule=rule, nvec=nvec)
             psis = r.psis
             ritz, alpha, beta, steps_done, conv = r.ritz, r.alpha, r.beta, r.steps, r.converged
+            if dtype == "mixed":
+                # FP64 three-term refinement from the FP32 Ritz vector (memory: four vectors)
+                rr = LZ.EnergyRule(1e-13 * max(1.0, abs(float(ritz[0]))), min_steps=10)
+                r2 = LZ.lanczos_plain(sec, psis[0], refine_steps, rule=rr, nvec=1)
+                psis = [r2.psis[0]] + list(psis[1:])
+                ritz = np.concatenate([[r2.ritz[0]], ritz[1:]])
         return {"eigenvalues": np.asarray(ritz), "psis": psis, "is_lanczos": True, "deg": rule.ndeg,
                 "alpha": alpha, "beta": beta, "nb_lcz": steps_done, "conv": rule.conv,
                 "converged": conv, "H": None, "nstates": sec.dim, "precision": dtype, "reorth": reorth}

@@ -387,7 +387,12 @@ def lanczos_plain(sec, v0, max_steps: int, rule=None, check_every: int = NADD, n
                 break
             s_prev, s_cur, bprev = s_cur, 1.0 / math.sqrt(nw2), b
             if psis is None and rule is not None and done % check_every == 0:
-                if rule(_tridiag_eigs(np.array(alpha), np.array(beta), done), done):
+                if getattr(rule, "wants_vectors", False):
+                    val, vec = _tridiag_eigs(np.array(alpha), np.array(beta), done, vectors=True)
+                    stop = rule(val, done, vec=vec, beta_last=b)
+                else:
+                    stop = rule(_tridiag_eigs(np.array(alpha), np.array(beta), done), done)
+                if stop:
                     conv = True
                     break
         return np.array(alpha), np.array(beta), done, conv
@@ -424,7 +429,7 @@ class GroundState:
 
 def ground_state(sec, mode: str = "mixed", steps: int = 200, seed: int = 0, v0=None, rule=None,
                  refine_steps: int = 60, refine_tol: float = 1e-13, check_every: int = NADD,
-                 timer: KernelTimer = None) -> GroundState:
+                 timer: KernelTimer = None, reorth: str = "full", refine_rule=None) -> GroundState:
     """Ground state of the sector operator.
 
     mode "f64":   FP64 vectors, FP64 scalars (the plain FP64 GPU Lanczos).
@@ -432,11 +437,18 @@ def ground_state(sec, mode: str = "mixed", steps: int = 200, seed: int = 0, v0=N
     mode "mixed": FP32 vectors + FP64 scalars for ``steps`` steps, then an
                   FP64 Lanczos restarted from the FP32 Ritz vector until the
                   lowest Ritz value moves less than refine_tol*max(1,|E0|)
-                  between checks (at most refine_steps steps)."""
+                  between checks (at most refine_steps steps).
+    reorth "full" keeps every Krylov vector (lanczos_full); "none" runs the
+    three-term recurrence on four vectors and rebuilds the Ritz vector by a
+    second pass (lanczos_plain), for sectors whose basis would not fit;
+    refine_rule (reorth "none") replaces the energy rule of the FP64 stage."""
     torch = _torch()
     t0 = time.perf_counter()
     if v0 is None:
         v0 = start_vector(sec, seed)
+    if reorth == "none":
+        return _ground_state_plain(sec, mode, steps, v0, rule, refine_steps, refine_tol, check_every, t0,
+                                   refine_rule=refine_rule)
     if mode == "f64":
         r = lanczos_full(sec, v0.to(torch.float64), steps, torch.float64, rule=rule, check_every=check_every,
                          timer=timer)
@@ -462,3 +474,26 @@ def ground_state(sec, mode: str = "mixed", steps: int = 200, seed: int = 0, v0=N
                        steps=r32.steps, refine_steps=r64.steps, converged=r32.converged or rr.converged,
                        ndeg=r32.ndeg, times={"total": t2 - t0, "fp32": t1 - t0, "refine": t2 - t1}, mode=mode,
                        e0_unrefined=float(r32.ritz[0]), ritz_vectors=r64.ritz_vectors)
+
+
+def _ground_state_plain(sec, mode, steps, v0, rule, refine_steps, refine_tol, check_every, t0,
+                        refine_rule=None) -> GroundState:
+    torch = _torch()
+    vt = torch.float64 if mode == "f64" else torch.float32
+    r = lanczos_plain(sec, v0.to(vt), steps, rule=rule, check_every=check_every, nvec=1)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    e0u = float(r.ritz[0])
+    if mode != "mixed":
+        return GroundState(e0=e0u, psi=r.psis[0], ritz=r.ritz, alpha=r.alpha, beta=r.beta, steps=r.steps,
+                           refine_steps=0, converged=r.converged, ndeg=1,
+                           times={"total": t1 - t0, mode: t1 - t0}, mode=mode, e0_unrefined=e0u,
+                           ritz_vectors=r.ritz_vectors)
+    rr = refine_rule or EnergyRule(refine_tol * max(1.0, abs(e0u)), min_steps=2 * check_every)
+    r64 = lanczos_plain(sec, r.psis[0], refine_steps, rule=rr, check_every=check_every, nvec=1)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    return GroundState(e0=float(r64.ritz[0]), psi=r64.psis[0], ritz=r64.ritz, alpha=r.alpha, beta=r.beta,
+                       steps=r.steps, refine_steps=r64.steps, converged=r.converged or rr.converged, ndeg=1,
+                       times={"total": t2 - t0, "fp32": t1 - t0, "refine": t2 - t1}, mode=mode,
+                       e0_unrefined=e0u, ritz_vectors=r64.ritz_vectors)

@@ -118,6 +118,8 @@ int heis_struct_build(ed_sector *s);
 void heis_struct_free(HeisStruct *hs);
 int heis_struct_hv(ed_sector *s, cudaStream_t st, int dtype, const void *x, void *y, double scale, double *dots,
                    double *partials);
+int heis_struct_rdm(ed_sector *s, cudaStream_t st, int dtype, const void *bra, const void *ket, int npairs,
+                    const int32_t *pairs, double *out, double *scratch, int max_blocks);
 int launch_reduce(const double *partials, int nblocks, int m, double *out, cudaStream_t st);
 
 }  // namespace ed

@@ -422,6 +422,165 @@ __global__ void __launch_bounds__(256) heis_slab_kernel(const T *__restrict__ x,
     }
 }
 
+// ------------------------------------------------------------ spin correlations
+//
+// J_SPIN of the Heisenberg solver (static_rq_heis.f90:58-116) on the row
+// layout, per pair p = (J,K) of the caller's list:
+//   q[p][0] = J!=K: sum over states I with J up, K down of (-1)^(J+K) bra[I'] ket[I]
+//             (I' = I with J and K swapped);  J==K: 0.5 sum bra ket
+//   q[p][1] = sum bra ket Sz_J Sz_K
+// CTAs are (row range, chunk of kRdmP pairs); each thread keeps the chunk's
+// sums in registers over all its rows, so one pass over the vector serves
+// kRdmP pairs.
+
+constexpr int kRdmP = 8;
+constexpr int kRdmThreads = 256;
+
+struct HsRdmArgs {
+    int nA, npairs;
+    int64_t nrows;
+    int64_t col_base[kMaxHalf + 2], ncol[kMaxHalf + 1];
+    const uint32_t *col_pat, *row_pat;
+    const int32_t *rankA, *row_m, *rowidx;
+    const int64_t *row_off;
+    int16_t pj[kMaxSites * kMaxSites], pk[kMaxSites * kMaxSites];   // hole-bit positions (site-1)
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kRdmThreads) heis_rdm_row_kernel(const T *__restrict__ bra, const T *__restrict__ ket,
+                                                                   const HsRdmArgs a, double *__restrict__ partials)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *xs = reinterpret_cast<T *>(smem_raw);   // the bra row
+    const int p0 = blockIdx.y * kRdmP;
+    const int np = min(kRdmP, a.npairs - p0);
+    const int nA = a.nA;
+    double acc0[kRdmP], acc1[kRdmP];
+#pragma unroll
+    for (int q = 0; q < kRdmP; ++q) acc0[q] = acc1[q] = 0.0;
+    for (int64_t row = blockIdx.x; row < a.nrows; row += gridDim.x) {
+        const uint32_t hb = __ldg(a.row_pat + row);
+        const int m = __ldg(a.row_m + row);
+        const int64_t off = __ldg(a.row_off + row);
+        const int len = (int)a.ncol[m];
+        const int64_t cbase = a.col_base[m];
+        __syncthreads();
+        for (int c = threadIdx.x; c < len; c += blockDim.x) xs[c] = bra[off + c];
+        __syncthreads();
+        // per-row facts of every pair: source row offset of the swapped state (or -1)
+        int64_t soff[kRdmP];
+#pragma unroll
+        for (int q = 0; q < kRdmP; ++q) {
+            soff[q] = -1;
+            if (q >= np) continue;
+            const int J = a.pj[p0 + q], K = a.pk[p0 + q];
+            uint32_t mb = 0;
+            if (J >= nA) mb |= 1u << (J - nA);
+            if (K >= nA) mb |= 1u << (K - nA);
+            if (mb) {
+                const int32_t r2 = __ldg(a.rowidx + (hb ^ mb));
+                if (r2 >= 0) soff[q] = __ldg(a.row_off + r2);
+            } else {
+                soff[q] = off;
+            }
+        }
+        T r0[kRdmP], r1[kRdmP];
+#pragma unroll
+        for (int q = 0; q < kRdmP; ++q) r0[q] = r1[q] = 0;
+        for (int c = threadIdx.x; c < len; c += blockDim.x) {
+            const uint32_t ha = __ldg(a.col_pat + cbase + c);
+            const uint64_t h = (uint64_t)ha | ((uint64_t)hb << nA);   // bit j: site j+1 is down
+            const T kv = __ldg(ket + off + c);
+            const T bk = xs[c] * kv;
+#pragma unroll
+            for (int q = 0; q < kRdmP; ++q) {
+                if (q >= np) break;
+                const int J = a.pj[p0 + q], K = a.pk[p0 + q];
+                const int dJ = (int)((h >> J) & 1u), dK = (int)((h >> K) & 1u);
+                if (J == K) {
+                    r0[q] += (T)0.5 * bk;
+                    r1[q] += (T)0.25 * bk;
+                    continue;
+                }
+                r1[q] += (dJ == dK) ? (T)0.25 * bk : (T)-0.25 * bk;
+                if (dJ || !dK || soff[q] < 0) continue;   // needs J up, K down
+                // the swapped state: A part and B part of h ^ (bit J | bit K)
+                uint32_t ma = 0;
+                if (J < nA) ma |= 1u << J;
+                if (K < nA) ma |= 1u << K;
+                const T sg = ((J + K) & 1) ? (T)-1 : (T)1;   // (-1)^((J+1)+(K+1))
+                const int cs = ma ? __ldg(a.rankA + (ha ^ ma)) : c;
+                const T bv = (soff[q] == off) ? xs[cs] : __ldg(bra + soff[q] + cs);
+                r0[q] += sg * bv * kv;
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kRdmP; ++q) {
+            acc0[q] += (double)r0[q];
+            acc1[q] += (double)r1[q];
+        }
+    }
+    __shared__ double red[kRdmThreads / 32][kRdmP][2];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int q = 0; q < kRdmP; ++q) {
+        const double w0 = warp_sum(acc0[q]), w1 = warp_sum(acc1[q]);
+        if (lane == 0) {
+            red[warp][q][0] = w0;
+            red[warp][q][1] = w1;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 2 * np) {
+        const int q = threadIdx.x >> 1, k = threadIdx.x & 1;
+        double t = 0.0;
+        for (int w = 0; w < kRdmThreads / 32; ++w) t += red[w][q][k];
+        partials[((int64_t)blockIdx.x * a.npairs + p0 + q) * 2 + k] = t;
+    }
+}
+
+template <typename T>
+static int heis_struct_rdm_run(ed_sector *s, cudaStream_t st, const T *bra, const T *ket, int npairs,
+                               const int32_t *pairs, double *out, double *scratch, int max_blocks)
+{
+    const HeisStruct &h = *s->hs;
+    HsRdmArgs a;
+    a.nA = h.nA;
+    a.npairs = npairs;
+    a.nrows = h.nrows;
+    for (int m = 0; m <= kMaxHalf + 1; ++m) {
+        a.col_base[m] = h.col_base[m];
+        if (m <= kMaxHalf) a.ncol[m] = h.ncol[m];
+    }
+    a.col_pat = h.col_pat; a.row_pat = h.row_pat;
+    a.rankA = h.rankA; a.row_m = h.row_m; a.rowidx = h.rowidx; a.row_off = h.row_off;
+    for (int p = 0; p < npairs; ++p) {
+        a.pj[p] = (int16_t)(pairs[2 * p] - 1);
+        a.pk[p] = (int16_t)(pairs[2 * p + 1] - 1);
+    }
+    const size_t smem = (size_t)std::max<int64_t>(h.max_len, 1) * sizeof(T);
+    ED_CHECK_CUDA(cudaFuncSetAttribute(heis_rdm_row_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int gx = (int)std::max<int64_t>(1, std::min<int64_t>(h.nrows, max_blocks));
+    const dim3 grid((unsigned)gx, (unsigned)((npairs + kRdmP - 1) / kRdmP));
+    heis_rdm_row_kernel<T><<<grid, kRdmThreads, smem, st>>>(bra, ket, a, scratch);
+    ED_CHECK_LAUNCH();
+    return launch_reduce(scratch, gx, 2 * npairs, out, st);
+}
+
+int heis_struct_rdm(ed_sector *s, cudaStream_t st, int dtype, const void *bra, const void *ket, int npairs,
+                    const int32_t *pairs, double *out, double *scratch, int max_blocks)
+{
+    if (!s->hs) {
+        set_error("Heisenberg sector without its row tables");
+        return ED_ERR_ARG;
+    }
+    if (dtype == ED_F32)
+        return heis_struct_rdm_run<float>(s, st, static_cast<const float *>(bra), static_cast<const float *>(ket),
+                                          npairs, pairs, out, scratch, max_blocks);
+    return heis_struct_rdm_run<double>(s, st, static_cast<const double *>(bra), static_cast<const double *>(ket),
+                                       npairs, pairs, out, scratch, max_blocks);
+}
+
 template <typename T>
 static int heis_struct_run(ed_sector *s, cudaStream_t st, const T *x, T *y, double scale, double *dots,
                            double *partials)

@@ -12,8 +12,8 @@
 //   its ~N neighbour rows; x therefore streams from HBM about once.  The pass
 //   also forms <x,y> and <y,y> for the Lanczos scalars.
 //
-// Heisenberg (replaces HPROD, hprod_heis.f90:1-61): one gather per
-// antiparallel bond with the flipped string ranked through byte tables.
+// Heisenberg (replaces HPROD, hprod_heis.f90:1-61): ed_heis.cu, on the same
+// row/pass structure (rows of B-half patterns over A-half patterns).
 #include "ed_common.cuh"
 
 namespace ed {
@@ -263,84 +263,7 @@ int launch_reduce(const double *partials, int nblocks, int m, double *out, cudaS
     return ED_OK;
 }
 
-// ------------------------------------------------------------ Heisenberg
-
-struct HeisArgs {
-    int norb, nholes;
-    int64_t n;
-    const uint32_t *lut;  // [4][33][256]
-    int nbond;
-    int8_t bj[kMaxSites * kMaxSites / 2];
-    int8_t bk[kMaxSites * kMaxSites / 2];
-    double flip_jk[kMaxSites * kMaxSites / 2];
-    double flip_kj[kMaxSites * kMaxSites / 2];
-    double zz[kMaxSites * kMaxSites / 2];
-    double dconst;
-    double scale;
-    uint32_t binom[kMaxSites + 1][17];
-};
-
-// colex unrank of an m-hole pattern among norb positions
-__device__ __forceinline__ uint32_t heis_unrank(const HeisArgs &a, uint32_t r)
-{
-    uint32_t h = 0;
-    int p = a.norb - 1;
-    for (int i = a.nholes; i >= 1; --i) {
-        while (p >= i && a.binom[p][i] > r) --p;
-        // largest p with C(p,i) <= r (p >= i-1 always satisfies since C(i-1,i)=0)
-        if (p < i) p = i - 1;
-        h |= 1u << p;
-        r -= a.binom[p][i];
-        --p;
-    }
-    return h;
-}
-
-template <typename T>
-__global__ void __launch_bounds__(256) heis_kernel(const T *__restrict__ x, T *__restrict__ y, const HeisArgs a,
-                                                   double *__restrict__ partials)
-{
-    double dxy = 0.0, dyy = 0.0;
-    const uint32_t full = (a.norb >= 32) ? 0xFFFFFFFFu : ((1u << a.norb) - 1u);
-    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t h = heis_unrank(a, (uint32_t)p);  // bit j: site j+1 is a down spin
-        T dg = (T)a.dconst;
-        T acc = 0;
-        for (int b = 0; b < a.nbond; ++b) {
-            const int J = a.bj[b], K = a.bk[b];
-            const uint32_t hj = (h >> (J - 1)) & 1u, hk = (h >> (K - 1)) & 1u;
-            if (hj == hk) {
-                dg += (T)(0.25 * a.zz[b]);
-                continue;
-            }
-            dg -= (T)(0.25 * a.zz[b]);
-            // target has K up (hk==0) and J down (hj==1): element flip_jk, else flip_kj
-            const double c = hj ? a.flip_jk[b] : a.flip_kj[b];
-            if (c == 0.0) continue;
-            const uint32_t q = h ^ ((1u << (J - 1)) | (1u << (K - 1)));
-            acc += (T)c * __ldg(x + rank_holes(a.lut, q));
-        }
-        (void)full;
-        const T xv = x[p];
-        const T out = (dg * xv + acc) * (T)a.scale;
-        y[p] = out;
-        if (partials) { dxy += (double)xv * (double)out; dyy += (double)out * (double)out; }
-    }
-    if (partials) {
-        __shared__ double red[2][8];
-        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-        dxy = warp_sum(dxy);
-        dyy = warp_sum(dyy);
-        if (lane == 0) { red[0][warp] = dxy; red[1][warp] = dyy; }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double sxy = 0.0, syy = 0.0;
-            for (int w = 0; w < 8; ++w) { sxy += red[0][w]; syy += red[1][w]; }
-            partials[2 * blockIdx.x] = sxy;
-            partials[2 * blockIdx.x + 1] = syy;
-        }
-    }
-}
+// The Heisenberg product lives in ed_heis.cu.
 
 // ------------------------------------------------------------ launchers
 
@@ -422,37 +345,6 @@ static int hub_hv(ed_sector *s, cudaStream_t st, int64_t ld, const T *x, T *y, d
         hub_slab_kernel<T, 1><<<(unsigned)blocks2, 256, 0, st>>>(x, y, a, slab_w, ngroups, nitems, part);
     ED_CHECK_LAUNCH();
     if (dots) return launch_reduce(partials, (int)blocks2, 2, dots, st);
-    return ED_OK;
-}
-
-template <typename T>
-static int heis_hv(ed_sector *s, cudaStream_t st, const T *x, T *y, double scale, double *dots, double *partials)
-{
-    HeisArgs a;
-    const HeisTables &h = s->heis;
-    a.norb = s->norb;
-    a.nholes = s->norb - s->nup;
-    a.n = s->nsup;
-    a.lut = s->lut;
-    if (h.nbond > kMaxSites * kMaxSites / 2) { set_error("too many bonds"); return ED_ERR_RANGE; }
-    a.nbond = h.nbond;
-    for (int b = 0; b < h.nbond; ++b) {
-        a.bj[b] = h.bj[b]; a.bk[b] = h.bk[b];
-        a.flip_jk[b] = h.flip_jk[b]; a.flip_kj[b] = h.flip_kj[b]; a.zz[b] = h.zz[b];
-    }
-    a.dconst = h.dconst;
-    a.scale = scale;
-    for (int n = 0; n <= kMaxSites; ++n)
-        for (int k = 0; k <= 16; ++k) a.binom[n][k] = (uint32_t)ed_binom(n, k);
-    const int nsm = num_sms();
-    int64_t blocks = (s->nsup + 255) / 256;
-    int64_t cap = (int64_t)nsm * 8;
-    if (cap > kMaxPartialBlocks) cap = kMaxPartialBlocks;
-    if (blocks > cap) blocks = cap;
-    if (blocks < 1) blocks = 1;
-    heis_kernel<T><<<(unsigned)blocks, 256, 0, st>>>(x, y, a, dots ? partials : nullptr);
-    ED_CHECK_LAUNCH();
-    if (dots) return launch_reduce(partials, (int)blocks, 2, dots, st);
     return ED_OK;
 }
 

@@ -171,73 +171,6 @@ __global__ void __launch_bounds__(256) rdm_cross_kernel(const T *__restrict__ br
     for (int i = threadIdx.x; i < 2 * a.npairs; i += blockDim.x) partials[(int64_t)blockIdx.x * 2 * a.npairs + i] = acc[i];
 }
 
-// Heisenberg: states in a grid-stride loop, per-pair sums aggregated by warp.
-struct HeisRdmArgs {
-    int norb, nholes;
-    int64_t n;
-    const uint32_t *lut;
-    int npairs;
-    int8_t pj[kMaxPairs], pk[kMaxPairs];
-    uint32_t binom[kMaxSites + 1][17];
-};
-
-__device__ __forceinline__ uint32_t unrank_holes(const HeisRdmArgs &a, uint32_t r)
-{
-    uint32_t h = 0;
-    int p = a.norb - 1;
-    for (int i = a.nholes; i >= 1; --i) {
-        while (p >= i && a.binom[p][i] > r) --p;
-        if (p < i) p = i - 1;
-        h |= 1u << p;
-        r -= a.binom[p][i];
-        --p;
-    }
-    return h;
-}
-
-template <typename T>
-__global__ void __launch_bounds__(256) heis_rdm_kernel(const T *__restrict__ bra, const T *__restrict__ ket,
-                                                       const HeisRdmArgs a, double *__restrict__ partials)
-{
-    extern __shared__ double hacc[];  // [8 warps][npairs][2]
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int i = threadIdx.x; i < 16 * a.npairs; i += blockDim.x) hacc[i] = 0.0;
-    __syncthreads();
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    const int64_t nround = (a.n + stride - 1) / stride;
-    for (int64_t it = 0; it < nround; ++it) {
-        const int64_t s = it * stride + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-        const bool ok = s < a.n;
-        const uint32_t h = ok ? unrank_holes(a, (uint32_t)s) : 0u;  // bit j: site j+1 is a down spin
-        const double bk = ok ? (double)bra[s] * (double)ket[s] : 0.0;
-        for (int p = 0; p < a.npairs; ++p) {
-            const int J = a.pj[p], K = a.pk[p];
-            const int dJ = (h >> (J - 1)) & 1, dK = (h >> (K - 1)) & 1;
-            double c0 = 0.0;
-            if (ok) {
-                if (J == K) c0 = 0.5 * bk;
-                else if (!dJ && dK) {  // J up, K down in this state
-                    const uint32_t q = h ^ ((1u << (J - 1)) | (1u << (K - 1)));
-                    const double sg = ((J + K) & 1) ? -1.0 : 1.0;
-                    c0 = sg * (double)bra[rank_holes(a.lut, q)] * (double)ket[s];
-                }
-            }
-            const double c1 = (dJ == dK) ? 0.25 * bk : -0.25 * bk;
-            const double w0 = warp_sum(c0), w1 = warp_sum(c1);
-            if (lane == 0) {
-                hacc[(warp * a.npairs + p) * 2] += w0;
-                hacc[(warp * a.npairs + p) * 2 + 1] += w1;
-            }
-        }
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < 2 * a.npairs; i += blockDim.x) {
-        double t = 0.0;
-        for (int w = 0; w < 8; ++w) t += hacc[w * 2 * a.npairs + i];
-        partials[(int64_t)blockIdx.x * 2 * a.npairs + i] = t;
-    }
-}
-
 static constexpr int kRdmBlocks = 256;
 
 template <typename T>
@@ -282,28 +215,6 @@ static int rdm_hub(ed_sector *s, cudaStream_t st, int64_t ld, const T *bra, cons
     return ED_OK;
 }
 
-template <typename T>
-static int rdm_heis(ed_sector *s, cudaStream_t st, const T *bra, const T *ket, int npairs, const int32_t *pairs,
-                    double *out, double *scratch)
-{
-    HeisRdmArgs a;
-    a.norb = s->norb;
-    a.nholes = s->norb - s->nup;
-    a.n = s->nsup;
-    a.lut = s->lut;
-    a.npairs = npairs;
-    for (int p = 0; p < npairs; ++p) { a.pj[p] = (int8_t)pairs[2 * p]; a.pk[p] = (int8_t)pairs[2 * p + 1]; }
-    for (int n = 0; n <= kMaxSites; ++n)
-        for (int k = 0; k <= 16; ++k) a.binom[n][k] = (uint32_t)ed_binom(n, k);
-    int blocks = (int)std::min<int64_t>((s->nsup + 255) / 256, kRdmBlocks);
-    if (blocks < 1) blocks = 1;
-    const size_t smem = sizeof(double) * 16 * (size_t)npairs;
-    ED_CHECK_CUDA(cudaFuncSetAttribute(heis_rdm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    heis_rdm_kernel<T><<<blocks, 256, smem, st>>>(bra, ket, a, scratch);
-    ED_CHECK_LAUNCH();
-    return launch_reduce(scratch, blocks, 2 * npairs, out, st);
-}
-
 }  // namespace ed
 
 using namespace ed;
@@ -337,7 +248,6 @@ extern "C" int ed_rdm(ed_sector *s, void *stream, int dtype, int64_t ld, const v
         return rdm_hub<double>(s, st, ld, (const double *)bra, (const double *)ket, npairs, pairs, flags, out,
                                (double *)scratch);
     }
-    if (dtype == ED_F32)
-        return rdm_heis<float>(s, st, (const float *)bra, (const float *)ket, npairs, pairs, out, (double *)scratch);
-    return rdm_heis<double>(s, st, (const double *)bra, (const double *)ket, npairs, pairs, out, (double *)scratch);
+    // partials [blocks][npairs][2] fit in the kRdmBlocks*kRdmQ*npairs doubles of ed_rdm_scratch_bytes
+    return heis_struct_rdm(s, st, dtype, bra, ket, npairs, pairs, out, (double *)scratch, kRdmBlocks);
 }

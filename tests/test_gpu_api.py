@@ -186,3 +186,32 @@ def test_three_term_lanczos_matches_full(edlib, dt):
         # dozen steps, so only the FP64 Ritz vector is compared
         ov = float((a.psi * b.psis[0]).sum().item())
         assert abs(abs(ov) - 1) < 1e-8
+
+
+def test_heisenberg_lattice_rdm_and_plain_mixed_ground_state(edlib):
+    """4x4 periodic Heisenberg (dim 12,870): spin correlations of the row
+    layout vs the oracle's J_SPIN on random bra/ket (all pairs, 1e-11); the
+    three-term mixed-precision ground state (FP32 then FP64 refinement, four
+    vectors) vs the full-reorthogonalisation FP64 one (|dE0| < 1e-9); and the
+    bond-energy identity E0 = sum_{J!=K} J_JK (q1 - q0) on its vector."""
+    import torch
+    from pyhub_gb300.core import lanczos as LZ
+    from pyhub_gb300.core.reduced_quantities import all_pairs, assemble_heisenberg
+    norb = 16
+    J = O.square_pbc(4, 4, 1.0)
+    sec = edlib.Sector(norb, 8, 0, edlib.ED_HEISENBERG, J=J)
+    rng = np.random.default_rng(4)
+    bra = rng.standard_normal(sec.dim)
+    ket = rng.standard_normal(sec.dim)
+    raw, _ = sec.rdm_raw(sec.from_ref(torch.tensor(bra, device="cuda")), sec.from_ref(torch.tensor(ket, device="cuda")),
+                         pairs=all_pairs(norb))
+    ref = O.j_spin_heis(norb, bra, ket)
+    assert np.abs(assemble_heisenberg(raw, norb) - ref).max() < 1e-11 * np.abs(ref).max()
+    full = LZ.ground_state(sec, mode="f64", steps=300, rule=LZ.ResidualRule(1e-11, 10))
+    gs = LZ.ground_state(sec, mode="mixed", steps=150, reorth="none", refine_steps=150,
+                         rule=LZ.EnergyRule(1e-9, min_steps=20))
+    assert abs(gs.e0 - full.e0) < 1e-9, (gs.e0, full.e0)
+    bonds = [(i + 1, j + 1) for i in range(norb) for j in range(norb) if i != j and J[i, j] != 0.0]
+    r2, _ = sec.rdm_raw(gs.psi, pairs=bonds)
+    e_bonds = sum(J[j - 1, i - 1] * (q[1] - q[0]) for (i, j), q in zip(bonds, r2))
+    assert abs(gs.e0 - e_bonds) < 1e-8, (gs.e0, e_bonds)
