@@ -58,11 +58,13 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--small", action="store_true", help="3x3 cluster, for a quick functional run")
-    p.add_argument("--config", default="c2", choices=["c2", "c3", "c4"],
+    p.add_argument("--config", default="c2", choices=["c2", "c3", "c4", "c5"],
                    help="c2: 4x4 Hubbard ground-state solve (default); c3: 4x8 Heisenberg ground state and "
-                        "nearest-neighbour spin correlations; c4: batched Green's functions of 256 clusters")
+                        "nearest-neighbour spin correlations; c4: batched Green's functions of 256 clusters; "
+                        "c5: gradients of E0 and of a 1-RDM loss for a 14-site random-bond cluster")
     p.add_argument("--clusters", type=int, default=256)
     p.add_argument("--lattice", default="4x8", help="c3: periodic LXxLY lattice (default 4x8)")
+    p.add_argument("--fd-params", type=int, default=8, help="c5: parameters checked by central differences")
     p.add_argument("--probe", action="store_true",
                    help="a few launches of each solve kernel on 4x4-sized vectors (about 4 GB), for profilers")
     return p.parse_args()
@@ -378,6 +380,90 @@ def run_c3(args):
         print(json.dumps(line), flush=True)
 
 
+def run_c5(args):
+    """14-site random-bond Hubbard cluster (ring + 7 seeded extra bonds,
+    t~U[0.5,1.5], U_i~U[2,6], eps_i~N(0,0.3^2), N_up=N_down=7, dim 3432^2 =
+    11,778,624), 49 parameters.  One step: forward (mixed-precision ground
+    state + spin-resolved 1-RDM) and backward (dE0/dtheta by the fused
+    Hellmann-Feynman RDM pass; dL/dtheta of L = sum_s ||gamma_s - target_s||^2
+    by the adjoint MINRES solve), target = the 1-RDM at a second seeded draw
+    of the parameters on the same bonds.  Checked against central
+    differences (h = 1e-5) of FP64 solves on a sample of parameters."""
+    import numpy as np
+    import torch
+    from pyhub_gb300 import _build
+    from pyhub_gb300.core import gradients as GR
+    from pyhub_gb300.tools import lattices as LT
+    _build.build()
+    ws, rank, local = dist()
+    torch.cuda.set_device(local)
+    n = 10 if args.small else 14
+    N = n // 2
+    t, U, bonds = LT.random_bond_cluster(n, 7 if n == 14 else 3, seed=0)
+    params = GR.HubbardParams(n, [tuple(b) for b in bonds])
+    theta = params.pack(t, U)
+    rng = np.random.default_rng(1)
+    t2 = np.zeros_like(t)
+    for (i, j) in params.bonds:
+        t2[i, j] = t2[j, i] = rng.uniform(0.5, 1.5)
+    t2[np.diag_indices(n)] = rng.normal(0.0, 0.3, n)
+    target = GR.solve(params, params.pack(t2, rng.uniform(2.0, 6.0, n)), N, N, mode="f64").gamma
+
+    def step():
+        sol = GR.solve(params, theta, N, N, mode="mixed")
+        g_e = GR.hf_gradient(params, sol)
+        L, g_l, info = GR.rdm_loss_gradient(params, sol, target)
+        torch.cuda.synchronize()
+        return sol, g_e, L, g_l, info
+
+    for _ in range(max(args.warmup, 1)):
+        step()
+    clocks = ClockSampler(local)
+    clocks.start()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        sol, g_e, L, g_l, info = step()
+        times.append(time.perf_counter() - t0)
+    clk = clocks.stop()
+    # central differences of FP64 solves on a sample of parameters (bonds, U, eps)
+    nb = len(params.bonds)
+    k = max(1, args.fd_params)
+    pick = sorted(set([int(v) for v in np.linspace(0, nb - 1, max(1, k // 2))] +
+                      [nb + int(v) for v in np.linspace(0, n - 1, max(1, k // 4))] +
+                      [nb + n + int(v) for v in np.linspace(0, n - 1, max(1, k - k // 2 - k // 4))]))
+    h = 1e-5
+    fd_e, fd_l = [], []
+    for p in pick:
+        vals = []
+        for sgn in (1.0, -1.0):
+            th = theta.copy()
+            th[p] += sgn * h
+            so = GR.solve(params, th, N, N, mode="f64")
+            gu, gd = so.gamma["up"], so.gamma["down"]
+            vals.append((so.e0, float(np.sum((gu - target["up"]) ** 2) + np.sum((gd - target["down"]) ** 2))))
+        fd_e.append((vals[0][0] - vals[1][0]) / (2 * h))
+        fd_l.append((vals[0][1] - vals[1][1]) / (2 * h))
+    fd_e, fd_l = np.array(fd_e), np.array(fd_l)
+    err_e = float(np.max(np.abs(g_e[pick] - fd_e)) / max(1e-12, np.max(np.abs(fd_e))))
+    err_l = float(np.max(np.abs(g_l[pick] - fd_l)) / max(1e-12, np.max(np.abs(fd_l))))
+    ms = statistics.median(times) * 1e3
+    if rank == 0:
+        line = {"metric": METRIC, "value": 1e3 / ms, "unit": "grad-evals/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": max(args.warmup, 1), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32 H*v + f64 refinement (forward), f64 adjoint",
+                "data": "synthetic (seeded cluster parameters)",
+                "config": {"workload": f"{n}-site random-bond Hubbard (ring + extra bonds), N_up=N_down={N}, "
+                                       f"dim {sol.sector.dim}, {params.nparams} parameters; forward E0 + 1-RDM, "
+                                       "backward dE0/dtheta (Hellmann-Feynman) + d||gamma-target||^2/dtheta "
+                                       "(adjoint MINRES)", "parallelism": "replicas"},
+                "e0": sol.e0, "loss": L, "minres_iters": info["minres_iters"], "minres_relres": info["minres_relres"],
+                "fd_check": {"params": [params.names()[p] for p in pick], "h": h,
+                             "max_rel_err_dE0": err_e, "max_rel_err_dL": err_l},
+                "clocks": clk}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -388,6 +474,9 @@ def main():
         return
     if args.config == "c3":
         run_c3(args)
+        return
+    if args.config == "c5":
+        run_c5(args)
         return
     import numpy as np
     import torch

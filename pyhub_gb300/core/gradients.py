@@ -193,11 +193,15 @@ def rdm_loss_gradient(params: HubbardParams, sol: Solution, target: dict, maxite
     gu, gd = sol.gamma["up"], sol.gamma["down"]
     L = float(np.sum((gu - target["up"]) ** 2) + np.sum((gd - target["down"]) ** 2))
     Gu, Gd = 2.0 * (gu - target["up"]), 2.0 * (gd - target["down"])
-    if np.abs(Gu - Gd).max() > 1e-8 * max(1.0, np.abs(Gu).max()):
+    # The one-body operator is applied through a sector product, which acts on both spins with one
+    # matrix.  With N_up = N_down and spin-symmetric targets the two weights agree up to the solve's
+    # rounding; their mean is applied, and a real asymmetry is refused.
+    if np.abs(Gu - Gd).max() > 1e-4 * max(1.0, np.abs(Gu).max()):
         raise NotImplementedError("spin-dependent loss weights (gamma_up != gamma_down) are not supported")
+    G = 0.5 * (Gu + Gd)
     psi = sol.psi
     Apsi = torch.zeros_like(psi)
-    _apply_one_body(sol, Gu, psi, Apsi)
+    _apply_one_body(sol, G, psi, Apsi)
     b = -2.0 * Apsi
     work = torch.zeros_like(psi)
 
