@@ -36,13 +36,16 @@ struct BatchInst {
     const float *ucf32, *dcf32;
     const double *ucf64, *dcf64;
     const double *uediag, *dediag;
+    const float *uediag32, *dediag32;
     const double *u_site;             // device, indexed by bit
+    const float *u_site32;
     const int32_t *ell_off, *ell_src; // sliced-ELL up-hop table of the sector
     const float *ell_cf32;
     const double *ell_cf64;
     const int2 *ell_pk32;
     int nslice;
     double u_value;
+    float u_value32;
     int u_uniform;
     int64_t blk0;                     // first CTA of this instance
     int nblk;
@@ -57,6 +60,7 @@ struct ed_batch {
     ed::BatchInst *dev = nullptr;      // [ninst]
     int32_t *blk_inst = nullptr;       // [nblocks] device: instance of every CTA
     double *u_site_all = nullptr;      // [ninst][kMaxSites] device
+    float *u_site_all32 = nullptr;     // the same in FP32
     std::vector<int64_t> offsets, dims;
     int max_nsup = 0;
     int max_ld = 0;
@@ -78,11 +82,12 @@ __device__ __forceinline__ double sum_partials_warp(const double *__restrict__ p
 template <typename T>
 __device__ __forceinline__ T u_energy_b(const BatchInst &a, uint32_t both)
 {
-    if (a.u_uniform) return (T)a.u_value * (T)__popc(both);
+    if (a.u_uniform) return ((sizeof(T) == 4) ? (T)a.u_value32 : (T)a.u_value) * (T)__popc(both);
+    const T *us = (sizeof(T) == 4) ? reinterpret_cast<const T *>(a.u_site32) : reinterpret_cast<const T *>(a.u_site);
     T e = 0;
     while (both) {
         const int b = __ffs(both) - 1;
-        e += (T)a.u_site[b];
+        e += us[b];
         both &= both - 1;
     }
     return e;
@@ -266,6 +271,8 @@ __global__ void __launch_bounds__(kBatchThreads) batch_hv_kernel(const BatchInst
     const T *ub = u + a.off;
     T *yb = y + a.off + (int64_t)r0 * ld;
     const T *dcf = (sizeof(T) == 4) ? reinterpret_cast<const T *>(a.dcf32) : reinterpret_cast<const T *>(a.dcf64);
+    const T *ued_t = (sizeof(T) == 4) ? reinterpret_cast<const T *>(a.uediag32) : reinterpret_cast<const T *>(a.uediag);
+    const T *ded_t = (sizeof(T) == 4) ? reinterpret_cast<const T *>(a.dediag32) : reinterpret_cast<const T *>(a.dediag);
     for (int r = 0; r < kRows; ++r) {
         const T *src = ub + (int64_t)(r0 + r) * ld;
         for (int c = threadIdx.x; c < nsup; c += blockDim.x) xs[c * S + r] = (r < nr) ? src[c] : (T)0;
@@ -285,7 +292,7 @@ __global__ void __launch_bounds__(kBatchThreads) batch_hv_kernel(const BatchInst
             nb_n[r] = nn;
             nb_e0[r] = e0;
             row_str[r] = (r < nr) ? __ldg(a.dstr + r0 + r) : 0u;
-            row_ed[r] = (r < nr) ? (T)__ldg(a.dediag + r0 + r) : (T)0;
+            row_ed[r] = (r < nr) ? __ldg(ded_t + r0 + r) : (T)0;
         }
     }
     __syncthreads();
@@ -295,7 +302,7 @@ __global__ void __launch_bounds__(kBatchThreads) batch_hv_kernel(const BatchInst
         const bool ok = c < nsup;
         const int cc = ok ? c : nsup - 1;
         const uint32_t su = __ldg(a.ustr + cc);
-        const T ued = (T)__ldg(a.uediag + cc);
+        const T ued = __ldg(ued_t + cc);
         T acc[kRows], xv[kRows];
         load_column(xs + cc * S, xv);
 #pragma unroll
@@ -485,6 +492,7 @@ extern "C" int ed_batch_create(int ninst, ed_sector *const *secs, ed_batch **out
     ED_REQUIRE(ninst >= 1 && secs != nullptr, "need at least one instance");
     std::vector<BatchInst> host((size_t)ninst);
     std::vector<double> usite((size_t)ninst * kMaxSites);
+    std::vector<float> usite32((size_t)ninst * kMaxSites);
     std::vector<int32_t> binst;
     std::vector<int64_t> offsets, dims;
     int64_t off = 0, blk = 0;
@@ -505,13 +513,18 @@ extern "C" int ed_batch_create(int ninst, ed_sector *const *secs, ed_batch **out
         a.uptr = s->up.ptr; a.usrc = s->up.src; a.dptr = s->dn.ptr; a.dsrc = s->dn.src;
         a.ucf32 = s->up.cf32; a.dcf32 = s->dn.cf32; a.ucf64 = s->up.cf64; a.dcf64 = s->dn.cf64;
         a.uediag = s->up.ediag; a.dediag = s->dn.ediag;
+        a.uediag32 = s->up.ediag32; a.dediag32 = s->dn.ediag32;
         a.ell_off = s->up.ell_off; a.ell_src = s->up.ell_src;
         a.ell_cf32 = s->up.ell_cf32; a.ell_cf64 = s->up.ell_cf64;
         a.ell_pk32 = s->up.ell_pk32;
         a.nslice = (int)s->up.nslice;
-        for (int q = 0; q < kMaxSites; ++q) usite[(size_t)i * kMaxSites + q] = s->u_site[q];
+        for (int q = 0; q < kMaxSites; ++q) {
+            usite[(size_t)i * kMaxSites + q] = s->u_site[q];
+            usite32[(size_t)i * kMaxSites + q] = (float)s->u_site[q];
+        }
         a.u_site = nullptr;   // set after the upload below
         a.u_value = s->u_value;
+        a.u_value32 = (float)s->u_value;
         a.u_uniform = s->u_uniform ? 1 : 0;
         a.blk0 = blk;
         a.nblk = (int)((s->nsdn + kRows - 1) / kRows);
@@ -536,6 +549,7 @@ extern "C" int ed_batch_create(int ninst, ed_sector *const *secs, ed_batch **out
     // one allocation per table: creating a batch of thousands of instances costs a few copies
     if (cudaMalloc(&bt->dev, sizeof(BatchInst) * ninst) != cudaSuccess ||
         cudaMalloc(&bt->u_site_all, sizeof(double) * usite.size()) != cudaSuccess ||
+        cudaMalloc(&bt->u_site_all32, sizeof(float) * usite32.size()) != cudaSuccess ||
         (blk > 0 && cudaMalloc(&bt->blk_inst, sizeof(int32_t) * (size_t)blk) != cudaSuccess)) {
         cudaGetLastError();
         set_error("allocation of batch descriptors failed");
@@ -547,9 +561,14 @@ extern "C" int ed_batch_create(int ninst, ed_sector *const *secs, ed_batch **out
         ed_batch_destroy(bt);
         return ED_ERR_CUDA;
     }
-    for (int i = 0; i < ninst; ++i) host[(size_t)i].u_site = bt->u_site_all + (size_t)i * kMaxSites;
+    for (int i = 0; i < ninst; ++i) {
+        host[(size_t)i].u_site = bt->u_site_all + (size_t)i * kMaxSites;
+        host[(size_t)i].u_site32 = bt->u_site_all32 + (size_t)i * kMaxSites;
+    }
     if (cudaMemcpy(bt->dev, host.data(), sizeof(BatchInst) * ninst, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(bt->u_site_all, usite.data(), sizeof(double) * usite.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(bt->u_site_all32, usite32.data(), sizeof(float) * usite32.size(), cudaMemcpyHostToDevice) !=
+            cudaSuccess ||
         (blk > 0 && cudaMemcpy(bt->blk_inst, binst.data(), sizeof(int32_t) * (size_t)blk, cudaMemcpyHostToDevice) !=
                         cudaSuccess)) {
         const cudaError_t e = cudaGetLastError();
@@ -567,6 +586,7 @@ extern "C" int ed_batch_destroy(ed_batch *bt)
     if (bt->dev) cudaFree(bt->dev);
     if (bt->blk_inst) cudaFree(bt->blk_inst);
     if (bt->u_site_all) cudaFree(bt->u_site_all);
+    if (bt->u_site_all32) cudaFree(bt->u_site_all32);
     delete bt;
     return ED_OK;
 }

@@ -61,6 +61,7 @@ struct HopTable {
     float *cf32 = nullptr;     // [nnz]
     double *cf64 = nullptr;    // [nnz]
     double *ediag = nullptr;   // [n]  sum of T(J,J) over occupied J (|T(J,J)| >= tol)
+    float *ediag32 = nullptr;  // [n]  the same, rounded to FP32 (FP32 kernels read it directly)
     // The same table in sliced-ELL form for the row pass: strings in slices of
     // 32; slice s holds width[s] slots, slot-major, so that the 32 lanes of a
     // warp read one slot with one coalesced load.  Padding slots point at the
@@ -105,10 +106,17 @@ struct HeisStruct {
     int32_t *row_m = nullptr, *rowidx = nullptr;    // holes in A per row; [2^nB] row of a pattern or -1
     int64_t *row_off = nullptr;
     double *diagB = nullptr;         // B-B zz energy + constant diagonal per row
+    float *diagA32 = nullptr, *diagB32 = nullptr;   // the two diagonals rounded to FP32
     int32_t *bb_ptr = nullptr, *bb_src = nullptr;   // B-B flips: neighbour rows per row (CSR)
     float *bb_cf32 = nullptr;
     double *bb_cf64 = nullptr;
     int32_t *rows_of_m = nullptr;    // rows grouped by m
+    int2 *aa_pk32 = nullptr;         // A-A flips packed {column, FP32 coefficient bits}
+    bool ab_fast = false;            // at most 32 A-B bonds: bits packed per column / row
+    uint32_t *col_abbits = nullptr;  // per column: its A bits at the A-B bonds
+    uint32_t *row_bbits = nullptr;   // per row: its B bits at the A-B bonds
+    int32_t *ab_rank = nullptr;      // [q][column]: rank after flipping A-B bond q's A bit
+    int64_t ncols = 0;               // columns over all m (the stride of ab_rank)
     int nab = 0;
     int8_t ab_pa[kMaxAB] = {}, ab_pb[kMaxAB] = {};  // A bit, B bit (relative to nA)
     double ab_fjk[kMaxAB] = {}, ab_fkj[kMaxAB] = {}, ab_zz[kMaxAB] = {};

@@ -193,12 +193,38 @@ int heis_struct_build(ed_sector *s)
         set_error("internal: rows cover %lld of %lld states", (long long)expect, (long long)s->nsup);
         return ED_ERR_ARG;
     }
+    // A-B bonds: with at most 32 of them, a column's A bits and a row's B bits at the bonds are
+    // packed into one word each; the bonds where they differ are the antiparallel ones
+    hs->ab_fast = ab.size() <= 32;
+    double ab_zz_sum = 0.0;   // sum of zz/4 over the A-B bonds (every bond taken as "equal")
+    for (int b : ab) ab_zz_sum += 0.25 * ht.zz[b];
+    std::vector<uint32_t> col_abbits, row_bbits;
+    std::vector<int32_t> ab_rank;   // [q][column]: rank of the column's pattern with the bond's A bit flipped
+    if (hs->ab_fast) {
+        ab_rank.resize(ab.size() * col_pat.size());
+        for (size_t q = 0; q < ab.size(); ++q)
+            for (size_t c = 0; c < col_pat.size(); ++c)
+                ab_rank[q * col_pat.size() + c] = rankA[col_pat[c] ^ (1u << (ht.bj[ab[q]] - 1))];
+        hs->ncols = (int64_t)col_pat.size();
+        col_abbits.resize(col_pat.size());
+        for (size_t c = 0; c < col_pat.size(); ++c) {
+            uint32_t w = 0;
+            for (size_t q = 0; q < ab.size(); ++q) w |= ((col_pat[c] >> (ht.bj[ab[q]] - 1)) & 1u) << q;
+            col_abbits[c] = w;
+        }
+        row_bbits.resize((size_t)nrows);
+        for (int64_t r = 0; r < nrows; ++r) {
+            uint32_t w = 0;
+            for (size_t q = 0; q < ab.size(); ++q) w |= ((row_pat[(size_t)r] >> (ht.bk[ab[q]] - 1 - nA)) & 1u) << q;
+            row_bbits[(size_t)r] = w;
+        }
+    }
     // B-B zz energy (+ the constant diagonal) and neighbour rows per row
     std::vector<int32_t> bb_ptr(1, 0), bb_src;
     std::vector<double> bb_cf;
     for (int64_t r = 0; r < nrows; ++r) {
         const uint32_t h = row_pat[(size_t)r];
-        double d = ht.dconst;
+        double d = ht.dconst + (hs->ab_fast ? ab_zz_sum : 0.0);
         for (int b : bb) {
             const int pj = ht.bj[b] - 1 - nA, pk = ht.bk[b] - 1 - nA;
             const uint32_t hj = (h >> pj) & 1u, hk = (h >> pk) & 1u;
@@ -232,13 +258,23 @@ int heis_struct_build(ed_sector *s)
         hs->ab_zz[q] = 0.25 * ht.zz[b];
     }
     std::vector<float> aa_cf32(aa_cf.begin(), aa_cf.end()), bb_cf32(bb_cf.begin(), bb_cf.end());
+    std::vector<float> diagA32(diagA.begin(), diagA.end()), diagB32(diagB.begin(), diagB.end());
+    std::vector<int2> aa_pk32(aa_src.size());
+    for (size_t q = 0; q < aa_src.size(); ++q) {
+        int32_t bits;
+        std::memcpy(&bits, &aa_cf32[q], sizeof(bits));
+        aa_pk32[q] = make_int2(aa_src[q], bits);
+    }
     int rc;
     if ((rc = up(&hs->col_pat, col_pat)) || (rc = up(&hs->rankA, rankA)) || (rc = up(&hs->diagA, diagA)) ||
         (rc = up(&hs->aa_off, aa_off)) || (rc = up(&hs->aa_src, aa_src)) || (rc = up(&hs->aa_cf32, aa_cf32)) ||
         (rc = up(&hs->aa_cf64, aa_cf)) || (rc = up(&hs->row_pat, row_pat)) || (rc = up(&hs->row_m, row_m)) ||
         (rc = up(&hs->row_off, row_off)) || (rc = up(&hs->rowidx, rowidx)) || (rc = up(&hs->diagB, diagB)) ||
         (rc = up(&hs->bb_ptr, bb_ptr)) || (rc = up(&hs->bb_src, bb_src)) || (rc = up(&hs->bb_cf32, bb_cf32)) ||
-        (rc = up(&hs->bb_cf64, bb_cf)) || (rc = up(&hs->rows_of_m, rows_of_m)))
+        (rc = up(&hs->bb_cf64, bb_cf)) || (rc = up(&hs->rows_of_m, rows_of_m)) ||
+        (rc = up(&hs->aa_pk32, aa_pk32)) || (rc = up(&hs->col_abbits, col_abbits)) ||
+        (rc = up(&hs->row_bbits, row_bbits)) || (rc = up(&hs->diagA32, diagA32)) || (rc = up(&hs->ab_rank, ab_rank)) ||
+        (rc = up(&hs->diagB32, diagB32)))
         return rc;
     return ED_OK;
 }
@@ -248,7 +284,8 @@ void heis_struct_free(HeisStruct *hs)
     if (!hs) return;
     void *ptrs[] = {hs->col_pat, hs->rankA, hs->diagA, hs->aa_off, hs->aa_src, hs->aa_cf32,
                     hs->aa_cf64, hs->row_pat, hs->row_m, hs->row_off, hs->rowidx, hs->diagB,
-                    hs->bb_ptr, hs->bb_src, hs->bb_cf32, hs->bb_cf64, hs->rows_of_m};
+                    hs->bb_ptr, hs->bb_src, hs->bb_cf32, hs->bb_cf64, hs->rows_of_m,
+                    hs->aa_pk32, hs->col_abbits, hs->row_bbits, hs->diagA32, hs->diagB32, hs->ab_rank};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete hs;
@@ -263,27 +300,41 @@ struct HsArgs {
     const uint32_t *col_pat, *row_pat;
     const int32_t *rankA, *aa_off, *aa_src, *row_m, *rowidx, *bb_ptr, *bb_src, *rows_of_m;
     const int64_t *row_off;
-    const double *diagA, *diagB;
+    const void *diagA, *diagB;     // float or double, like the vectors
     const void *aa_cf, *bb_cf;     // float or double
+    const int2 *aa_pk32;           // {column, FP32 coefficient bits} of the A-A flips
+    const uint32_t *col_abbits, *row_bbits;
+    const int32_t *ab_rank;        // [q][column] rank after flipping bond q's A bit (packed path)
+    int64_t ncols;
+    int ab_fast;
     int8_t ab_pa[kMaxAB], ab_pb[kMaxAB];
     double ab_fjk[kMaxAB], ab_fkj[kMaxAB], ab_zz[kMaxAB];
     double scale;
 };
 
 constexpr int kHeisRowThreads = 512;
+
+// bytes of the A-B bond facts ahead of the staged row (16-byte aligned)
+__host__ __device__ inline size_t heis_row_head_bytes(int nab, size_t tsize)
+{
+    const size_t b = (size_t)nab * (sizeof(int64_t) + 3 * tsize + sizeof(uint32_t));
+    return (b + 15) / 16 * 16;
+}
 constexpr int64_t kMaxPartialBlocksHeis = 1024;   // the partials that ed_scratch_bytes provides for
 
 // Pass R: y[row] = s * (diag + A-A flips + A-B flips) of every row.
 template <typename T>
-__global__ void __launch_bounds__(kHeisRowThreads) heis_row_kernel(const T *__restrict__ x, T *__restrict__ y,
+__global__ void __launch_bounds__(kHeisRowThreads, 4) heis_row_kernel(const T *__restrict__ x, T *__restrict__ y,
                                                                     const HsArgs a)
 {
+    // dynamic shared memory: per-row A-B bond facts (nab entries each), then the staged row
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *xs = reinterpret_cast<T *>(smem_raw);
-    __shared__ int64_t ab_src[kMaxAB];   // element offset of the bond's source row, -1 if the flip is impossible
-    __shared__ T ab_c[kMaxAB];           // flip element when the A site is in the required state
-    __shared__ uint32_t ab_need[kMaxAB]; // required A bit (1: A site down) for the flip
-    __shared__ T ab_dsame[kMaxAB];       // +-zz/4 when the two sites are equal
+    int64_t *ab_src = reinterpret_cast<int64_t *>(smem_raw);      // source row offset, -1 if impossible
+    T *ab_c = reinterpret_cast<T *>(ab_src + a.nab);               // flip element for the required A state
+    T *ab_dsame = ab_c + a.nab;                                    // zz/4 (generic path)
+    T *ab_w2 = ab_dsame + a.nab;                                   // zz/2: drop of an antiparallel bond
+    uint32_t *ab_need = reinterpret_cast<uint32_t *>(ab_w2 + a.nab);  // required A bit (1: A site down)
+    T *xs = reinterpret_cast<T *>(smem_raw + heis_row_head_bytes(a.nab, sizeof(T)));
     const T *acf = reinterpret_cast<const T *>(a.aa_cf);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = kHeisRowThreads / 32;
     const T sc = (T)a.scale;
@@ -294,7 +345,8 @@ __global__ void __launch_bounds__(kHeisRowThreads) heis_row_kernel(const T *__re
         const int len = (int)a.ncol[m];
         const int64_t cbase = a.col_base[m];
         const int64_t sbase = a.slice_base[m];
-        const T db = (T)__ldg(a.diagB + row);
+        const T db = __ldg(static_cast<const T *>(a.diagB) + row);
+        const uint32_t rbits = a.ab_fast ? __ldg(a.row_bbits + row) : 0u;
         __syncthreads();   // the previous row's readers are done with xs / ab_*
         for (int c = threadIdx.x; c < len; c += blockDim.x) xs[c] = x[off + c];
         for (int q = threadIdx.x; q < a.nab; q += blockDim.x) {
@@ -305,6 +357,7 @@ __global__ void __launch_bounds__(kHeisRowThreads) heis_row_kernel(const T *__re
             ab_need[q] = 1u - hk;
             ab_c[q] = (T)(hk ? a.ab_fkj[q] : a.ab_fjk[q]);   // target hj = 1-hk: hj ? fjk : fkj
             ab_dsame[q] = (T)a.ab_zz[q];
+            ab_w2[q] = (T)(2.0 * a.ab_zz[q]);
         }
         __syncthreads();
         const int nsl = (len + 31) / 32;
@@ -313,14 +366,34 @@ __global__ void __launch_bounds__(kHeisRowThreads) heis_row_kernel(const T *__re
             const bool ok = c < len;
             const int cc = ok ? c : len - 1;
             const uint32_t ha = __ldg(a.col_pat + cbase + cc);
-            T d = (T)__ldg(a.diagA + cbase + cc) + db;
+            T d = __ldg(static_cast<const T *>(a.diagA) + cbase + cc) + db;
             T acc = 0;
             const int s0 = __ldg(a.aa_off + sbase + sl), ns = __ldg(a.aa_off + sbase + sl + 1) - s0;
+            if (sizeof(T) == 4) {
 #pragma unroll 4
-            for (int q = 0; q < ns; ++q) {
-                const int at = (s0 + q) * 32 + lane;
-                acc += __ldg(acf + at) * xs[__ldg(a.aa_src + at)];
+                for (int q = 0; q < ns; ++q) {
+                    const int2 pk = __ldg(a.aa_pk32 + (s0 + q) * 32 + lane);
+                    acc += (T)__int_as_float(pk.y) * xs[pk.x];
+                }
+            } else {
+#pragma unroll 4
+                for (int q = 0; q < ns; ++q) {
+                    const int at = (s0 + q) * 32 + lane;
+                    acc += __ldg(acf + at) * xs[__ldg(a.aa_src + at)];
+                }
             }
+            if (a.ab_fast) {
+                // antiparallel A-B bonds: the set bits of (column's A bits ^ row's B bits); their
+                // zz/4 was counted as "equal" in diagB, so each one drops the diagonal by zz/2
+                uint32_t diff = __ldg(a.col_abbits + cbase + cc) ^ rbits;
+                while (diff) {
+                    const int q = __ffs(diff) - 1;
+                    diff &= diff - 1;
+                    d -= ab_w2[q];
+                    const int64_t src = ab_src[q];
+                    if (src >= 0) acc += ab_c[q] * __ldg(x + src + __ldg(a.ab_rank + q * a.ncols + cbase + cc));
+                }
+            } else
             for (int q = 0; q < a.nab; ++q) {
                 const uint32_t hj = (ha >> a.ab_pa[q]) & 1u;
                 if (hj != ab_need[q]) {
@@ -380,25 +453,35 @@ __global__ void __launch_bounds__(256) heis_slab_kernel(const T *__restrict__ x,
                 my_cf = __ldg(bcf + e0 + eb + lane);
             }
             const bool last = eb + 32 >= nn;
-            for (int64_t cb = c0; cb < c1; cb += 32) {
-                const int64_t c = cb + lane;
-                const bool ok = c < c1;
-                T acc = 0;
-#pragma unroll 4
+            T sxy = 0, syy = 0;
+            // four 32-column chunks per pass: four independent loads per neighbour row
+            for (int64_t cb = c0; cb < c1; cb += 128) {
+                T acc[4] = {0, 0, 0, 0};
+#pragma unroll 2
                 for (int e = 0; e < ne; ++e) {
                     const int64_t so = __shfl_sync(0xffffffffu, my_off, e);
                     const T w = __shfl_sync(0xffffffffu, my_cf, e);
-                    if (ok) acc += w * __ldg(x + so + c);
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const int64_t c = cb + 32 * j + lane;
+                        if (c < c1) acc[j] += w * __ldg(x + so + c);
+                    }
                 }
-                if (ok) {
-                    const T yv = y[off + c] + acc * sc;
-                    y[off + c] = yv;
-                    if (last) {
-                        dxy += (double)x[off + c] * (double)yv;
-                        dyy += (double)yv * (double)yv;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int64_t c = cb + 32 * j + lane;
+                    if (c < c1) {
+                        const T yv = y[off + c] + acc[j] * sc;
+                        y[off + c] = yv;
+                        if (last) {
+                            sxy += x[off + c] * yv;
+                            syy += yv * yv;
+                        }
                     }
                 }
             }
+            dxy += (double)sxy;
+            dyy += (double)syy;
         }
     }
     if (partials) {
@@ -601,8 +684,15 @@ static int heis_struct_run(ed_sector *s, cudaStream_t st, const T *x, T *y, doub
     a.rankA = h.rankA; a.aa_off = h.aa_off; a.aa_src = h.aa_src; a.row_m = h.row_m;
     a.rowidx = h.rowidx; a.bb_ptr = h.bb_ptr; a.bb_src = h.bb_src; a.rows_of_m = h.rows_of_m;
     a.row_off = h.row_off;
-    a.diagA = h.diagA; a.diagB = h.diagB;
+    a.diagA = (sizeof(T) == 4) ? (const void *)h.diagA32 : (const void *)h.diagA;
+    a.diagB = (sizeof(T) == 4) ? (const void *)h.diagB32 : (const void *)h.diagB;
     a.aa_cf = (sizeof(T) == 4) ? (const void *)h.aa_cf32 : (const void *)h.aa_cf64;
+    a.aa_pk32 = h.aa_pk32;
+    a.col_abbits = h.col_abbits;
+    a.row_bbits = h.row_bbits;
+    a.ab_rank = h.ab_rank;
+    a.ncols = h.ncols;
+    a.ab_fast = h.ab_fast ? 1 : 0;
     a.bb_cf = (sizeof(T) == 4) ? (const void *)h.bb_cf32 : (const void *)h.bb_cf64;
     for (int q = 0; q < h.nab; ++q) {
         a.ab_pa[q] = h.ab_pa[q]; a.ab_pb[q] = h.ab_pb[q];
@@ -611,7 +701,7 @@ static int heis_struct_run(ed_sector *s, cudaStream_t st, const T *x, T *y, doub
     a.scale = scale;
     const int nsm = num_sms();
     // ---- pass R
-    const size_t smem = (size_t)std::max<int64_t>(h.max_len, 1) * sizeof(T);
+    const size_t smem = heis_row_head_bytes(h.nab, sizeof(T)) + (size_t)std::max<int64_t>(h.max_len, 1) * sizeof(T);
     ED_CHECK_CUDA(cudaFuncSetAttribute(heis_row_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int64_t blocks = std::min<int64_t>(h.nrows, (int64_t)nsm * 4);
     if (blocks < 1) blocks = 1;

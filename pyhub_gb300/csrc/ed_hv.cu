@@ -16,28 +16,39 @@
 // row/pass structure (rows of B-half patterns over A-half patterns).
 #include "ed_common.cuh"
 
+#include <cstdlib>
+
 namespace ed {
 
 struct HubArgs {
     int64_t nsup, nsdn, ld;
-    const uint32_t *ustr; const int32_t *uptr; const int32_t *usrc; const void *ucf; const double *uediag;
-    const uint32_t *dstr; const int32_t *dptr; const int32_t *dsrc; const void *dcf; const double *dediag;
+    const uint32_t *ustr; const int32_t *uptr; const int32_t *usrc; const void *ucf; const void *uediag;
+    const uint32_t *dstr; const int32_t *dptr; const int32_t *dsrc; const void *dcf; const void *dediag;
     int64_t nslice;
     const int32_t *ell_off; const int32_t *ell_src;
     double u_site[kMaxSites];
+    float u_site32[kMaxSites];
     int u_uniform;
     double u_value;
     double scale;
 };
 
 template <typename T>
-__device__ __forceinline__ T u_energy(const HubArgs &a, uint32_t both)
+__device__ __forceinline__ const T *u_sites(const HubArgs &a)
 {
-    if (a.u_uniform) return (T)a.u_value * (T)__popc(both);
+    return (sizeof(T) == 4) ? reinterpret_cast<const T *>(a.u_site32) : reinterpret_cast<const T *>(a.u_site);
+}
+
+// on-site energy of the doubly occupied bits `both`; uval = U in T (uniform U)
+template <typename T>
+__device__ __forceinline__ T u_energy(const HubArgs &a, uint32_t both, T uval)
+{
+    if (a.u_uniform) return uval * (T)__popc(both);
+    const T *us = u_sites<T>(a);
     T e = 0;
     while (both) {
         int b = __ffs(both) - 1;
-        e += (T)a.u_site[b];
+        e += us[b];
         both &= both - 1;
     }
     return e;
@@ -71,6 +82,8 @@ __global__ void __launch_bounds__(512) hub_row_kernel(const T *__restrict__ x, T
     const T *__restrict__ ecf = static_cast<const T *>(a.ucf);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
     const int64_t nsup = a.nsup, ld = a.ld;
+    const T uval = (T)a.u_value, sc = (T)a.scale;
+    const T *ued_t = static_cast<const T *>(a.uediag), *ded_t = static_cast<const T *>(a.dediag);
     for (int64_t d0 = (int64_t)blockIdx.x * R; d0 < a.nsdn; d0 += (int64_t)gridDim.x * R) {
         const int nr = (int)min((int64_t)R, a.nsdn - d0);
 #pragma unroll
@@ -82,17 +95,17 @@ __global__ void __launch_bounds__(512) hub_row_kernel(const T *__restrict__ x, T
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             sd[r] = (r < nr) ? __ldg(a.dstr + d0 + r) : 0u;
-            ed[r] = (r < nr) ? (T)__ldg(a.dediag + d0 + r) : (T)0;
+            ed[r] = (r < nr) ? __ldg(ded_t + d0 + r) : (T)0;
         }
         for (int64_t sl = warp; sl < a.nslice; sl += nwarps) {
             const int64_t u = sl * 32 + lane;
             const bool ok = u < nsup;
             const int64_t uu = ok ? u : nsup - 1;
             const uint32_t su = __ldg(a.ustr + uu);
-            const T eu = (T)__ldg(a.uediag + uu);
+            const T eu = __ldg(ued_t + uu);
             T acc[R];
 #pragma unroll
-            for (int r = 0; r < R; ++r) acc[r] = (eu + ed[r] + u_energy<T>(a, su & sd[r])) * xs[r * sld + uu];
+            for (int r = 0; r < R; ++r) acc[r] = (eu + ed[r] + u_energy<T>(a, su & sd[r], uval)) * xs[r * sld + uu];
             const int s0 = __ldg(a.ell_off + sl), ns = __ldg(a.ell_off + sl + 1) - s0;
             const int32_t *sp = a.ell_src + (int64_t)s0 * 32 + lane;
             const T *cp = ecf + (int64_t)s0 * 32 + lane;
@@ -116,7 +129,7 @@ __global__ void __launch_bounds__(512) hub_row_kernel(const T *__restrict__ x, T
             if (ok) {
 #pragma unroll
                 for (int r = 0; r < R; ++r)
-                    if (r < nr) y[(d0 + r) * ld + u] = acc[r] * (T)a.scale;
+                    if (r < nr) y[(d0 + r) * ld + u] = acc[r] * sc;
             }
         }
         __syncthreads();
@@ -269,20 +282,38 @@ int launch_reduce(const double *partials, int nblocks, int m, double *out, cudaS
 
 static constexpr int kMaxPartialBlocks = 1024;
 
+// L2 budget of one x slab in the slab pass: 48 MB (a third of the 129 MB
+// L2, leaving room for the y slab in flight and the tables); the
+// environment variable PYHUB_ED_SLAB_L2_BYTES overrides it for tuning.
+static double slab_l2_bytes()
+{
+    static double v = []() {
+        const char *e = std::getenv("PYHUB_ED_SLAB_L2_BYTES");
+        const double d = e ? std::atof(e) : 0.0;
+        return (d >= 1.0e6 && d <= 1.0e9) ? d : 48.0e6;
+    }();
+    return v;
+}
+
 template <typename T>
 static int hub_hv(ed_sector *s, cudaStream_t st, int64_t ld, const T *x, T *y, double scale, double *dots,
                   double *partials)
 {
     HubArgs a;
     a.nsup = s->nsup; a.nsdn = s->nsdn; a.ld = ld;
-    a.ustr = s->up.str; a.uptr = s->up.ptr; a.usrc = s->up.src; a.uediag = s->up.ediag;
-    a.dstr = s->dn.str; a.dptr = s->dn.ptr; a.dsrc = s->dn.src; a.dediag = s->dn.ediag;
+    a.ustr = s->up.str; a.uptr = s->up.ptr; a.usrc = s->up.src;
+    a.dstr = s->dn.str; a.dptr = s->dn.ptr; a.dsrc = s->dn.src;
+    a.uediag = (sizeof(T) == 4) ? (const void *)s->up.ediag32 : (const void *)s->up.ediag;
+    a.dediag = (sizeof(T) == 4) ? (const void *)s->dn.ediag32 : (const void *)s->dn.ediag;
     if (sizeof(T) == 4) { a.ucf = s->up.ell_cf32; a.dcf = s->dn.cf32; }
     else { a.ucf = s->up.ell_cf64; a.dcf = s->dn.cf64; }
     a.nslice = s->up.nslice;
     a.ell_off = s->up.ell_off;
     a.ell_src = s->up.ell_src;
-    for (int b = 0; b < kMaxSites; ++b) a.u_site[b] = s->u_site[b];
+    for (int b = 0; b < kMaxSites; ++b) {
+        a.u_site[b] = s->u_site[b];
+        a.u_site32[b] = (float)s->u_site[b];
+    }
     a.u_uniform = s->u_uniform ? 1 : 0;
     a.u_value = s->u_value;
     a.scale = scale;
@@ -324,8 +355,8 @@ static int hub_hv(ed_sector *s, cudaStream_t st, int64_t ld, const T *x, T *y, d
     }
     ED_CHECK_LAUNCH();
     // ---- pass 2
-    // slab width: the x slab (nsdn rows x width) should take at most ~48 MB of L2
-    int64_t slab_w = (int64_t)(48.0e6 / ((double)s->nsdn * sizeof(T)));
+    // slab width: the x slab (nsdn rows x width) should take at most slab_l2_bytes() of L2
+    int64_t slab_w = (int64_t)(slab_l2_bytes() / ((double)s->nsdn * sizeof(T)));
     slab_w = slab_w / 256 * 256;
     if (slab_w < 256) slab_w = 256;
     if (slab_w > s->nsup) slab_w = (s->nsup + VWS - 1) / VWS * VWS;

@@ -208,48 +208,60 @@ static int upload_ell(const HostHop &h, HopTable &d)
     const int64_t slots = off[(size_t)ns];
     std::vector<int32_t> src((size_t)std::max<int64_t>(slots * 32, 1));
     std::vector<double> c64((size_t)std::max<int64_t>(slots * 32, 1), 0.0);
-    // Slot order within a lane is free.  The batched kernel gathers 16-byte
-    // column pieces for 8 lanes at a time (one quarter warp), and a column's
-    // bank group is (source string mod 8); so each quarter's lanes take, slot
-    // by slot, neighbours of pairwise different groups where they can (greedy,
-    // lanes with the most neighbours left first).  Padding slots read the
-    // lane's own string (consecutive strings: distinct groups) with weight 0.
+    // Slot order within a lane is free, so each slot is filled to spread the
+    // 32 lanes' sources over the shared-memory banks of the kernels that
+    // gather them:
+    //   * the batched kernel gathers 16-byte column pieces for 8 lanes at a
+    //     time (one quarter warp); a column's bank group is (source mod 8);
+    //   * the row kernels gather one 4- or 8-byte word per lane from a staged
+    //     row; its bank is (source mod 32) for FP32.
+    // Greedy per slot, lanes with the most neighbours left first: prefer a
+    // neighbour whose (source mod 32) no lane of the warp and whose
+    // (source mod 8) no lane of the quarter uses yet, then one that is new
+    // for the quarter only, then one new for the warp only.  Padding slots
+    // read the lane's own string (consecutive strings: distinct banks) with
+    // weight 0.
     for (int64_t sl = 0; sl < ns; ++sl) {
         const int64_t w = off[(size_t)sl + 1] - off[(size_t)sl];
-        for (int qw = 0; qw < 4; ++qw) {
-            std::vector<std::vector<int32_t>> left(8);   // remaining neighbour entries (hop-table positions)
-            for (int l = 0; l < 8; ++l) {
-                const int64_t u = sl * 32 + qw * 8 + l;
-                if (u >= n) continue;
-                for (int32_t e = h.ptr[(size_t)u]; e < h.ptr[(size_t)u + 1]; ++e) left[(size_t)l].push_back(e);
-            }
-            for (int64_t k = 0; k < w; ++k) {
-                bool used[8] = {false, false, false, false, false, false, false, false};
-                int order[8] = {0, 1, 2, 3, 4, 5, 6, 7};
-                std::stable_sort(order, order + 8, [&](int x, int y) { return left[(size_t)x].size() > left[(size_t)y].size(); });
-                for (int oi = 0; oi < 8; ++oi) {
-                    const int l = order[oi];
-                    const int64_t u = sl * 32 + qw * 8 + l;
-                    const size_t at = (size_t)((off[(size_t)sl] + k) * 32 + qw * 8 + l);
-                    const int64_t uu = u < n ? u : n - 1;
-                    std::vector<int32_t> &L = left[(size_t)l];
-                    const bool must = (int64_t)L.size() >= w - k;   // no spare slot left for this lane
-                    int pick = -1;
-                    for (size_t j = 0; j < L.size(); ++j)
-                        if (!used[h.src[(size_t)L[j]] & 7]) { pick = (int)j; break; }
-                    if (pick < 0 && must) pick = 0;
-                    if (pick < 0 && !L.empty() && used[uu & 7]) pick = 0;   // padding would conflict too
-                    if (pick >= 0) {
-                        const int32_t e = L[(size_t)pick];
-                        L.erase(L.begin() + pick);
-                        src[at] = h.src[(size_t)e];
-                        c64[at] = h.coef[(size_t)e];
-                    } else {
-                        src[at] = (int32_t)uu;
-                        c64[at] = 0.0;
-                    }
-                    used[src[at] & 7] = true;
+        std::vector<std::vector<int32_t>> left(32);   // remaining neighbour entries (hop-table positions)
+        for (int l = 0; l < 32; ++l) {
+            const int64_t u = sl * 32 + l;
+            if (u >= n) continue;
+            for (int32_t e = h.ptr[(size_t)u]; e < h.ptr[(size_t)u + 1]; ++e) left[(size_t)l].push_back(e);
+        }
+        for (int64_t k = 0; k < w; ++k) {
+            bool used32[32] = {};
+            bool used8[4][8] = {};
+            int order[32];
+            for (int l = 0; l < 32; ++l) order[l] = l;
+            std::stable_sort(order, order + 32, [&](int x, int y) { return left[(size_t)x].size() > left[(size_t)y].size(); });
+            for (int oi = 0; oi < 32; ++oi) {
+                const int l = order[oi], qw = l >> 3;
+                const int64_t u = sl * 32 + l;
+                const size_t at = (size_t)((off[(size_t)sl] + k) * 32 + l);
+                const int64_t uu = u < n ? u : n - 1;
+                std::vector<int32_t> &L = left[(size_t)l];
+                const bool must = (int64_t)L.size() >= w - k;   // no spare slot left for this lane
+                int pick = -1, best = -1;
+                for (size_t j = 0; j < L.size(); ++j) {
+                    const int32_t sj = h.src[(size_t)L[j]];
+                    const int score = (used8[qw][sj & 7] ? 0 : 2) + (used32[sj & 31] ? 0 : 1);
+                    if (score > best) { best = score; pick = (int)j; }
+                    if (score == 3) break;
                 }
+                const int pad_score = (used8[qw][uu & 7] ? 0 : 2) + (used32[uu & 31] ? 0 : 1);
+                if (pick >= 0 && !must && best < pad_score) pick = -1;   // padding now is the cleaner choice
+                if (pick >= 0) {
+                    const int32_t e = L[(size_t)pick];
+                    L.erase(L.begin() + pick);
+                    src[at] = h.src[(size_t)e];
+                    c64[at] = h.coef[(size_t)e];
+                } else {
+                    src[at] = (int32_t)uu;
+                    c64[at] = 0.0;
+                }
+                used8[qw][src[at] & 7] = true;
+                used32[src[at] & 31] = true;
             }
         }
     }
@@ -285,6 +297,8 @@ static int upload_hop(const HostHop &h, int norb, int ne, HopTable &d)
     if ((rc = upload(&d.cf32, c32.data(), c32.size()))) return rc;
     if ((rc = upload(&d.cf64, h.coef.data(), h.coef.size()))) return rc;
     if ((rc = upload(&d.ediag, h.ediag.data(), h.ediag.size()))) return rc;
+    std::vector<float> e32(h.ediag.begin(), h.ediag.end());
+    if ((rc = upload(&d.ediag32, e32.data(), e32.size()))) return rc;
     if ((rc = upload_ell(h, d))) return rc;
     d.owner = true;
     return ED_OK;
@@ -294,7 +308,7 @@ static void free_hop(HopTable &d)
 {
     if (!d.owner) { d = HopTable(); return; }
     cudaFree(d.str); cudaFree(d.ptr); cudaFree(d.src);
-    cudaFree(d.cf32); cudaFree(d.cf64); cudaFree(d.ediag);
+    cudaFree(d.cf32); cudaFree(d.cf64); cudaFree(d.ediag); cudaFree(d.ediag32);
     cudaFree(d.ell_off); cudaFree(d.ell_src); cudaFree(d.ell_cf32); cudaFree(d.ell_cf64);
     cudaFree(d.ell_pk32);
     d = HopTable();
