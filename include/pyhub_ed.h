@@ -150,6 +150,13 @@ int ed_gf_start(const ed_sector *src, const ed_sector *dst, void *stream, int ki
  * (the engine's internal row stride). */
 typedef struct ed_batch ed_batch;
 int ed_batch_create(int ninst, ed_sector *const *secs, ed_batch **out);
+/* ed_batch_create with the H*v work split chosen by the caller: rows of one
+ * instance per CTA, 4, 8 (the default of ed_batch_create) or 16.  More rows
+ * share each hop-table load among more rows but take more shared memory per
+ * CTA; pyhub_gb300 times the three on the actual batch and keeps the fastest.
+ * No reference counterpart (a launch parameter of this engine). */
+int ed_batch_create_rows(int ninst, ed_sector *const *secs, int rows, ed_batch **out);
+int ed_batch_rows(const ed_batch *b);
 int ed_batch_destroy(ed_batch *b);
 /* total elements of one concatenated vector, per-instance offsets and sizes
  * (nsdn_i*ld_i), and the CTA count of one step (scratch sizing). */

@@ -44,6 +44,8 @@ _SIGS = {
     "ed_batch_scratch_bytes": (_I64, [_P]),
     "ed_batch_lanczos": (_I, [_P, _P, _I, _P, _P, _I, _P, _P, _P, _I64]),
     "ed_batch_ritz": (_I, [_P, _P, _I, _P, _P, _I, _P, _P, _P, _P, _P, _I64]),
+    "ed_batch_create_rows": (_I, [_I, _P, _I, ctypes.POINTER(_P)]),
+    "ed_batch_rows": (_I, [_P]),
 }
 
 GF_KINDS = {"h_up": 0, "h_down": 1, "e_up": 2, "e_down": 3}
@@ -242,11 +244,14 @@ class Sector:
 class Batch:
     """ed_batch: independent three-term Lanczos runs on their own sectors."""
 
-    def __init__(self, sectors):
+    ROWS = (4, 8, 16)
+
+    def __init__(self, sectors, rows: int = 8):
         self.sectors = list(sectors)
         arr = (_P * len(self.sectors))(*[s.handle.value for s in self.sectors])
         h = _P()
-        check("ed_batch_create", lib().ed_batch_create(len(self.sectors), arr, ctypes.byref(h)))
+        check("ed_batch_create_rows", lib().ed_batch_create_rows(len(self.sectors), arr, int(rows), ctypes.byref(h)))
+        self.rows = int(lib().ed_batch_rows(h))
         self._h = h
         tot, nb = _I64(), _I64()
         off = np.zeros(len(self.sectors), dtype=np.int64)

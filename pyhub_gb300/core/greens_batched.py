@@ -28,14 +28,55 @@ def _torch():
     return torch
 
 
-class BatchedLanczos:
-    """Fixed-length three-term Lanczos of many instances in one enqueue."""
+_TUNED = {}   # (dtype, sector shapes) -> rows per CTA chosen by autotune()
 
-    def __init__(self, sectors, nsteps: int, dtype=None, device="cuda"):
+
+def autotune(sectors, dtype, steps: int = 3, sample: int = 192, device="cuda"):
+    """Rows per CTA of the batched H*v for this set of sectors: each candidate
+    (4, 8, 16) runs `steps` Lanczos steps (CUDA events on the current stream,
+    after one untimed run) on an evenly spaced sample of at most `sample`
+    instances, which keeps the batch's mix of sector shapes; the fastest is
+    kept and remembered for batches of the same shapes and dtype."""
+    torch = _torch()
+    key = (str(dtype), tuple(sorted((s.nsup, s.nsdn) for s in sectors)))
+    if key in _TUNED:
+        return _TUNED[key]
+    pick = [sectors[int(j)] for j in np.linspace(0, len(sectors) - 1, min(sample, len(sectors)))]
+    times = {}
+    for rows in _capi.Batch.ROWS:
+        b = _capi.Batch(pick, rows=rows)
+        work = torch.zeros(3 * b.total, dtype=dtype, device=device)
+        x0 = torch.rand(b.total, dtype=dtype, device=device)
+        n = len(b.sectors)
+        alpha = torch.zeros((n, steps), dtype=torch.float64, device=device)
+        beta = torch.zeros((n, steps + 1), dtype=torch.float64, device=device)
+        scratch = torch.empty(b.scratch_bytes() // 8 + 1, dtype=torch.float64, device=device)
+        b.lanczos(work, x0, steps, alpha, beta, scratch)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        b.lanczos(work, x0, steps, alpha, beta, scratch)
+        e1.record()
+        torch.cuda.synchronize()
+        times[rows] = e0.elapsed_time(e1)
+        del b, work, x0, scratch
+    best = min(times, key=times.get)
+    _TUNED[key] = best
+    return best
+
+
+class BatchedLanczos:
+    """Fixed-length three-term Lanczos of many instances in one enqueue.
+    rows: rows of one instance per CTA of the H*v (4, 8 or 16), or "auto"
+    to let autotune() pick it on this batch."""
+
+    def __init__(self, sectors, nsteps: int, dtype=None, device="cuda", rows=8):
         torch = _torch()
         self.dtype = dtype or torch.float32
         self.nsteps = int(nsteps)
-        self.batch = _capi.Batch(sectors)
+        if rows == "auto":
+            rows = autotune(sectors, self.dtype, device=device)
+        self.batch = _capi.Batch(sectors, rows=rows)
+        self.rows = self.batch.rows
         self.sectors = list(sectors)
         n = len(self.sectors)
         tot = self.batch.total
@@ -252,7 +293,7 @@ def c4_clusters(n: int = 256, seed: int = 0):
 
 
 def sweep(clusters, nsteps: int = 150, chunk: int = 64, dtype=None, gs_steps: int = 120, gs_tol: float = 1e-10,
-          omega=None, eta: float = 0.05, graph: bool = True, timings: dict = None):
+          omega=None, eta: float = 0.05, graph: bool = True, timings: dict = None, rows="auto"):
     """Ground states (batched over the clusters of a chunk), then G_ii^s(w)
     of every cluster from its 4*norb particle/hole start vectors by
     continued fractions (batched over all start vectors of the chunk).
@@ -266,6 +307,7 @@ def sweep(clusters, nsteps: int = 150, chunk: int = 64, dtype=None, gs_steps: in
     t_gs = t_start = t_lz = t_cf = 0.0
     n_inst = 0
     restarts = 0
+    rows_used = []
     for c0 in range(0, len(clusters), chunk):
         cl = clusters[c0:c0 + chunk]
         secs, inst, srcs = [], [], []
@@ -292,7 +334,8 @@ def sweep(clusters, nsteps: int = 150, chunk: int = 64, dtype=None, gs_steps: in
         restarts = max(restarts, gsb.restarts)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        bl = BatchedLanczos(secs, nsteps, dtype=dtype)
+        bl = BatchedLanczos(secs, nsteps, dtype=dtype, rows=rows)
+        rows_used.append(bl.rows)
         for i, (ci, spin, part, site) in enumerate(inst):
             kind = ("e_" if part == "greater" else "h_") + spin
             _capi.gf_start(srcs[ci], secs[i], kind, site, gsb.psi[ci], bl.start(i))
@@ -324,7 +367,8 @@ def sweep(clusters, nsteps: int = 150, chunk: int = 64, dtype=None, gs_steps: in
         del bl, secs, srcs, gsb
         torch.cuda.empty_cache()
     timings.update({"ground_states_s": t_gs, "start_vectors_s": t_start, "lanczos_s": t_lz, "cf_eval_s": t_cf,
-                    "instances": n_inst, "total_s": t_gs + t_start + t_lz + t_cf, "gs_restarts": restarts})
+                    "instances": n_inst, "total_s": t_gs + t_start + t_lz + t_cf, "gs_restarts": restarts,
+                    "rows_per_cta": rows_used})
     return results
 
 

@@ -15,7 +15,7 @@
 // captured in a CUDA graph.  alpha/beta are written per instance and step
 // for the continued fraction <phi|(z-H)^-1|phi> = beta_0^2/(z-a_0-b_1^2/...).
 //
-// Sectors here are small (D ~ 1e5..1e6): each CTA stages kRows rows of u_k in
+// Sectors here are small (D ~ 1e5..1e6): each CTA stages R rows of u_k in
 // shared memory for the up hops and reads the neighbour rows of the down
 // hops straight from L2, where the instances in flight keep their vectors.
 #include "ed_common.cuh"
@@ -26,7 +26,7 @@
 
 namespace ed {
 
-constexpr int kRows = 8;          // rows of one instance per CTA
+constexpr int kDefaultRows = 8;   // rows of one instance per CTA (4, 8 or 16; chosen per batch)
 constexpr int kBatchThreads = 256;
 
 struct BatchInst {
@@ -49,6 +49,7 @@ struct BatchInst {
     int u_uniform;
     int64_t blk0;                     // first CTA of this instance
     int nblk;
+    int rows;                         // rows per CTA of the batch
 };
 
 }  // namespace ed
@@ -64,6 +65,7 @@ struct ed_batch {
     std::vector<int64_t> offsets, dims;
     int max_nsup = 0;
     int max_ld = 0;
+    int rows = 8;                      // rows per CTA (4, 8 or 16)
 };
 
 namespace ed {
@@ -114,8 +116,8 @@ __global__ void __launch_bounds__(kBatchThreads) batch_norm_kernel(const BatchIn
 {
     const int64_t b = blockIdx.x;
     const BatchInst &a = inst[__ldg(blk_inst + b)];
-    const int64_t r0 = (b - a.blk0) * kRows;
-    const int nr = (int)min((int64_t)kRows, a.nsdn - r0);
+    const int64_t r0 = (b - a.blk0) * a.rows;
+    const int nr = (int)min((int64_t)a.rows, a.nsdn - r0);
     double s = 0.0;
     for (int r = 0; r < nr; ++r) {
         const T *row = x + a.off + (r0 + r) * a.ld;
@@ -173,17 +175,22 @@ template <typename T> struct alignas(sizeof(T) == 4 ? 8 : 16) NbEnt {
     T cf;
 };
 
-// Column c of the staged block: rows 0..kRows-1 of string c, padded to a
-// 16-byte multiple that spreads consecutive columns over all bank groups
-// (48 B for FP32, 80 B for FP64).
-template <typename T> __host__ __device__ constexpr int staged_stride() { return kRows + 16 / (int)sizeof(T); }
+// Column c of the staged block: rows 0..R-1 of string c.  The column stride
+// in 16-byte units is made odd (padding by 16 bytes when R rows fill an even
+// number), so that column c starts in bank group (odd * c) mod 8: 8
+// consecutive or otherwise distinct-mod-8 columns hit 8 different groups.
+// FP32: 16, 48, 80 bytes for R = 4, 8, 16; FP64: 48, 80, 144 bytes.
+template <typename T, int R> __host__ __device__ constexpr int staged_stride()
+{
+    return ((R * (int)sizeof(T) / 16) % 2 == 0) ? R + 16 / (int)sizeof(T) : R;
+}
 
-template <typename T>
-__device__ __forceinline__ void load_column(const T *p, T (&v)[kRows])
+template <typename T, int R>
+__device__ __forceinline__ void load_column(const T *p, T (&v)[R])
 {
     using V = typename V16<T>::type;
 #pragma unroll
-    for (int q = 0; q < kRows / V16<T>::n; ++q) {
+    for (int q = 0; q < R / V16<T>::n; ++q) {
         const V w = reinterpret_cast<const V *>(p)[q];
 #pragma unroll
         for (int k = 0; k < V16<T>::n; ++k) v[q * V16<T>::n + k] = reinterpret_cast<const T *>(&w)[k];
@@ -192,10 +199,10 @@ __device__ __forceinline__ void load_column(const T *p, T (&v)[kRows])
 
 // G up-hop slots of one lane (table entries at `at`, `at`+32, ...): the G
 // table loads are issued before the first gather.
-template <typename T, int G>
-__device__ __forceinline__ void up_group(const BatchInst &a, const T *xs, int at, T (&acc)[kRows])
+template <typename T, int G, int R>
+__device__ __forceinline__ void up_group(const BatchInst &a, const T *xs, int at, T (&acc)[R])
 {
-    constexpr int S = staged_stride<T>();
+    constexpr int S = staged_stride<T, R>();
     int src[G];
     T w[G];
 #pragma unroll
@@ -211,10 +218,10 @@ __device__ __forceinline__ void up_group(const BatchInst &a, const T *xs, int at
     }
 #pragma unroll
     for (int j = 0; j < G; ++j) {
-        T xv[kRows];
-        load_column(xs + src[j] * S, xv);
+        T xv[R];
+        load_column<T, R>(xs + src[j] * S, xv);
 #pragma unroll
-        for (int r = 0; r < kRows; ++r) acc[r] += w[j] * xv[r];
+        for (int r = 0; r < R; ++r) acc[r] += w[j] * xv[r];
     }
 }
 
@@ -238,14 +245,14 @@ __device__ __forceinline__ void down_group(const NbEnt<T> *en, const T *__restri
         for (int k = 0; k < V16<T>::n; ++k) vat(acc, k) += cf[j] * reinterpret_cast<const T *>(&xn[j])[k];
 }
 
-// y = s_k H u_k and partial <u_k, y> over kRows rows of one instance.
+// y = s_k H u_k and partial <u_k, y> over R rows of one instance.
 // Phase A (diagonal + up hops): the rows are staged in shared memory one
 // column per string; a warp owns 32-string slices, loads each sliced-ELL
 // slot once and applies it to all rows with 16-byte shared loads; the sums
 // go to y.  Phase B (down hops): each row adds its neighbour rows as
 // 16-byte-vector axpys read from L2 (the instances in flight keep their
 // vectors there), then scales, stores and forms the dot product.
-template <typename T>
+template <typename T, int R>
 __global__ void __launch_bounds__(kBatchThreads) batch_hv_kernel(const BatchInst *__restrict__ inst,
                                                                  const int32_t *__restrict__ blk_inst,
                                                                  const T *__restrict__ u, T *__restrict__ y,
@@ -254,31 +261,30 @@ __global__ void __launch_bounds__(kBatchThreads) batch_hv_kernel(const BatchInst
 {
     using V = typename V16<T>::type;
     constexpr int VN = V16<T>::n;
-    constexpr int S = staged_stride<T>();
+    constexpr int S = staged_stride<T, R>();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *xs = reinterpret_cast<T *>(smem_raw);   // [nsup][S]
-    __shared__ NbEnt<T> nb[kRows][kMaxNb];
-    __shared__ int nb_n[kRows], nb_e0[kRows];
-    __shared__ uint32_t row_str[kRows];
-    __shared__ T row_ed[kRows];
+    __shared__ NbEnt<T> nb[R][kMaxNb];
+    __shared__ int nb_n[R], nb_e0[R];
+    __shared__ uint32_t row_str[R];
+    __shared__ T row_ed[R];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = kBatchThreads / 32;
     const int64_t b = blockIdx.x;
     const int i = __ldg(blk_inst + b);
     const BatchInst &a = inst[i];
-    const int r0 = (int)((b - a.blk0) * kRows);
-    const int nr = (int)min((int64_t)kRows, a.nsdn - r0);
+    const int r0 = (int)((b - a.blk0) * R);
+    const int nr = (int)min((int64_t)R, a.nsdn - r0);
     const int nsup = (int)a.nsup, ld = (int)a.ld;
     const T *ub = u + a.off;
     T *yb = y + a.off + (int64_t)r0 * ld;
     const T *dcf = (sizeof(T) == 4) ? reinterpret_cast<const T *>(a.dcf32) : reinterpret_cast<const T *>(a.dcf64);
     const T *ued_t = (sizeof(T) == 4) ? reinterpret_cast<const T *>(a.uediag32) : reinterpret_cast<const T *>(a.uediag);
     const T *ded_t = (sizeof(T) == 4) ? reinterpret_cast<const T *>(a.dediag32) : reinterpret_cast<const T *>(a.dediag);
-    for (int r = 0; r < kRows; ++r) {
+    for (int r = 0; r < R; ++r) {
         const T *src = ub + (int64_t)(r0 + r) * ld;
         for (int c = threadIdx.x; c < nsup; c += blockDim.x) xs[c * S + r] = (r < nr) ? src[c] : (T)0;
     }
-    if (warp < kRows) {
-        const int r = warp;
+    for (int r = warp; r < R; r += nwarps) {
         int e0 = 0, nn = 0;
         if (r < nr) {
             e0 = __ldg(a.dptr + r0 + r);
@@ -303,23 +309,23 @@ __global__ void __launch_bounds__(kBatchThreads) batch_hv_kernel(const BatchInst
         const int cc = ok ? c : nsup - 1;
         const uint32_t su = __ldg(a.ustr + cc);
         const T ued = __ldg(ued_t + cc);
-        T acc[kRows], xv[kRows];
-        load_column(xs + cc * S, xv);
+        T acc[R], xv[R];
+        load_column<T, R>(xs + cc * S, xv);
 #pragma unroll
-        for (int r = 0; r < kRows; ++r) acc[r] = (ued + row_ed[r] + u_energy_b<T>(a, su & row_str[r])) * xv[r];
+        for (int r = 0; r < R; ++r) acc[r] = (ued + row_ed[r] + u_energy_b<T>(a, su & row_str[r])) * xv[r];
         const int s0 = __ldg(a.ell_off + sl), ns = __ldg(a.ell_off + sl + 1) - s0;
         // slots in groups: all table loads of a group are in flight before
         // its first gather
         int q = 0;
-        for (; q + 8 <= ns; q += 8) up_group<T, 8>(a, xs, (s0 + q) * 32 + lane, acc);
+        for (; q + 8 <= ns; q += 8) up_group<T, 8, R>(a, xs, (s0 + q) * 32 + lane, acc);
         if (q + 4 <= ns) {
-            up_group<T, 4>(a, xs, (s0 + q) * 32 + lane, acc);
+            up_group<T, 4, R>(a, xs, (s0 + q) * 32 + lane, acc);
             q += 4;
         }
-        for (; q < ns; ++q) up_group<T, 1>(a, xs, (s0 + q) * 32 + lane, acc);
+        for (; q < ns; ++q) up_group<T, 1, R>(a, xs, (s0 + q) * 32 + lane, acc);
         if (ok) {
 #pragma unroll
-            for (int r = 0; r < kRows; ++r)
+            for (int r = 0; r < R; ++r)
                 if (r < nr) yb[r * ld + c] = acc[r];
         }
     }
@@ -381,8 +387,8 @@ __global__ void __launch_bounds__(kBatchThreads) batch_update_kernel(const Batch
     const double *sc = scal + (int64_t)i * kScal;
     const T cc = (T)sc[kCCur], cp = (T)sc[kCPrev];
     const T cr = ritz_coef ? (T)(ritz_coef[(int64_t)i * nsteps + k] * sc[kS]) : (T)0;
-    const int64_t r0 = (b - a.blk0) * kRows;
-    const int nr = (int)min((int64_t)kRows, a.nsdn - r0);
+    const int64_t r0 = (b - a.blk0) * a.rows;
+    const int nr = (int)min((int64_t)a.rows, a.nsdn - r0);
     const int64_t base = a.off + r0 * a.ld;
     const int nv = nr * (int)(a.ld / VN);
     const V *yv = reinterpret_cast<const V *>(y + base);
@@ -412,7 +418,7 @@ __global__ void __launch_bounds__(kBatchThreads) batch_update_kernel(const Batch
     block_partial((double)sp, part_nrm + b);
 }
 
-template <typename T>
+template <typename T, int R>
 static int run_batch(ed_batch *bt, cudaStream_t st, T *work, const T *x0, int nsteps, double *alpha, double *beta,
                      double *scratch, const double *ritz_coef, T *ritz_out)
 {
@@ -420,7 +426,7 @@ static int run_batch(ed_batch *bt, cudaStream_t st, T *work, const T *x0, int ns
     T *U[2] = {work, work + tot};
     T *Y = work + 2 * tot;
     double *pa = scratch, *pb = scratch + bt->nblocks, *scal = scratch + 2 * bt->nblocks;
-    const size_t smem = (size_t)bt->max_ld * staged_stride<T>() * sizeof(T);
+    const size_t smem = (size_t)bt->max_ld * staged_stride<T, R>() * sizeof(T);
     const unsigned nb = (unsigned)bt->nblocks;
     const unsigned ns = (unsigned)((bt->ninst * 32 + 255) / 256);
     // u_{k+1} overwrites u_{k-1} in place, so u_k lives in slot k % 2
@@ -435,7 +441,7 @@ static int run_batch(ed_batch *bt, cudaStream_t st, T *work, const T *x0, int ns
     for (int k = 0; k < nsteps; ++k) {
         T *uk = U[k % 2], *uprev = U[(k + 1) % 2];
         if (nb > 0) {
-            batch_hv_kernel<T><<<nb, kBatchThreads, smem, st>>>(bt->dev, bt->blk_inst, uk, Y, scal, pa);
+            batch_hv_kernel<T, R><<<nb, kBatchThreads, smem, st>>>(bt->dev, bt->blk_inst, uk, Y, scal, pa);
             ED_CHECK_LAUNCH();
         }
         batch_scalar_kernel<<<ns, 256, 0, st>>>(bt->dev, bt->ninst, pa, scal, alpha, beta, k, nsteps, 1);
@@ -455,41 +461,54 @@ static int run_batch(ed_batch *bt, cudaStream_t st, T *work, const T *x0, int ns
 
 using namespace ed;
 
-static size_t hv_smem_bytes(int dtype, int64_t ld)
+static int rows_index(int rows) { return rows == 4 ? 0 : (rows == 8 ? 1 : 2); }
+
+static size_t hv_smem_bytes(int dtype, int64_t ld, int rows)
 {
-    return (dtype == ED_F32) ? (size_t)ld * staged_stride<float>() * sizeof(float)
-                             : (size_t)ld * staged_stride<double>() * sizeof(double);
+    static const int s32[3] = {staged_stride<float, 4>(), staged_stride<float, 8>(), staged_stride<float, 16>()};
+    static const int s64[3] = {staged_stride<double, 4>(), staged_stride<double, 8>(), staged_stride<double, 16>()};
+    const int k = rows_index(rows);
+    return (dtype == ED_F32) ? (size_t)ld * s32[k] * sizeof(float) : (size_t)ld * s64[k] * sizeof(double);
+}
+
+template <typename T, int R>
+static cudaError_t set_hv_smem(size_t bytes)
+{
+    return cudaFuncSetAttribute(batch_hv_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
 // Dynamic shared memory of the H*v kernels: raised once to the largest need
 // (at batch creation, so a later launch inside a stream capture only launches).
 static std::mutex g_smem_mu;
-static size_t g_smem_set[2] = {0, 0};
+static size_t g_smem_set[2][3] = {};
 
-static int ensure_hv_smem(int dtype, size_t bytes)
+static int ensure_hv_smem(int dtype, int rows, size_t bytes)
 {
     std::lock_guard<std::mutex> lk(g_smem_mu);
-    const int k = (dtype == ED_F32) ? 0 : 1;
-    if (bytes <= g_smem_set[k]) return ED_OK;
-    const cudaError_t e = (dtype == ED_F32)
-                              ? cudaFuncSetAttribute(batch_hv_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                     (int)bytes)
-                              : cudaFuncSetAttribute(batch_hv_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                     (int)bytes);
+    const int k = (dtype == ED_F32) ? 0 : 1, r = rows_index(rows);
+    if (bytes <= g_smem_set[k][r]) return ED_OK;
+    cudaError_t e;
+    if (dtype == ED_F32)
+        e = (rows == 4) ? set_hv_smem<float, 4>(bytes) : (rows == 8) ? set_hv_smem<float, 8>(bytes)
+                                                                     : set_hv_smem<float, 16>(bytes);
+    else
+        e = (rows == 4) ? set_hv_smem<double, 4>(bytes) : (rows == 8) ? set_hv_smem<double, 8>(bytes)
+                                                                      : set_hv_smem<double, 16>(bytes);
     if (e != cudaSuccess) {
         set_error("cudaFuncSetAttribute: %s", cudaGetErrorString(e));
         return ED_ERR_CUDA;
     }
-    g_smem_set[k] = bytes;
+    g_smem_set[k][r] = bytes;
     return ED_OK;
 }
 
-extern "C" int ed_batch_create(int ninst, ed_sector *const *secs, ed_batch **out)
+extern "C" int ed_batch_create_rows(int ninst, ed_sector *const *secs, int rows, ed_batch **out)
 {
     clear_error();
     ED_REQUIRE(out != nullptr, "out is NULL");
     *out = nullptr;
     ED_REQUIRE(ninst >= 1 && secs != nullptr, "need at least one instance");
+    ED_REQUIRE(rows == 4 || rows == 8 || rows == 16, "rows per CTA must be 4, 8 or 16, got %d", rows);
     std::vector<BatchInst> host((size_t)ninst);
     std::vector<double> usite((size_t)ninst * kMaxSites);
     std::vector<float> usite32((size_t)ninst * kMaxSites);
@@ -501,7 +520,7 @@ extern "C" int ed_batch_create(int ninst, ed_sector *const *secs, ed_batch **out
         const ed_sector *s = secs[i];
         ED_REQUIRE(s != nullptr && s->kind == ED_HUBBARD, "instance %d is not a Hubbard sector", i);
         const int64_t ld = (s->nsup + 31) / 32 * 32;   // the internal row stride of pyhub_gb300 vectors
-        if (hv_smem_bytes(ED_F64, ld) > 200 * 1024) {
+        if (hv_smem_bytes(ED_F64, ld, rows) > 200 * 1024) {
             set_error("instance %d: rows of %lld strings are too long for the batched kernel", i, (long long)s->nsup);
             return ED_ERR_RANGE;
         }
@@ -527,7 +546,8 @@ extern "C" int ed_batch_create(int ninst, ed_sector *const *secs, ed_batch **out
         a.u_value32 = (float)s->u_value;
         a.u_uniform = s->u_uniform ? 1 : 0;
         a.blk0 = blk;
-        a.nblk = (int)((s->nsdn + kRows - 1) / kRows);
+        a.nblk = (int)((s->nsdn + rows - 1) / rows);
+        a.rows = rows;
         for (int q = 0; q < a.nblk; ++q) binst.push_back(i);
         blk += a.nblk;
         offsets.push_back(off);
@@ -556,8 +576,9 @@ extern "C" int ed_batch_create(int ninst, ed_sector *const *secs, ed_batch **out
         ed_batch_destroy(bt);
         return ED_ERR_MEM;
     }
-    if (ensure_hv_smem(ED_F32, hv_smem_bytes(ED_F32, max_ld)) != ED_OK ||
-        ensure_hv_smem(ED_F64, hv_smem_bytes(ED_F64, max_ld)) != ED_OK) {
+    bt->rows = rows;
+    if (ensure_hv_smem(ED_F32, rows, hv_smem_bytes(ED_F32, max_ld, rows)) != ED_OK ||
+        ensure_hv_smem(ED_F64, rows, hv_smem_bytes(ED_F64, max_ld, rows)) != ED_OK) {
         ed_batch_destroy(bt);
         return ED_ERR_CUDA;
     }
@@ -579,6 +600,13 @@ extern "C" int ed_batch_create(int ninst, ed_sector *const *secs, ed_batch **out
     *out = bt;
     return ED_OK;
 }
+
+extern "C" int ed_batch_create(int ninst, ed_sector *const *secs, ed_batch **out)
+{
+    return ed_batch_create_rows(ninst, secs, kDefaultRows, out);
+}
+
+extern "C" int ed_batch_rows(const ed_batch *bt) { return bt ? bt->rows : -1; }
 
 extern "C" int ed_batch_destroy(ed_batch *bt)
 {
@@ -620,14 +648,21 @@ static int batch_launch(ed_batch *bt, void *stream, int dtype, void *work, const
     ED_REQUIRE(scratch != nullptr && scratch_bytes >= ed_batch_scratch_bytes(bt), "scratch of %lld bytes is below %lld",
                (long long)scratch_bytes, (long long)ed_batch_scratch_bytes(bt));
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const int rc = ensure_hv_smem(dtype, hv_smem_bytes(dtype, bt->max_ld));
+    const int rc = ensure_hv_smem(dtype, bt->rows, hv_smem_bytes(dtype, bt->max_ld, bt->rows));
     if (rc != ED_OK) return rc;
+    double *sc = (double *)scratch;
     if (dtype == ED_F32) {
-        return run_batch<float>(bt, st, (float *)work, (const float *)x0, nsteps, alpha, beta, (double *)scratch,
-                                ritz_coef, (float *)ritz_out);
+        float *w = (float *)work, *ro = (float *)ritz_out;
+        const float *x = (const float *)x0;
+        if (bt->rows == 4) return run_batch<float, 4>(bt, st, w, x, nsteps, alpha, beta, sc, ritz_coef, ro);
+        if (bt->rows == 16) return run_batch<float, 16>(bt, st, w, x, nsteps, alpha, beta, sc, ritz_coef, ro);
+        return run_batch<float, 8>(bt, st, w, x, nsteps, alpha, beta, sc, ritz_coef, ro);
     }
-    return run_batch<double>(bt, st, (double *)work, (const double *)x0, nsteps, alpha, beta, (double *)scratch,
-                             ritz_coef, (double *)ritz_out);
+    double *w = (double *)work, *ro = (double *)ritz_out;
+    const double *x = (const double *)x0;
+    if (bt->rows == 4) return run_batch<double, 4>(bt, st, w, x, nsteps, alpha, beta, sc, ritz_coef, ro);
+    if (bt->rows == 16) return run_batch<double, 16>(bt, st, w, x, nsteps, alpha, beta, sc, ritz_coef, ro);
+    return run_batch<double, 8>(bt, st, w, x, nsteps, alpha, beta, sc, ritz_coef, ro);
 }
 
 extern "C" int ed_batch_lanczos(ed_batch *bt, void *stream, int dtype, void *work, const void *x0, int nsteps,

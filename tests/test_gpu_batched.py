@@ -165,3 +165,32 @@ def test_batched_ground_states_match_dense(edlib):
         assert abs(gs.e0[i] - e) < 1e-10, (cases[i], gs.e0[i] - e)
         psi = secs[i].to_ref(gs.psi[i]).cpu().numpy()
         assert abs(float(np.dot(psi, v))) >= 1 - 1e-9, cases[i]
+
+
+def test_rows_per_cta_variants_agree(edlib):
+    """The three H*v work splits (4, 8, 16 rows of an instance per CTA) give
+    the same alpha/beta as the per-instance three-term Lanczos (FP64, 1e-9:
+    the splits group the CTA partial sums differently, and the recurrence
+    amplifies the rounding difference over 30 steps), and the autotuner
+    picks one of them."""
+    import torch
+    from pyhub_gb300.core import greens_batched as GB
+    t, U, src, gs, secs, inst, bl = _setup(edlib, nsteps=30)
+    ref = None
+    for rows in (4, 8, 16):
+        b = GB.BatchedLanczos(secs, 30, dtype=torch.float64, rows=rows)
+        assert b.rows == rows
+        b.x0.copy_(bl.x0)
+        b.run()
+        torch.cuda.synchronize()
+        A, B = b.alpha.cpu().numpy(), b.beta.cpu().numpy()
+        for key in [("up", "greater", 1), ("down", "lesser", 4), ("up", "lesser", 6)]:
+            i = inst[key]
+            if ref is None or key not in ref:
+                ref = ref or {}
+                ref[key] = GB.plain_coefficients(secs[i], bl.start(i).clone(), 30)
+            a, bb = ref[key]
+            n = np.count_nonzero(bb[1:] > 1e-8)
+            assert np.allclose(A[i, :n], a[:n], rtol=1e-9, atol=1e-9), (rows, key)
+            assert np.allclose(B[i, :n + 1], bb[:n + 1], rtol=1e-9, atol=1e-9), (rows, key)
+    assert GB.autotune(secs, torch.float32) in (4, 8, 16)
