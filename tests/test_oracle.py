@@ -193,3 +193,26 @@ def test_boltzmann_zero_temperature():
     assert np.array_equal(w, [1.0, 0.0])
     w = O.boltzmann(np.array([-3.0, -2.9, 50.0]), 1.0, 1)
     assert len(w) == 2 and np.allclose(w, [1.0, np.exp(-0.1)])
+
+
+def test_operator_algebra_recognises_hubbard_form():
+    """Operators API on the host: the Hubbard model's term list maps back to
+    its (t, U); sisj stays outside the Hubbard form (CPU, no GPU needed)."""
+    from pyhub_gb300.core.basis import Basis
+    from pyhub_gb300.tools.models import fermi_hubbard
+    from pyhub_gb300.tools.operators import c_dagger_c, n, sisj
+    rng = np.random.default_rng(0)
+    t = rng.standard_normal((5, 5))
+    U = rng.uniform(1, 4, 5)
+    H = fermi_hubbard(t, U) + 0.5
+    H.set_basis(Basis(5, (2, 3)))
+    tt, UU, const = H._hubbard()
+    assert np.array_equal(tt, t) and np.array_equal(UU, U) and const == 0.5
+    assert (2.0 * H)._hubbard()[0][1, 2] == 2.0 * t[1, 2]
+    S = sisj((0,), (3,))
+    S.set_basis(Basis(5, (2, 3)))
+    assert S._hubbard() is None and len(S._classify()[4]) == 3
+    op = c_dagger_c((0, "up"), (1, "up")) + n((2, "down"))
+    op.set_basis(Basis(5, (2, 3)))
+    assert op._hubbard() is None          # spin-dependent one-body terms: averages only
+    assert str(c_dagger_c((0, "u"), (1, "u"))) == "1.0*c^\\dagger_{0,u}c_{1,u}"
