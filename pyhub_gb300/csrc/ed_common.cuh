@@ -145,7 +145,8 @@ struct ed_sector {
     // colex rank of an empty-site pattern h (bit j: site j+1 empty) in byte
     // chunks, shared by every kernel that ranks strings on the fly:
     // rank = sum_b lut[b][popcount(h & (2^(8b)-1))][byte b of h]
-    uint32_t *lut = nullptr;   // [4][33][256]
+    uint32_t *lut = nullptr;   // [4][33][256], shared by all sectors of the device
+    void *pool = nullptr;      // the one device allocation holding this sector's hop tables
     double t_host[ed::kMaxSites * ed::kMaxSites];
     double j_host[ed::kMaxSites * ed::kMaxSites];
     int device = 0;

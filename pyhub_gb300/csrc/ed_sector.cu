@@ -12,6 +12,9 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
+#include <unordered_map>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -173,41 +176,97 @@ static int build_hop_host(int norb, int ne, const double *t, HostHop &h)
     return ED_OK;
 }
 
-template <typename T>
-static int upload(T **dst, const T *src, size_t count)
-{
-    *dst = nullptr;
-    if (count == 0) count = 1;  // keep a valid pointer for empty tables
-    cudaError_t e = cudaMalloc((void **)dst, count * sizeof(T));
-    if (e != cudaSuccess) {
-        set_error("cudaMalloc of %zu bytes for sector tables failed: %s", count * sizeof(T),
-                  cudaGetErrorString(e));
+// All device tables of one sector live in one allocation: the pieces are
+// packed on the host (256-byte aligned) and copied with one cudaMemcpy, so
+// creating a sector costs one allocation instead of one per table.
+struct TablePool {
+    std::vector<unsigned char> host;
+    std::vector<std::pair<void **, size_t>> slots;
+
+    template <typename T>
+    void add(T **dst, const T *src, size_t count)
+    {
+        if (count == 0) count = 1;  // keep a valid pointer for empty tables
+        const size_t off = (host.size() + 255) / 256 * 256;
+        host.resize(off + count * sizeof(T), 0);
+        if (src) std::memcpy(host.data() + off, src, count * sizeof(T));
+        slots.push_back({reinterpret_cast<void **>(dst), off});
         *dst = nullptr;
-        return ED_ERR_MEM;
     }
-    if (src) {
-        e = cudaMemcpy(*dst, src, count * sizeof(T), cudaMemcpyHostToDevice);
+
+    int commit(void **pool)
+    {
+        *pool = nullptr;
+        if (host.empty()) return ED_OK;
+        cudaError_t e = cudaMalloc(pool, host.size());
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            *pool = nullptr;
+            set_error("cudaMalloc of %zu bytes for sector tables failed: %s", host.size(), cudaGetErrorString(e));
+            return ED_ERR_MEM;
+        }
+        e = cudaMemcpy(*pool, host.data(), host.size(), cudaMemcpyHostToDevice);
         if (e != cudaSuccess) {
             set_error("cudaMemcpy to sector tables failed: %s", cudaGetErrorString(e));
             return ED_ERR_CUDA;
         }
+        for (auto &sl : slots) *sl.first = static_cast<unsigned char *>(*pool) + sl.second;
+        return ED_OK;
     }
-    return ED_OK;
+};
+
+// Slot layout of a sliced-ELL table: slice offsets and, per (slot, lane),
+// the hop-table entry it holds (-1: padding).  It depends only on the hop
+// structure (ptr, src), not on the coefficients, so sectors that share a
+// lattice and particle number (every cluster of a parameter sweep) share it.
+struct EllOrder {
+    std::vector<int32_t> ptr, src;   // the structure it was built for
+    std::vector<int32_t> off;        // [nslice+1]
+    std::vector<int32_t> entry;      // [slots*32]
+};
+
+static std::mutex g_ell_mu;
+static std::unordered_map<uint64_t, std::vector<std::shared_ptr<const EllOrder>>> g_ell_cache;
+
+static uint64_t hash_structure(const HostHop &h)
+{
+    uint64_t x = 1469598103934665603ull;   // FNV-1a over (n, ptr, src)
+    auto mix = [&x](uint32_t v) {
+        for (int k = 0; k < 4; ++k) {
+            x ^= (v >> (8 * k)) & 0xffu;
+            x *= 1099511628211ull;
+        }
+    };
+    mix((uint32_t)h.str.size());
+    for (int32_t v : h.ptr) mix((uint32_t)v);
+    for (int32_t v : h.src) mix((uint32_t)v);
+    return x;
 }
 
-static int upload_ell(const HostHop &h, HopTable &d)
+static std::shared_ptr<const EllOrder> ell_order(const HostHop &h)
 {
+    const uint64_t key = hash_structure(h);
+    {
+        std::lock_guard<std::mutex> lk(g_ell_mu);
+        auto it = g_ell_cache.find(key);
+        if (it != g_ell_cache.end())
+            for (const auto &o : it->second)
+                if (o->ptr == h.ptr && o->src == h.src) return o;
+    }
+    auto o = std::make_shared<EllOrder>();
+    o->ptr = h.ptr;
+    o->src = h.src;
     const int64_t n = (int64_t)h.str.size();
     const int64_t ns = (n + 31) / 32;
-    std::vector<int32_t> off((size_t)ns + 1, 0);
+    std::vector<int32_t> &off = o->off;
+    off.assign((size_t)ns + 1, 0);
     for (int64_t sl = 0; sl < ns; ++sl) {
         int32_t w = 0;
         for (int64_t u = sl * 32; u < std::min(n, sl * 32 + 32); ++u) w = std::max(w, h.ptr[(size_t)u + 1] - h.ptr[(size_t)u]);
         off[(size_t)sl + 1] = off[(size_t)sl] + w;
     }
     const int64_t slots = off[(size_t)ns];
-    std::vector<int32_t> src((size_t)std::max<int64_t>(slots * 32, 1));
-    std::vector<double> c64((size_t)std::max<int64_t>(slots * 32, 1), 0.0);
+    o->entry.assign((size_t)std::max<int64_t>(slots * 32, 1), -1);
     // Slot order within a lane is free, so each slot is filled to spread the
     // 32 lanes' sources over the shared-memory banks of the kernels that
     // gather them:
@@ -233,8 +292,13 @@ static int upload_ell(const HostHop &h, HopTable &d)
             bool used32[32] = {};
             bool used8[4][8] = {};
             int order[32];
-            for (int l = 0; l < 32; ++l) order[l] = l;
-            std::stable_sort(order, order + 32, [&](int x, int y) { return left[(size_t)x].size() > left[(size_t)y].size(); });
+            {
+                // lanes by remaining neighbours, most first (stable within equal counts)
+                int m = 0;
+                for (int64_t cnt = w; cnt >= 0 && m < 32; --cnt)
+                    for (int l = 0; l < 32; ++l)
+                        if ((int64_t)left[(size_t)l].size() == cnt) order[m++] = l;
+            }
             for (int oi = 0; oi < 32; ++oi) {
                 const int l = order[oi], qw = l >> 3;
                 const int64_t u = sl * 32 + l;
@@ -251,20 +315,48 @@ static int upload_ell(const HostHop &h, HopTable &d)
                 }
                 const int pad_score = (used8[qw][uu & 7] ? 0 : 2) + (used32[uu & 31] ? 0 : 1);
                 if (pick >= 0 && !must && best < pad_score) pick = -1;   // padding now is the cleaner choice
+                int32_t sat;
                 if (pick >= 0) {
                     const int32_t e = L[(size_t)pick];
                     L.erase(L.begin() + pick);
-                    src[at] = h.src[(size_t)e];
-                    c64[at] = h.coef[(size_t)e];
+                    o->entry[at] = e;
+                    sat = h.src[(size_t)e];
                 } else {
-                    src[at] = (int32_t)uu;
-                    c64[at] = 0.0;
+                    sat = (int32_t)uu;
                 }
-                used8[qw][src[at] & 7] = true;
-                used32[src[at] & 31] = true;
+                used8[qw][sat & 7] = true;
+                used32[sat & 31] = true;
             }
         }
     }
+    std::lock_guard<std::mutex> lk(g_ell_mu);
+    g_ell_cache[key].push_back(o);
+    return o;
+}
+
+static int upload_ell(const HostHop &h, HopTable &d, TablePool &pool)
+{
+    const std::shared_ptr<const EllOrder> o = ell_order(h);
+    const int64_t n = (int64_t)h.str.size();
+    const int64_t ns = (int64_t)o->off.size() - 1;
+    const int64_t slots = o->off[(size_t)ns];
+    const std::vector<int32_t> &off = o->off;
+    std::vector<int32_t> src((size_t)std::max<int64_t>(slots * 32, 1));
+    std::vector<double> c64((size_t)std::max<int64_t>(slots * 32, 1), 0.0);
+    for (int64_t sl = 0; sl < ns; ++sl)
+        for (int64_t k = off[(size_t)sl]; k < off[(size_t)sl + 1]; ++k)
+            for (int l = 0; l < 32; ++l) {
+                const size_t at = (size_t)(k * 32 + l);
+                const int32_t e = o->entry[at];
+                const int64_t u = sl * 32 + l;
+                if (e >= 0) {
+                    src[at] = h.src[(size_t)e];
+                    c64[at] = h.coef[(size_t)e];
+                } else {
+                    src[at] = (int32_t)(u < n ? u : n - 1);
+                    c64[at] = 0.0;
+                }
+            }
     std::vector<float> c32(c64.begin(), c64.end());
     std::vector<int2> pk(src.size());
     for (size_t q = 0; q < src.size(); ++q) {
@@ -274,63 +366,71 @@ static int upload_ell(const HostHop &h, HopTable &d)
     }
     d.nslice = ns;
     d.ell_slots = slots;
-    int rc;
-    if ((rc = upload(&d.ell_off, off.data(), off.size()))) return rc;
-    if ((rc = upload(&d.ell_src, src.data(), src.size()))) return rc;
-    if ((rc = upload(&d.ell_cf32, c32.data(), c32.size()))) return rc;
-    if ((rc = upload(&d.ell_cf64, c64.data(), c64.size()))) return rc;
-    if ((rc = upload(&d.ell_pk32, pk.data(), pk.size()))) return rc;
+    pool.add(&d.ell_off, off.data(), off.size());
+    pool.add(&d.ell_src, src.data(), src.size());
+    pool.add(&d.ell_cf32, c32.data(), c32.size());
+    pool.add(&d.ell_cf64, c64.data(), c64.size());
+    pool.add(&d.ell_pk32, pk.data(), pk.size());
     return ED_OK;
 }
 
-static int upload_hop(const HostHop &h, int norb, int ne, HopTable &d)
+// Host side of a hop table: pointers are set when the pool is committed.
+static int upload_hop(const HostHop &h, int norb, int ne, HopTable &d, TablePool &pool)
 {
     d.norb = norb;
     d.ne = ne;
     d.n = (int64_t)h.str.size();
     d.nnz = (int64_t)h.src.size();
     std::vector<float> c32(h.coef.begin(), h.coef.end());
-    int rc;
-    if ((rc = upload(&d.str, h.str.data(), h.str.size()))) return rc;
-    if ((rc = upload(&d.ptr, h.ptr.data(), h.ptr.size()))) return rc;
-    if ((rc = upload(&d.src, h.src.data(), h.src.size()))) return rc;
-    if ((rc = upload(&d.cf32, c32.data(), c32.size()))) return rc;
-    if ((rc = upload(&d.cf64, h.coef.data(), h.coef.size()))) return rc;
-    if ((rc = upload(&d.ediag, h.ediag.data(), h.ediag.size()))) return rc;
     std::vector<float> e32(h.ediag.begin(), h.ediag.end());
-    if ((rc = upload(&d.ediag32, e32.data(), e32.size()))) return rc;
-    if ((rc = upload_ell(h, d))) return rc;
+    pool.add(&d.str, h.str.data(), h.str.size());
+    pool.add(&d.ptr, h.ptr.data(), h.ptr.size());
+    pool.add(&d.src, h.src.data(), h.src.size());
+    pool.add(&d.cf32, c32.data(), c32.size());
+    pool.add(&d.cf64, h.coef.data(), h.coef.size());
+    pool.add(&d.ediag, h.ediag.data(), h.ediag.size());
+    pool.add(&d.ediag32, e32.data(), e32.size());
     d.owner = true;
-    return ED_OK;
-}
-
-static void free_hop(HopTable &d)
-{
-    if (!d.owner) { d = HopTable(); return; }
-    cudaFree(d.str); cudaFree(d.ptr); cudaFree(d.src);
-    cudaFree(d.cf32); cudaFree(d.cf64); cudaFree(d.ediag); cudaFree(d.ediag32);
-    cudaFree(d.ell_off); cudaFree(d.ell_src); cudaFree(d.ell_cf32); cudaFree(d.ell_cf64);
-    cudaFree(d.ell_pk32);
-    d = HopTable();
+    return upload_ell(h, d, pool);
 }
 
 // ------------------------------------------------------------ Heisenberg
 
+// The rank table depends on nothing but the binomials, so every sector of a
+// device shares one copy (allocated on first use, kept until the process exits).
+static std::mutex g_lut_mu;
+static uint32_t *g_lut[64] = {};
+
 static int build_lut(ed_sector *s)
 {
-    // lut[b][c][x] = sum over the set bits q of byte x, taken in increasing
-    // order with running index i = c+1, c+2, ..., of C(8b+q, i)
-    std::vector<uint32_t> lut(4 * 33 * 256, 0u);
-    for (int b = 0; b < 4; ++b)
-        for (int c = 0; c <= 32; ++c)
-            for (int x = 0; x < 256; ++x) {
-                int64_t r = 0;
-                int i = c;
-                for (int q = 0; q < 8; ++q)
-                    if ((x >> q) & 1) r += binom(8 * b + q, ++i);
-                lut[(b * 33 + c) * 256 + x] = (uint32_t)r;
-            }
-    return upload(&s->lut, lut.data(), lut.size());
+    std::lock_guard<std::mutex> lk(g_lut_mu);
+    if (s->device < 0 || s->device >= 64) {
+        set_error("device %d outside 0..63", s->device);
+        return ED_ERR_RANGE;
+    }
+    if (!g_lut[s->device]) {
+        // lut[b][c][x] = sum over the set bits q of byte x, taken in increasing
+        // order with running index i = c+1, c+2, ..., of C(8b+q, i)
+        std::vector<uint32_t> lut(4 * 33 * 256, 0u);
+        for (int b = 0; b < 4; ++b)
+            for (int c = 0; c <= 32; ++c)
+                for (int x = 0; x < 256; ++x) {
+                    int64_t r = 0;
+                    int i = c;
+                    for (int q = 0; q < 8; ++q)
+                        if ((x >> q) & 1) r += binom(8 * b + q, ++i);
+                    lut[(b * 33 + c) * 256 + x] = (uint32_t)r;
+                }
+        TablePool pool;
+        uint32_t *dev = nullptr;
+        pool.add(&dev, lut.data(), lut.size());
+        void *base = nullptr;
+        const int rc = pool.commit(&base);
+        if (rc) return rc;
+        g_lut[s->device] = dev;
+    }
+    s->lut = g_lut[s->device];
+    return ED_OK;
 }
 
 static int build_heis(ed_sector *s, const double *J)
@@ -466,18 +566,19 @@ int ed_sector_create(int norb, int nup, int ndn, int kind, const double *t, cons
             s->u_site[norb - p] = U[p - 1];  // bit norb-p holds site p
             if (U[p - 1] != U[0]) s->u_uniform = false;
         }
+        TablePool pool;
         HostHop hu;
         rc = build_hop_host(norb, nup, t, hu);
-        if (!rc) rc = upload_hop(hu, norb, nup, s->up);
-        if (!rc) {
-            if (ndn == nup) {
-                s->dn = s->up;
-                s->dn.owner = false;
-            } else {
-                HostHop hd;
-                rc = build_hop_host(norb, ndn, t, hd);
-                if (!rc) rc = upload_hop(hd, norb, ndn, s->dn);
-            }
+        if (!rc) rc = upload_hop(hu, norb, nup, s->up, pool);
+        if (!rc && ndn != nup) {
+            HostHop hd;
+            rc = build_hop_host(norb, ndn, t, hd);
+            if (!rc) rc = upload_hop(hd, norb, ndn, s->dn, pool);
+        }
+        if (!rc) rc = pool.commit(&s->pool);
+        if (!rc && ndn == nup) {
+            s->dn = s->up;      // after the commit: the copy carries the device pointers
+            s->dn.owner = false;
         }
     } else if (rc == ED_OK) {
         for (int i = 0; i < norb * norb; ++i) {
@@ -500,9 +601,7 @@ int ed_sector_create(int norb, int nup, int ndn, int kind, const double *t, cons
 int ed_sector_destroy(ed_sector *s)
 {
     if (!s) return ED_OK;
-    free_hop(s->dn);
-    free_hop(s->up);
-    if (s->lut) cudaFree(s->lut);
+    if (s->pool) cudaFree(s->pool);   // every hop table of the sector; the rank table is shared
     heis_struct_free(s->hs);
     delete s;
     return ED_OK;
