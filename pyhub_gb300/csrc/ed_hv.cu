@@ -26,6 +26,7 @@ struct HubArgs {
     const uint32_t *dstr; const int32_t *dptr; const int32_t *dsrc; const void *dcf; const void *dediag;
     int64_t nslice;
     const int32_t *ell_off; const int32_t *ell_src;
+    const int2 *ell_pk32;
     double u_site[kMaxSites];
     float u_site32[kMaxSites];
     int u_uniform;
@@ -70,6 +71,32 @@ __device__ __forceinline__ void stage_row(T *dst, const T *__restrict__ src, int
     }
 }
 
+// G up-hop slots of one lane (table entries at, at+32, ...) applied to the R
+// staged rows; the G table loads are issued before the first gather (FP32:
+// one packed 8-byte {source, coefficient} load per slot).
+template <typename T, int R, int G>
+__device__ __forceinline__ void row_group(const HubArgs &a, const T *__restrict__ ecf, int64_t at, const T *xs,
+                                          int64_t sld, T (&acc)[R])
+{
+    int q[G];
+    T c[G];
+#pragma unroll
+    for (int i = 0; i < G; ++i) {
+        if (sizeof(T) == 4) {
+            const int2 pk = __ldg(a.ell_pk32 + at + i * 32);
+            q[i] = pk.x;
+            c[i] = (T)__int_as_float(pk.y);
+        } else {
+            q[i] = __ldg(a.ell_src + at + i * 32);
+            c[i] = __ldg(ecf + at + i * 32);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < G; ++i)
+#pragma unroll
+        for (int r = 0; r < R; ++r) acc[r] += c[i] * xs[r * sld + q[i]];
+}
+
 // Pass 1: diagonal + up hops, R rows per CTA iteration.  Each warp owns one
 // 32-string slice at a time and walks its sliced-ELL slots (coalesced,
 // four slots in flight), gathering the sources from the staged rows.
@@ -107,25 +134,15 @@ __global__ void __launch_bounds__(512) hub_row_kernel(const T *__restrict__ x, T
 #pragma unroll
             for (int r = 0; r < R; ++r) acc[r] = (eu + ed[r] + u_energy<T>(a, su & sd[r], uval)) * xs[r * sld + uu];
             const int s0 = __ldg(a.ell_off + sl), ns = __ldg(a.ell_off + sl + 1) - s0;
-            const int32_t *sp = a.ell_src + (int64_t)s0 * 32 + lane;
-            const T *cp = ecf + (int64_t)s0 * 32 + lane;
+            const int64_t at0 = (int64_t)s0 * 32 + lane;
+            // slots in groups: all table loads of a group are in flight before its first gather
             int k = 0;
-            for (; k + 4 <= ns; k += 4) {
-                int q[4];
-                T c[4];
-#pragma unroll
-                for (int i = 0; i < 4; ++i) { q[i] = __ldg(sp + (k + i) * 32); c[i] = __ldg(cp + (k + i) * 32); }
-#pragma unroll
-                for (int i = 0; i < 4; ++i)
-#pragma unroll
-                    for (int r = 0; r < R; ++r) acc[r] += c[i] * xs[r * sld + q[i]];
+            for (; k + 8 <= ns; k += 8) row_group<T, R, 8>(a, ecf, at0 + k * 32, xs, sld, acc);
+            if (k + 4 <= ns) {
+                row_group<T, R, 4>(a, ecf, at0 + k * 32, xs, sld, acc);
+                k += 4;
             }
-            for (; k < ns; ++k) {
-                const int q = __ldg(sp + k * 32);
-                const T c = __ldg(cp + k * 32);
-#pragma unroll
-                for (int r = 0; r < R; ++r) acc[r] += c * xs[r * sld + q];
-            }
+            for (; k < ns; ++k) row_group<T, R, 1>(a, ecf, at0 + k * 32, xs, sld, acc);
             if (ok) {
 #pragma unroll
                 for (int r = 0; r < R; ++r)
@@ -310,6 +327,7 @@ static int hub_hv(ed_sector *s, cudaStream_t st, int64_t ld, const T *x, T *y, d
     a.nslice = s->up.nslice;
     a.ell_off = s->up.ell_off;
     a.ell_src = s->up.ell_src;
+    a.ell_pk32 = s->up.ell_pk32;
     for (int b = 0; b < kMaxSites; ++b) {
         a.u_site[b] = s->u_site[b];
         a.u_site32[b] = (float)s->u_site[b];
