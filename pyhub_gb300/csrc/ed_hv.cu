@@ -153,6 +153,8 @@ __global__ void __launch_bounds__(512) hub_row_kernel(const T *__restrict__ x, T
     }
 }
 
+constexpr int kSlabLoads = 4;   // neighbour-row loads in flight per warp in the slab pass (8 costs occupancy)
+
 // Pass 2: down hops, y[d][slab] += sum_e c_e x[src_e][slab]; optional dots.
 // Work items (slab, group of 8 rows) are visited slab-major by a persistent
 // grid so that the CTAs in flight share one or two slabs of x in L2.  A warp
@@ -193,11 +195,11 @@ __global__ void __launch_bounds__(256) hub_slab_kernel(const T *__restrict__ x, 
 #pragma unroll
                 for (int k = 0; k < VW; ++k) acc[k] = (k < nk) ? yr[c + k] : (T)0;
                 int e = 0;
-                for (; e + 4 <= nb; e += 4) {
-                    T v[4][VW];
-                    T wgt[4];
+                for (; e + kSlabLoads <= nb; e += kSlabLoads) {
+                    T v[kSlabLoads][VW];
+                    T wgt[kSlabLoads];
 #pragma unroll
-                    for (int i = 0; i < 4; ++i) {
+                    for (int i = 0; i < kSlabLoads; ++i) {
                         const int64_t sidx = __shfl_sync(0xffffffffu, my_src, e + i);
                         wgt[i] = __shfl_sync(0xffffffffu, my_cf, e + i);
                         const T *xr = x + sidx * ld + c;
@@ -218,7 +220,7 @@ __global__ void __launch_bounds__(256) hub_slab_kernel(const T *__restrict__ x, 
                         }
                     }
 #pragma unroll
-                    for (int i = 0; i < 4; ++i)
+                    for (int i = 0; i < kSlabLoads; ++i)
 #pragma unroll
                         for (int k = 0; k < VW; ++k) acc[k] += wgt[i] * v[i][k];
                 }
