@@ -100,8 +100,8 @@ __device__ __forceinline__ void row_group(const HubArgs &a, const T *__restrict_
 // Pass 1: diagonal + up hops, R rows per CTA iteration.  Each warp owns one
 // 32-string slice at a time and walks its sliced-ELL slots (coalesced,
 // four slots in flight), gathering the sources from the staged rows.
-template <typename T, int R>
-__global__ void __launch_bounds__(512) hub_row_kernel(const T *__restrict__ x, T *__restrict__ y,
+template <typename T, int R, int NT = 512>
+__global__ void __launch_bounds__(NT) hub_row_kernel(const T *__restrict__ x, T *__restrict__ y,
                                                       const HubArgs a, int64_t sld, int vec_ok)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -354,11 +354,24 @@ static int hub_hv(ed_sector *s, cudaStream_t st, int64_t ld, const T *x, T *y, d
                   (long long)s->nsup, maxsm);
         return ED_ERR_RANGE;
     }
-    // two rows per CTA when they fit with two CTAs per SM, else one
+    // FP32: four rows per 1024-thread CTA (one CTA per SM) when they fit, so every
+    // hop-table slot serves four rows; else two rows per CTA with two CTAs per SM;
+    // else one.  PYHUB_ED_ROW_RPC=2 forces the two-row form (for timing).
     constexpr int R2 = 2;
     const bool two = (size_t)R2 * row_bytes * 2 <= (size_t)maxsm;
     const int threads = 512;
-    if (two) {
+    static const int rpc_env = []() {
+        const char *e = std::getenv("PYHUB_ED_ROW_RPC");
+        return e ? std::atoi(e) : 0;
+    }();
+    if (sizeof(T) == 4 && rpc_env != 2 && (size_t)4 * row_bytes <= (size_t)maxsm) {
+        size_t smem = (size_t)4 * row_bytes;
+        ED_CHECK_CUDA(cudaFuncSetAttribute(hub_row_kernel<T, 4, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem));
+        int64_t blocks = (s->nsdn + 3) / 4;
+        if (blocks > nsm) blocks = nsm;
+        hub_row_kernel<T, 4, 1024><<<(unsigned)blocks, 1024, smem, st>>>(x, y, a, sld, vec_ok ? 1 : 0);
+    } else if (two) {
         size_t smem = (size_t)R2 * row_bytes;
         ED_CHECK_CUDA(cudaFuncSetAttribute(hub_row_kernel<T, R2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         int64_t blocks = (s->nsdn + R2 - 1) / R2;
