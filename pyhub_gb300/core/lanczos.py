@@ -441,7 +441,7 @@ def ground_state(sec, mode: str = "mixed", steps: int = 200, seed: int = 0, v0=N
     reorth "full" keeps every Krylov vector (lanczos_full); "none" runs the
     three-term recurrence on four vectors and rebuilds the Ritz vector by a
     second pass (lanczos_plain), for sectors whose basis would not fit;
-    refine_rule (reorth "none") replaces the energy rule of the FP64 stage."""
+    refine_rule replaces the energy rule of the FP64 stage."""
     torch = _torch()
     t0 = time.perf_counter()
     if v0 is None:
@@ -465,8 +465,10 @@ def ground_state(sec, mode: str = "mixed", steps: int = 200, seed: int = 0, v0=N
                            steps=r32.steps, refine_steps=0, converged=r32.converged, ndeg=r32.ndeg,
                            times={"total": t1 - t0, "fp32": r32.times["total"]}, mode=mode,
                            e0_unrefined=float(r32.ritz[0]), ritz_vectors=r32.ritz_vectors)
-    rr = EnergyRule(refine_tol * max(1.0, abs(float(r32.ritz[0]))), min_steps=2 * check_every)
-    r64 = lanczos_full(sec, r32.psi, refine_steps, torch.float64, rule=rr, check_every=check_every,
+    rr = refine_rule or EnergyRule(refine_tol * max(1.0, abs(float(r32.ritz[0]))), min_steps=2 * check_every)
+    psi32 = r32.psi
+    r32.release()
+    r64 = lanczos_full(sec, psi32, refine_steps, torch.float64, rule=rr, check_every=check_every,
                        timer=timer)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
