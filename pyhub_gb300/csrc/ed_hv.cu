@@ -100,8 +100,8 @@ __device__ __forceinline__ void row_group(const HubArgs &a, const T *__restrict_
 // Pass 1: diagonal + up hops, R rows per CTA iteration.  Each warp owns one
 // 32-string slice at a time and walks its sliced-ELL slots (coalesced,
 // four slots in flight), gathering the sources from the staged rows.
-template <typename T, int R, int NT = 512>
-__global__ void __launch_bounds__(NT) hub_row_kernel(const T *__restrict__ x, T *__restrict__ y,
+template <typename T, int R>
+__global__ void __launch_bounds__(512) hub_row_kernel(const T *__restrict__ x, T *__restrict__ y,
                                                       const HubArgs a, int64_t sld, int vec_ok)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -146,6 +146,90 @@ __global__ void __launch_bounds__(NT) hub_row_kernel(const T *__restrict__ x, T 
             if (ok) {
 #pragma unroll
                 for (int r = 0; r < R; ++r)
+                    if (r < nr) y[(d0 + r) * ld + u] = acc[r] * sc;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Pass 1 for FP32 with four rows per CTA, column layout: the four rows of
+// string u are staged as one 16-byte column xs4[u], so a hop gathers all four
+// rows with one 128-bit shared load.  A quarter warp's 8 lanes hit 8 bank
+// groups when their sources differ mod 8, which the sliced-ELL slot order
+// arranges (ed_sector.cu, ell_order).
+template <int G>
+__device__ __forceinline__ void col_group(const HubArgs &a, int64_t at, const float4 *xs4, float (&acc)[4])
+{
+    int q[G];
+    float c[G];
+#pragma unroll
+    for (int i = 0; i < G; ++i) {
+        const int2 pk = __ldg(a.ell_pk32 + at + i * 32);
+        q[i] = pk.x;
+        c[i] = __int_as_float(pk.y);
+    }
+#pragma unroll
+    for (int i = 0; i < G; ++i) {
+        const float4 v = xs4[q[i]];
+        acc[0] += c[i] * v.x;
+        acc[1] += c[i] * v.y;
+        acc[2] += c[i] * v.z;
+        acc[3] += c[i] * v.w;
+    }
+}
+
+__global__ void __launch_bounds__(1024) hub_row_col4_kernel(const float *__restrict__ x, float *__restrict__ y,
+                                                            const HubArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float4 *xs4 = reinterpret_cast<float4 *>(smem_raw);   // [nsup]
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    const int64_t nsup = a.nsup, ld = a.ld;
+    const float uval = (float)a.u_value, sc = (float)a.scale;
+    const float *ued_t = static_cast<const float *>(a.uediag), *ded_t = static_cast<const float *>(a.dediag);
+    for (int64_t d0 = (int64_t)blockIdx.x * 4; d0 < a.nsdn; d0 += (int64_t)gridDim.x * 4) {
+        const int nr = (int)min((int64_t)4, a.nsdn - d0);
+        const float *x0 = x + d0 * ld;
+        for (int64_t c = threadIdx.x; c < nsup; c += blockDim.x) {
+            float4 v;
+            v.x = __ldg(x0 + c);
+            v.y = nr > 1 ? __ldg(x0 + ld + c) : 0.f;
+            v.z = nr > 2 ? __ldg(x0 + 2 * ld + c) : 0.f;
+            v.w = nr > 3 ? __ldg(x0 + 3 * ld + c) : 0.f;
+            xs4[c] = v;
+        }
+        __syncthreads();
+        uint32_t sd[4];
+        float ed[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            sd[r] = (r < nr) ? __ldg(a.dstr + d0 + r) : 0u;
+            ed[r] = (r < nr) ? __ldg(ded_t + d0 + r) : 0.f;
+        }
+        for (int64_t sl = warp; sl < a.nslice; sl += nwarps) {
+            const int64_t u = sl * 32 + lane;
+            const bool ok = u < nsup;
+            const int64_t uu = ok ? u : nsup - 1;
+            const uint32_t su = __ldg(a.ustr + uu);
+            const float eu = __ldg(ued_t + uu);
+            const float4 xv = xs4[uu];
+            const float xr[4] = {xv.x, xv.y, xv.z, xv.w};
+            float acc[4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r) acc[r] = (eu + ed[r] + u_energy<float>(a, su & sd[r], uval)) * xr[r];
+            const int s0 = __ldg(a.ell_off + sl), ns = __ldg(a.ell_off + sl + 1) - s0;
+            const int64_t at0 = (int64_t)s0 * 32 + lane;
+            int k = 0;
+            for (; k + 8 <= ns; k += 8) col_group<8>(a, at0 + k * 32, xs4, acc);
+            if (k + 4 <= ns) {
+                col_group<4>(a, at0 + k * 32, xs4, acc);
+                k += 4;
+            }
+            for (; k < ns; ++k) col_group<1>(a, at0 + k * 32, xs4, acc);
+            if (ok) {
+#pragma unroll
+                for (int r = 0; r < 4; ++r)
                     if (r < nr) y[(d0 + r) * ld + u] = acc[r] * sc;
             }
         }
@@ -355,22 +439,20 @@ static int hub_hv(ed_sector *s, cudaStream_t st, int64_t ld, const T *x, T *y, d
         return ED_ERR_RANGE;
     }
     // FP32: four rows per 1024-thread CTA (one CTA per SM) when they fit, so every
-    // hop-table slot serves four rows; else two rows per CTA with two CTAs per SM;
-    // else one.  PYHUB_ED_ROW_RPC=2 forces the two-row form (for timing).
+    // hop-table slot serves four rows and one 128-bit gather reads all four;
+    // else two rows per CTA with two CTAs per SM; else one.
     constexpr int R2 = 2;
     const bool two = (size_t)R2 * row_bytes * 2 <= (size_t)maxsm;
     const int threads = 512;
-    static const int rpc_env = []() {
-        const char *e = std::getenv("PYHUB_ED_ROW_RPC");
-        return e ? std::atoi(e) : 0;
-    }();
-    if (sizeof(T) == 4 && rpc_env != 2 && (size_t)4 * row_bytes <= (size_t)maxsm) {
-        size_t smem = (size_t)4 * row_bytes;
-        ED_CHECK_CUDA(cudaFuncSetAttribute(hub_row_kernel<T, 4, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)smem));
+    if (sizeof(T) == 4 && (size_t)s->nsup * 16 <= (size_t)maxsm) {
+        // four rows per 1024-thread CTA, staged as 16-byte columns
+        const size_t smem = (size_t)s->nsup * 16;
         int64_t blocks = (s->nsdn + 3) / 4;
         if (blocks > nsm) blocks = nsm;
-        hub_row_kernel<T, 4, 1024><<<(unsigned)blocks, 1024, smem, st>>>(x, y, a, sld, vec_ok ? 1 : 0);
+        ED_CHECK_CUDA(cudaFuncSetAttribute(hub_row_col4_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem));
+        hub_row_col4_kernel<<<(unsigned)blocks, 1024, smem, st>>>(reinterpret_cast<const float *>(x),
+                                                                  reinterpret_cast<float *>(y), a);
     } else if (two) {
         size_t smem = (size_t)R2 * row_bytes;
         ED_CHECK_CUDA(cudaFuncSetAttribute(hub_row_kernel<T, R2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
