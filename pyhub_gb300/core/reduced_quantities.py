@@ -191,14 +191,52 @@ class GreenFunction:
                 "down": np.array([[Pole({"positions": self.ek, "weights": self.Vk[i, :] * self.Vk[j, :]})
                                    for i in range(self.nb_sites)] for j in range(self.nb_sites)])}
 
+    def gf_matrix(self, w, eta=0.05, device=None):
+        """G_s(w)[k, i, j] = sum_p weight_p / (w_k - position_p + i eta) for all
+        frequencies at once: every (i, j) pole set is padded into one [n, n, P]
+        array and the sum runs as one tensor contraction (on the GPU when there
+        is one).  Returns {spin: complex128 torch tensor [nw, n, n]}."""
+        import torch
+        dev = device or ("cuda" if torch.cuda.is_available() else "cpu")
+        wv = torch.as_tensor(np.atleast_1d(np.asarray(w, dtype=np.float64)), device=dev)
+        n = self.nb_sites_comp
+        out = {}
+        for s in ("up", "down"):
+            P = max(1, max(len(self.gf[s][i, j].pole["positions"]) for i in range(n) for j in range(n)))
+            pos = np.zeros((n, n, P))
+            wts = np.zeros((n, n, P))
+            for i in range(n):
+                for j in range(n):
+                    pl = self.gf[s][i, j].pole
+                    k = len(pl["positions"])
+                    pos[i, j, :k] = pl["positions"]
+                    wts[i, j, :k] = pl["weights"]
+            pos_t = torch.as_tensor(pos, device=dev)
+            wts_t = torch.as_tensor(wts, device=dev).to(torch.complex128)
+            den = wv[:, None, None, None] - pos_t[None] + 1j * eta
+            out[s] = (wts_t[None] / den).sum(dim=-1)
+        return out
+
     def self_energy(self, w, eta=0.05):
         """Sigma(w) = G0^-1 - G^-1 with the reference's pseudo-inverses
-        (reduced_quantities.py:134-161), G evaluated from its poles."""
+        (reduced_quantities.py:134-161), G evaluated from its poles.  For an
+        array of frequencies all of them are done at once (gf_matrix and
+        batched pseudo-inverses); the result keeps the reference's layout
+        [j][i][k] = Sigma(w_k)[i, j]."""
         if isinstance(w, (list, np.ndarray)):
-            A = [self.self_energy(w_, eta=eta) for w_ in w]
+            import torch
+            wv = np.asarray(w, dtype=np.float64)
+            G = self.gf_matrix(wv, eta=eta)
+            dev = G["up"].device
             n = self.nb_sites_comp
-            return {s: np.array([[[A[k][s][i, j] for k in range(len(w))] for i in range(n)] for j in range(n)],
-                                dtype=np.complex128) for s in ("up", "down")}
+            Vk = torch.as_tensor(self.Vk, device=dev).to(torch.complex128)
+            ek = torch.as_tensor(self.ek, device=dev)
+            wt = torch.as_tensor(wv, device=dev)
+            d0 = 1.0 / (wt[:, None] - ek[None, :] + 1j * eta)                 # [nw, nk]
+            g0 = torch.einsum("ik,jk,wk->wij", Vk, Vk, d0)
+            g0i = torch.linalg.pinv(g0, rtol=1e-15)[:, :n, :n]
+            return {s: (g0i - torch.linalg.pinv(G[s], rtol=1e-15)).permute(2, 1, 0).cpu().numpy()
+                    for s in ("up", "down")}
         g0 = np.linalg.pinv(np.einsum("ik,jk,k->ij", self.Vk, self.Vk, 1. / (w - self.ek + 1j * eta)))
         out = {}
         for s in ("up", "down"):

@@ -215,3 +215,30 @@ def test_heisenberg_lattice_rdm_and_plain_mixed_ground_state(edlib):
     r2, _ = sec.rdm_raw(gs.psi, pairs=bonds)
     e_bonds = sum(J[j - 1, i - 1] * (q[1] - q[0]) for (i, j), q in zip(bonds, r2))
     assert abs(gs.e0 - e_bonds) < 1e-8, (gs.e0, e_bonds)
+
+
+def test_self_energy_array_matches_per_frequency(edlib):
+    """GreenFunction.self_energy on a frequency array (gf_matrix + batched
+    pseudo-inverses) equals the reference's per-frequency evaluation, in the
+    reference's [j][i][k] layout, to 1e-10 relative; gf_matrix equals the
+    Pole objects' retarded values."""
+    from pyhub_gb300.solver import FermiHubbard
+    norb = 6
+    t = O.ring(norb)
+    t[0, 3] = t[3, 0] = -0.3
+    fh = FermiHubbard(norb, 3, 3, t, 3.0)
+    fh.kernel(max_lcz=300, acc_lcz=1e-13, compute_rq=False)
+    fh.spgf(nsteps=200)
+    w = np.linspace(-6, 6, 41)
+    G = fh.gf_matrix(w, eta=0.1)
+    for s in ("up", "down"):
+        for i in range(norb):
+            for j in range(norb):
+                ref = fh.gf[s][i, j].retarded(w, eta=0.1)
+                assert np.abs(G[s][:, i, j].cpu().numpy() - ref).max() <= 1e-12 * max(1.0, np.abs(ref).max())
+    S = fh.self_energy(w, eta=0.1)
+    for k in (0, 17, 40):
+        one = fh.self_energy(w[k], eta=0.1)
+        for s in ("up", "down"):
+            got = S[s][:, :, k].T
+            assert np.abs(got - one[s]).max() <= 1e-10 * max(1.0, np.abs(one[s]).max()), (s, k)
