@@ -150,6 +150,27 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
+class StreamClock:
+    """Elapsed time of a region on the device: CUDA events recorded on the
+    current stream (where every C-ABI call enqueues its kernels) at start()
+    and stop(); stop() synchronises and returns seconds."""
+
+    def __init__(self):
+        import torch
+        self.torch = torch
+        self.e0 = torch.cuda.Event(enable_timing=True)
+        self.e1 = torch.cuda.Event(enable_timing=True)
+
+    def start(self):
+        self.e0.record(self.torch.cuda.current_stream())
+        return self
+
+    def stop(self) -> float:
+        self.e1.record(self.torch.cuda.current_stream())
+        self.e1.synchronize()
+        return self.e0.elapsed_time(self.e1) / 1e3
+
+
 def dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -256,10 +277,10 @@ def run_c4(args):
     clocks = ClockSampler(local)
     clocks.start()
     tim = {}
-    t0 = time.perf_counter()
+    clock = StreamClock().start()
     res = GB.sweep(mine, nsteps=150, chunk=64, timings=tim)
+    elapsed_local = clock.stop()
     RP.barrier()
-    elapsed_local = time.perf_counter() - t0
     clk = clocks.stop()
     rate, total_gf, elapsed = RP.aggregate_rate(tim["instances"], elapsed_local)
     # per-instance path on the start vectors of the first cluster
@@ -280,10 +301,9 @@ def run_c4(args):
             _capi.gf_start(src, dst, ("e_" if part == "greater" else "h_") + spin, site, gs.psi, phi)
             sample.append((dst, phi.float()))
     torch.cuda.synchronize()
-    t1 = time.perf_counter()
+    clock = StreamClock().start()
     coef = [GB.plain_coefficients(dst, phi, 150) for dst, phi in sample]
-    torch.cuda.synchronize()
-    t_plain = (time.perf_counter() - t1) / len(sample)
+    t_plain = clock.stop() / len(sample)
     n_gf = tim["instances"]
     gf_rate = n_gf / tim["lanczos_s"]
     if rank == 0:
@@ -347,7 +367,7 @@ def run_c3(args):
     clocks = ClockSampler(local)
     clocks.start()
     RP.barrier()
-    t0 = time.perf_counter()
+    clock = StreamClock().start()
     # FP32 stage until E0 stalls at FP32 resolution; FP64 stage until the residual estimate is below 1e-9.
     # Three-term form on four vectors: keeping the bases instead (55 x 2.4 GB FP32, 40 x 4.8 GB FP64) was
     # measured no faster, the saved second passes being paid for by allocating and clearing the bases.
@@ -355,8 +375,8 @@ def run_c3(args):
     gs = LZ.ground_state(sec, mode="mixed", steps=steps32, reorth=reorth, refine_steps=steps64,
                          rule=LZ.EnergyRule(1e-7, min_steps=20), refine_rule=LZ.ResidualRule(1e-9, 10))
     raw, _ = sec.rdm_raw(gs.psi, pairs=bonds)
+    t_solve = clock.stop()
     RP.barrier()
-    t_solve = time.perf_counter() - t0
     clk = clocks.stop()
     rate, _, t_max = RP.aggregate_rate(1.0, t_solve)   # replicas: one solve per rank
     sij = raw[:, 0] + raw[:, 1]          # SMATRIX(J,K) as J_SPIN forms it (static_rq_heis.f90:66-114)
@@ -435,13 +455,13 @@ def run_c5(args):
     clocks.start()
     RP.barrier()
     times = []
-    t_all = time.perf_counter()
+    clock_all = StreamClock().start()
     for _ in range(args.steps):
-        t0 = time.perf_counter()
+        clock = StreamClock().start()
         sol, g_e, L, g_l, info = step()
-        times.append(time.perf_counter() - t0)
+        times.append(clock.stop())
+    t_all = clock_all.stop()
     RP.barrier()
-    t_all = time.perf_counter() - t_all
     clk = clocks.stop()
     rate, _, t_max = RP.aggregate_rate(args.steps, t_all)   # replicas: args.steps evaluations per rank
     # central differences of FP64 solves on a sample of parameters (bonds, U, eps)
@@ -536,14 +556,14 @@ def main():
     clocks = ClockSampler(local)
     clocks.start()
     timer = LZ.KernelTimer()
-    t0 = time.perf_counter()
+    clock = StreamClock().start()
     res = []
     for _ in range(args.steps):
         g = solve(timer)
         res.append((g.e0, g.steps, g.refine_steps, g.e0_unrefined))
         del g
+    elapsed = clock.stop()
     barrier()
-    elapsed = time.perf_counter() - t0
     clk = clocks.stop()
     elapsed = max_over_ranks(elapsed)
     ksum = timer.summary()
@@ -617,10 +637,10 @@ def main():
             del held
             torch.cuda.empty_cache()
             barrier()
-            t1 = time.perf_counter()
+            clock = StreamClock().start()
             g64 = LZ.ground_state(sec, mode="f64", steps=args.lanczos_steps, seed=0)
+            t64 = max_over_ranks(clock.stop())
             barrier()
-            t64 = max_over_ranks(time.perf_counter() - t1)
             fp64 = {"seconds": t64, "e0": g64.e0, "steps": g64.steps,
                     "abs_dE0_mixed_vs_fp64": abs(e0_mixed - g64.e0),
                     "speedup_mixed_vs_fp64": t64 / (elapsed / args.steps),
