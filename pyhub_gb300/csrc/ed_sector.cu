@@ -227,6 +227,8 @@ struct EllOrder {
 
 static std::mutex g_ell_mu;
 static std::unordered_map<uint64_t, std::vector<std::shared_ptr<const EllOrder>>> g_ell_cache;
+static size_t g_ell_count = 0;
+constexpr size_t kEllCacheMax = 256;
 
 static uint64_t hash_structure(const HostHop &h)
 {
@@ -330,7 +332,14 @@ static std::shared_ptr<const EllOrder> ell_order(const HostHop &h)
         }
     }
     std::lock_guard<std::mutex> lk(g_ell_mu);
+    // a sweep over many different lattices must not grow the cache without bound: past
+    // kEllCacheMax structures it starts over (orders in use stay alive through their owners)
+    if (g_ell_count >= kEllCacheMax) {
+        g_ell_cache.clear();
+        g_ell_count = 0;
+    }
     g_ell_cache[key].push_back(o);
+    ++g_ell_count;
     return o;
 }
 
