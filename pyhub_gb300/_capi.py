@@ -78,9 +78,19 @@ def check(func: str, rc: int):
         raise EDError(func, rc, lib().ed_last_error().decode(errors="replace"))
 
 
-def _ptr(t) -> int | None:
+def _ptr(t, need: int | None = None, what: str = "tensor") -> int | None:
+    """Device pointer of a tensor handed to a kernel.  Refuses what would make
+    a kernel read or write outside the caller's memory: host tensors, a
+    non-unit innermost stride, and (with ``need``) fewer than ``need``
+    elements."""
     if t is None:
         return None
+    if not t.is_cuda:
+        raise ValueError(f"{what} must be a CUDA tensor (got device {t.device})")
+    if t.dim() > 0 and t.stride(-1) != 1:
+        raise ValueError(f"{what} must have unit stride in its last dimension")
+    if need is not None and t.numel() < need:
+        raise ValueError(f"{what} holds {t.numel()} elements, {need} needed")
     return t.data_ptr()
 
 
@@ -224,8 +234,12 @@ class Sector:
         nb = int(lib().ed_rdm_scratch_bytes(npairs))
         scratch = torch.empty((nb + 7) // 8, dtype=torch.float64, device=bra.device)
         ld = self.ld if ld is None else ld
-        check("ed_rdm", lib().ed_rdm(self._h, _stream(stream), dtype_code(bra.dtype), int(ld), _ptr(bra), _ptr(ket),
-                                     npairs, pr.ctypes.data, int(flags), _ptr(out), _ptr(scratch), nb))
+        need = self._need(ld)
+        if ket.dtype != bra.dtype:
+            raise TypeError("bra and ket must have the same dtype")
+        check("ed_rdm", lib().ed_rdm(self._h, _stream(stream), dtype_code(bra.dtype), int(ld), _ptr(bra, need, "bra"),
+                                     _ptr(ket, need, "ket"), npairs, pr.ctypes.data, int(flags), _ptr(out),
+                                     _ptr(scratch), nb))
         o = out.cpu().numpy()
         if self.kind == ED_HUBBARD:
             raw = np.concatenate([o[: 4 * npairs].reshape(npairs, 4), o[4 * npairs:].reshape(npairs, 2)], axis=1)
@@ -237,8 +251,18 @@ class Sector:
         """y = scale * H x (device tensors in the internal layout unless ld is given)."""
         ld = self.ld if ld is None else ld
         sb = 0 if scratch is None else scratch.numel() * scratch.element_size()
-        check("ed_hv", lib().ed_hv(self._h, _stream(stream), dtype_code(x.dtype), int(ld), _ptr(x), _ptr(y),
-                                   float(scale), _ptr(dots), _ptr(scratch), int(sb)))
+        need = self._need(ld)
+        if y.dtype != x.dtype:
+            raise TypeError("x and y must have the same dtype")
+        check("ed_hv", lib().ed_hv(self._h, _stream(stream), dtype_code(x.dtype), int(ld), _ptr(x, need, "x"),
+                                   _ptr(y, need, "y"), float(scale), _ptr(dots, 2, "dots"), _ptr(scratch),
+                                   int(sb)))
+
+    def _need(self, ld: int) -> int:
+        """Elements a vector with row stride ld must hold."""
+        if self.kind != ED_HUBBARD:
+            return self.dim
+        return (self.nsdn - 1) * int(ld) + self.nsup if self.nsdn > 0 else 0
 
 
 class Batch:
@@ -280,6 +304,7 @@ class Batch:
 
     def lanczos(self, work, x0, nsteps: int, alpha, beta, scratch, stream=None):
         sb = scratch.numel() * scratch.element_size()
+        self._check(work, x0, nsteps, alpha, beta)
         check("ed_batch_lanczos", lib().ed_batch_lanczos(self._h, _stream(stream), dtype_code(x0.dtype), _ptr(work),
                                                          _ptr(x0), int(nsteps), _ptr(alpha), _ptr(beta), _ptr(scratch),
                                                          int(sb)))
@@ -287,17 +312,34 @@ class Batch:
     def ritz(self, work, x0, nsteps: int, alpha, beta, coef, out, scratch, stream=None):
         """Replay of lanczos() accumulating out_i += sum_k coef[i, k] q_k."""
         sb = scratch.numel() * scratch.element_size()
+        self._check(work, x0, nsteps, alpha, beta)
+        if out.dtype != x0.dtype:
+            raise TypeError("out must have the dtype of x0")
+        n = len(self.sectors)
         check("ed_batch_ritz", lib().ed_batch_ritz(self._h, _stream(stream), dtype_code(x0.dtype), _ptr(work),
-                                                   _ptr(x0), int(nsteps), _ptr(alpha), _ptr(beta), _ptr(coef),
-                                                   _ptr(out), _ptr(scratch), int(sb)))
+                                                   _ptr(x0), int(nsteps), _ptr(alpha), _ptr(beta),
+                                                   _ptr(coef, n * int(nsteps), "coef"), _ptr(out, self.total, "out"),
+                                                   _ptr(scratch), int(sb)))
+
+    def _check(self, work, x0, nsteps, alpha, beta):
+        import torch
+        n = len(self.sectors)
+        if work.dtype != x0.dtype:
+            raise TypeError("work and x0 must have the same dtype")
+        if alpha.dtype != torch.float64 or beta.dtype != torch.float64:
+            raise TypeError("alpha and beta are FP64")
+        _ptr(work, 3 * self.total, "work")
+        _ptr(x0, self.total, "x0")
+        _ptr(alpha, n * int(nsteps), "alpha")
+        _ptr(beta, n * (int(nsteps) + 1), "beta")
 
 
 def gf_start(src: "Sector", dst: "Sector", kind: str, site: int, psi, out, stream=None):
     """out = c_{site}|psi> or c^+_{site}|psi> (kind 'h_up','h_down','e_up','e_down'),
     both vectors in their sectors' internal layouts."""
     check("ed_gf_start", lib().ed_gf_start(src.handle, dst.handle, _stream(stream), GF_KINDS[kind], int(site),
-                                           dtype_code(psi.dtype), src.ld, _ptr(psi), dtype_code(out.dtype), dst.ld,
-                                           _ptr(out)))
+                                           dtype_code(psi.dtype), src.ld, _ptr(psi, src._need(src.ld), "psi"),
+                                           dtype_code(out.dtype), dst.ld, _ptr(out, dst._need(dst.ld), "out")))
 
 
 def multidot(V, nvec: int, w, out, scratch, z=None, n: int | None = None, stream=None):
@@ -305,8 +347,11 @@ def multidot(V, nvec: int, w, out, scratch, z=None, n: int | None = None, stream
     n = w.numel() if n is None else n
     ldv = V.stride(0) if V.dim() > 1 else n
     sb = scratch.numel() * scratch.element_size()
-    check("ed_multidot", lib().ed_multidot(_stream(stream), dtype_code(V.dtype), int(n), _ptr(V), int(ldv), int(nvec),
-                                           _ptr(w), _ptr(z), _ptr(out), _ptr(scratch), int(sb)))
+    check("ed_multidot", lib().ed_multidot(_stream(stream), dtype_code(V.dtype), int(n),
+                                           _ptr(V, (int(nvec) - 1) * int(ldv) + int(n), "V"), int(ldv), int(nvec),
+                                           _ptr(w, n, "w"), _ptr(z, n, "z"),
+                                           _ptr(out, (2 if z is not None else 1) * int(nvec), "out"),
+                                           _ptr(scratch), int(sb)))
 
 
 def update(V, nvec: int, coef, w, out, norm2=None, scratch=None, n: int | None = None, stream=None):
@@ -315,5 +360,7 @@ def update(V, nvec: int, coef, w, out, norm2=None, scratch=None, n: int | None =
     ldv = V.stride(0) if (V is not None and V.dim() > 1) else n
     sb = 0 if scratch is None else scratch.numel() * scratch.element_size()
     vdt = dtype_code(V.dtype) if V is not None else dtype_code(out.dtype)
-    check("ed_update", lib().ed_update(_stream(stream), vdt, dtype_code(out.dtype), int(n), _ptr(V), int(ldv),
-                                       int(nvec), _ptr(coef), _ptr(w), _ptr(out), _ptr(norm2), _ptr(scratch), int(sb)))
+    needV = (int(nvec) - 1) * int(ldv) + int(n) if (V is not None and int(nvec) > 0) else None
+    check("ed_update", lib().ed_update(_stream(stream), vdt, dtype_code(out.dtype), int(n), _ptr(V, needV, "V"),
+                                       int(ldv), int(nvec), _ptr(coef, int(nvec), "coef"), _ptr(w, n, "w"),
+                                       _ptr(out, n, "out"), _ptr(norm2, 1, "norm2"), _ptr(scratch), int(sb)))

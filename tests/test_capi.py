@@ -60,3 +60,13 @@ def test_invalid_arguments_rejected_before_launch(edlib):
     L = edlib.lib()
     assert L.ed_hv(None, None, 0, 0, None, None, 1.0, None, None, 0) == edlib.ED_ERR_ARG
     assert "NULL" in L.ed_last_error().decode()
+
+
+def test_pointer_checks_refuse_host_and_short_tensors():
+    """Tensors handed to kernels are checked on the host first: a CPU tensor,
+    a strided last dimension or too few elements raise before any launch."""
+    import torch
+    from pyhub_gb300 import _capi
+    with pytest.raises(ValueError, match="CUDA tensor"):
+        _capi._ptr(torch.zeros(8), 4, "x")
+    assert _capi._ptr(None) is None
