@@ -310,26 +310,31 @@ def sweep(clusters, nsteps: int = 150, chunk: int = 64, dtype=None, gs_steps: in
     rows_used = []
     for c0 in range(0, len(clusters), chunk):
         cl = clusters[c0:c0 + chunk]
-        secs, inst, srcs = [], [], []
+        secs, inst = [], []
         base = []
         t0 = time.perf_counter()
+        # the five sectors of every cluster (ground state and the four N+-1 sectors), built on
+        # host threads: the table construction runs in the library with the GIL released
+        shapes = []
+        for spec in cl:
+            N = spec["N"]
+            shapes.append([(N, N), (N + 1, N), (N - 1, N), (N, N + 1), (N, N - 1)])
+        built = _build_sectors([(spec, key) for spec, keys in zip(cl, shapes) for key in keys])
+        srcs = []
         for ci, spec in enumerate(cl):
             norb = spec["t"].shape[0]
             N = spec["N"]
-            U = np.full(norb, spec["U"])
-            srcs.append(_capi.Sector(norb, N, N, _capi.ED_HUBBARD, t=spec["t"], U=U))
-            cache = {}
+            own = dict(zip(shapes[ci], built[5 * ci: 5 * ci + 5]))
+            srcs.append(own[(N, N)])
             base.append(len(inst))
             # instance order inside a cluster: spin (up, down) x part (greater, lesser) x site
             for spin in ("up", "down"):
                 for part in ("greater", "lesser"):
                     d = 1 if part == "greater" else -1
                     key = (N + d, N) if spin == "up" else (N, N + d)
-                    if key not in cache:
-                        cache[key] = _capi.Sector(norb, key[0], key[1], _capi.ED_HUBBARD, t=spec["t"], U=U)
                     for site in range(1, norb + 1):
                         inst.append((ci, spin, part, site))
-                        secs.append(cache[key])
+                        secs.append(own[key])
         gsb = batched_ground_states(srcs, nsteps=gs_steps, tol=gs_tol, seed=c0)
         restarts = max(restarts, gsb.restarts)
         torch.cuda.synchronize()
@@ -364,12 +369,29 @@ def sweep(clusters, nsteps: int = 150, chunk: int = 64, dtype=None, gs_steps: in
         t_lz += t3 - t2
         t_cf += t4 - t3
         n_inst += len(inst)
-        del bl, secs, srcs, gsb
+        del bl, secs, srcs, gsb, built
         torch.cuda.empty_cache()
     timings.update({"ground_states_s": t_gs, "start_vectors_s": t_start, "lanczos_s": t_lz, "cf_eval_s": t_cf,
                     "instances": n_inst, "total_s": t_gs + t_start + t_lz + t_cf, "gs_restarts": restarts,
                     "rows_per_cta": rows_used})
     return results
+
+
+def _build_sectors(jobs, workers: int = 8):
+    """Hubbard sectors for [(cluster spec, (N_up, N_down))], built concurrently
+    on host threads (each on the caller's current device)."""
+    torch = _torch()
+    from concurrent.futures import ThreadPoolExecutor
+    dev = torch.cuda.current_device()
+
+    def make(job):
+        spec, (nu, nd) = job
+        torch.cuda.set_device(dev)
+        norb = spec["t"].shape[0]
+        return _capi.Sector(norb, nu, nd, _capi.ED_HUBBARD, t=spec["t"], U=np.full(norb, spec["U"]))
+
+    with ThreadPoolExecutor(max_workers=workers) as ex:
+        return list(ex.map(make, jobs))
 
 
 def _cf_rows(alpha, beta, z, sign):

@@ -44,18 +44,20 @@ int num_sms()
 // ------------------------------------------------------------ combinatorics
 
 static int64_t g_binom[kMaxSites + 2][kMaxSites + 2];
-static bool g_binom_ready = false;
+static std::once_flag g_binom_once;
 
+// Sectors may be created from several host threads at once: the table is
+// filled exactly once.
 static void binom_init()
 {
-    if (g_binom_ready) return;
-    for (int n = 0; n <= kMaxSites + 1; ++n)
-        for (int k = 0; k <= kMaxSites + 1; ++k) {
-            if (k > n) g_binom[n][k] = 0;
-            else if (k == 0 || k == n) g_binom[n][k] = 1;
-            else g_binom[n][k] = g_binom[n - 1][k - 1] + g_binom[n - 1][k];
-        }
-    g_binom_ready = true;
+    std::call_once(g_binom_once, []() {
+        for (int n = 0; n <= kMaxSites + 1; ++n)
+            for (int k = 0; k <= kMaxSites + 1; ++k) {
+                if (k > n) g_binom[n][k] = 0;
+                else if (k == 0 || k == n) g_binom[n][k] = 1;
+                else g_binom[n][k] = g_binom[n - 1][k - 1] + g_binom[n - 1][k];
+            }
+    });
 }
 
 static inline int64_t binom(int n, int k)
