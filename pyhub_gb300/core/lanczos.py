@@ -427,6 +427,9 @@ class GroundState:
     ritz_vectors: np.ndarray = None
 
 
+REFINE_CHECK = 2   # steps between energy checks of the FP64 refinement
+
+
 def ground_state(sec, mode: str = "mixed", steps: int = 200, seed: int = 0, v0=None, rule=None,
                  refine_steps: int = 60, refine_tol: float = 1e-13, check_every: int = NADD,
                  timer: KernelTimer = None, reorth: str = "full", refine_rule=None) -> GroundState:
@@ -465,10 +468,12 @@ def ground_state(sec, mode: str = "mixed", steps: int = 200, seed: int = 0, v0=N
                            steps=r32.steps, refine_steps=0, converged=r32.converged, ndeg=r32.ndeg,
                            times={"total": t1 - t0, "fp32": r32.times["total"]}, mode=mode,
                            e0_unrefined=float(r32.ritz[0]), ritz_vectors=r32.ritz_vectors)
-    rr = refine_rule or EnergyRule(refine_tol * max(1.0, abs(float(r32.ritz[0]))), min_steps=2 * check_every)
+    # the FP64 stage starts from the FP32 Ritz vector and converges in a few steps: its energy
+    # is checked every REFINE_CHECK steps (two agreeing checks stop it)
+    rr = refine_rule or EnergyRule(refine_tol * max(1.0, abs(float(r32.ritz[0]))), min_steps=2 * REFINE_CHECK)
     psi32 = r32.psi
     r32.release()
-    r64 = lanczos_full(sec, psi32, refine_steps, torch.float64, rule=rr, check_every=check_every,
+    r64 = lanczos_full(sec, psi32, refine_steps, torch.float64, rule=rr, check_every=REFINE_CHECK,
                        timer=timer)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
