@@ -268,6 +268,102 @@ void orc_hprod_hubbard_ref_pairs(int norb, int nup, int ndn,
     }
 }
 
+/* orc_hprod_hubbard_ref_pairs on nthreads host threads (0: the OpenMP
+ * default), with the same results bit for bit.  For each pair:
+ *  1. the rank search of every string (the linear search of
+ *     hprod_hubbard.f90:41-47 and :97-103) is split over the threads;
+ *  2. the axpys run with each thread owning a block of output rows.  Every
+ *     thread walks the strings in the serial order and adds only into its own
+ *     rows, so each element of y receives its terms in the serial loop's order
+ *     (for one string the column term precedes the row term, as in the
+ *     reference's d loop).
+ * This is the reference loop with all host cores working on it; the
+ * arithmetic and the memory access pattern are the serial loop's. */
+void orc_hprod_hubbard_ref_pairs_mt(int norb, int nup, int ndn,
+                                    const uint32_t *bup, int64_t nsup,
+                                    const uint32_t *bdn, int64_t nsdn,
+                                    const double *t, const int32_t *pairs, int npairs,
+                                    const double *x, double *y, int nthreads)
+{
+    int64_t nmax = nsup > nsdn ? nsup : nsdn;
+    int64_t *pos = (int64_t *)malloc((size_t)nmax * sizeof(int64_t));
+    double *acs = (double *)malloc((size_t)nmax * sizeof(double));
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+    for (int q = 0; q < npairs; ++q) {
+        int J = pairs[2 * q], K = pairs[2 * q + 1];
+        double tjk = TF(t, norb, J, K);
+        if (!(fabs(tjk) >= TOL14)) continue;
+#pragma omp parallel for schedule(dynamic, 64)
+        for (int64_t u = 0; u < nsup; ++u) {
+            pos[u] = -1;
+            uint32_t nw = orc_kinop(norb, bup[u], J, K);
+            if (nw == 0) continue;
+            int64_t p = lin_rank(nw, bup, nsup);
+            if (p <= 0) continue;
+            pos[u] = p - 1;
+            acs[u] = orc_anticom(norb, J, bup[u]) * orc_anticom(norb, K, nw);
+        }
+#pragma omp parallel
+        {
+            int nt = omp_get_num_threads(), id = omp_get_thread_num();
+            int64_t r0 = nsdn * id / nt, r1 = nsdn * (id + 1) / nt;
+            for (int64_t u = 0; u < nsup; ++u) {
+                int64_t p = pos[u];
+                if (p < 0) continue;
+                double ac = acs[u];
+                for (int64_t d = r0; d < r1; ++d)
+                    y[d * nsup + p] = y[d * nsup + p] + ac * x[d * nsup + u] * tjk;
+                if (nup == ndn && p >= r0 && p < r1)
+                    for (int64_t d = 0; d < nsdn; ++d)
+                        y[p * nsup + d] = y[p * nsup + d] + ac * x[u * nsup + d] * tjk;
+            }
+        }
+        if (nup != ndn) {
+#pragma omp parallel for schedule(dynamic, 64)
+            for (int64_t d = 0; d < nsdn; ++d) {
+                pos[d] = -1;
+                uint32_t nw = orc_kinop(norb, bdn[d], J, K);
+                if (nw == 0) continue;
+                int64_t p = lin_rank(nw, bdn, nsdn);
+                if (p <= 0) continue;
+                pos[d] = p - 1;
+                acs[d] = orc_anticom(norb, J, bdn[d]) * orc_anticom(norb, K, nw);
+            }
+#pragma omp parallel
+            {
+                int nt = omp_get_num_threads(), id = omp_get_thread_num();
+                int64_t r0 = nsdn * id / nt, r1 = nsdn * (id + 1) / nt;
+                for (int64_t d = 0; d < nsdn; ++d) {
+                    int64_t p = pos[d];
+                    if (p < r0 || p >= r1) continue;
+                    double ac = acs[d];
+                    for (int64_t u = 0; u < nsup; ++u)
+                        y[p * nsup + u] = y[p * nsup + u] + ac * x[d * nsup + u] * tjk;
+                }
+            }
+        }
+    }
+    free(pos);
+    free(acs);
+}
+
+/* The on-site U part of the reference loop for site J on nthreads threads
+ * (each up string's column belongs to one thread; one term per element, so the
+ * result equals the serial loop's). */
+void orc_hprod_hubbard_ref_udiag_mt(int norb, const uint32_t *bup, int64_t nsup,
+                                    const uint32_t *bdn, int64_t nsdn, int J, double uj,
+                                    const double *x, double *y, int nthreads)
+{
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(static, 16)
+    for (int64_t u = 0; u < nsup; ++u) {
+        if (!is_part(norb, J, bup[u])) continue;
+        for (int64_t d = 0; d < nsdn; ++d)
+            if (is_part(norb, J, bdn[d]))
+                y[d * nsup + u] = y[d * nsup + u] + x[d * nsup + u] * uj;
+    }
+}
+
 /* The on-site U part of the reference loop for one site J only
  * (hprod_hubbard.f90:27-35), adding into y: the bounded sample used with
  * orc_hprod_hubbard_ref_pairs to time the reference loop on large sectors. */

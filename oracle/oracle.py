@@ -74,6 +74,8 @@ def lib():
             L.orc_hprod_hubbard_ref.argtypes = [i32, i32, i32, P, i64, P, i64, P, P, P, P]
             L.orc_hprod_hubbard_ref_pairs.argtypes = [i32, i32, i32, P, i64, P, i64, P, P, i32, P, P]
             L.orc_hprod_hubbard_ref_udiag.argtypes = [i32, P, i64, P, i64, i32, ctypes.c_double, P, P]
+            L.orc_hprod_hubbard_ref_pairs_mt.argtypes = [i32, i32, i32, P, i64, P, i64, P, P, i32, P, P, i32]
+            L.orc_hprod_hubbard_ref_udiag_mt.argtypes = [i32, P, i64, P, i64, i32, ctypes.c_double, P, P, i32]
             L.orc_hprod_hubbard_fast.argtypes = [i32, i32, i32, P, i64, P, i64, P, P, P, P, i32]
             L.orc_hprod_heis_ref.argtypes = [i32, P, i64, P, P, P]
             L.orc_hprod_heis_fast.argtypes = [i32, P, i64, P, P, P, i32]
@@ -150,18 +152,28 @@ def hprod_hubbard(sec: Sector, t, U, x, fast: bool = False, nthreads: int = 0) -
     return y
 
 
-def hprod_hubbard_pairs(sec: Sector, t, pairs, x, y) -> None:
-    """Reference loop restricted to the (J,K) pairs given (1-based), adds into y."""
+def hprod_hubbard_pairs(sec: Sector, t, pairs, x, y, nthreads: int = 1) -> None:
+    """Reference loop restricted to the (J,K) pairs given (1-based), adds into y.
+    nthreads > 1 (or 0: all cores) runs the same loop on host threads with the
+    same result bit for bit."""
     t = _f64(t)
     pr = np.ascontiguousarray(np.asarray(pairs, dtype=np.int32).reshape(-1, 2))
-    lib().orc_hprod_hubbard_ref_pairs(sec.norb, sec.nup, sec.ndn, _p(sec.bup), sec.nsup, _p(sec.bdn),
-                                      sec.nsdn, _p(t), _p(pr), len(pr), _p(x), _p(y))
+    if nthreads == 1:
+        lib().orc_hprod_hubbard_ref_pairs(sec.norb, sec.nup, sec.ndn, _p(sec.bup), sec.nsup, _p(sec.bdn),
+                                          sec.nsdn, _p(t), _p(pr), len(pr), _p(x), _p(y))
+    else:
+        lib().orc_hprod_hubbard_ref_pairs_mt(sec.norb, sec.nup, sec.ndn, _p(sec.bup), sec.nsup, _p(sec.bdn),
+                                             sec.nsdn, _p(t), _p(pr), len(pr), _p(x), _p(y), int(nthreads))
 
 
-def hprod_hubbard_udiag(sec: Sector, J: int, uj: float, x, y) -> None:
+def hprod_hubbard_udiag(sec: Sector, J: int, uj: float, x, y, nthreads: int = 1) -> None:
     """U term of the reference loop for site J (1-based) only, adds into y."""
-    lib().orc_hprod_hubbard_ref_udiag(sec.norb, _p(sec.bup), sec.nsup, _p(sec.bdn), sec.nsdn, int(J), float(uj),
-                                      _p(x), _p(y))
+    if nthreads == 1:
+        lib().orc_hprod_hubbard_ref_udiag(sec.norb, _p(sec.bup), sec.nsup, _p(sec.bdn), sec.nsdn, int(J),
+                                          float(uj), _p(x), _p(y))
+    else:
+        lib().orc_hprod_hubbard_ref_udiag_mt(sec.norb, _p(sec.bup), sec.nsup, _p(sec.bdn), sec.nsdn, int(J),
+                                             float(uj), _p(x), _p(y), int(nthreads))
 
 
 def heis_sector(norb: int) -> Sector:

@@ -114,6 +114,26 @@ def test_pair_sample_sums_to_full_product():
     assert np.allclose(y, full, rtol=0, atol=1e-13)
 
 
+@pytest.mark.parametrize("case", [(8, 4, 4), (9, 4, 3), (10, 3, 6)])
+def test_threaded_reference_loop_is_bit_identical(case):
+    """The host-threaded reference loop timed as the CPU baseline adds every
+    element's terms in the serial loop's order: equal bit for bit."""
+    norb, nu, nd = case
+    rng = np.random.default_rng(norb + nu)
+    t = rng.standard_normal((norb, norb))
+    t = 0.5 * (t + t.T)
+    sec = O.Sector(norb, nu, nd)
+    pairs = [(J, K) for J in range(1, norb + 1) for K in range(1, norb + 1) if J != K]
+    x = rng.standard_normal(sec.dim)
+    y1, y2 = np.zeros(sec.dim), np.zeros(sec.dim)
+    O.hprod_hubbard_pairs(sec, t, pairs, x, y1, nthreads=1)
+    O.hprod_hubbard_pairs(sec, t, pairs, x, y2, nthreads=5)
+    for J in range(1, norb + 1):
+        O.hprod_hubbard_udiag(sec, J, 1.5 + J, x, y1, nthreads=1)
+        O.hprod_hubbard_udiag(sec, J, 1.5 + J, x, y2, nthreads=3)
+    assert np.array_equal(y1, y2)
+
+
 @pytest.mark.parametrize("n", [2, 4, 6])
 def test_heisenberg_restatement_equals_jordan_wigner(n):
     rng = np.random.default_rng(n)
