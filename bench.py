@@ -281,8 +281,11 @@ def run_c4(args):
     clusters = GB.c4_clusters(args.clusters, seed=0)
     # every rank sweeps its own share of the clusters (no collective on the data path)
     mine = RP.shard(clusters, rank, ws)
+    # warm-up on one cluster of each filling: the batched H*v form is tuned there
+    # for every sector shape of the sweep (autotune keys on the distinct shapes)
+    warm = list({spec["N"]: spec for spec in reversed(mine)}.values())
     for _ in range(max(args.warmup, 1)):
-        GB.sweep(mine[:2], nsteps=150, chunk=2)
+        GB.sweep(warm, nsteps=150, chunk=len(warm))
     RP.barrier()
     clocks = ClockSampler(local)
     clocks.start()

@@ -36,9 +36,10 @@ def autotune(sectors, dtype, steps: int = 3, sample: int = 192, device="cuda"):
     (4, 8, 16) runs `steps` Lanczos steps (CUDA events on the current stream,
     after one untimed run) on an evenly spaced sample of at most `sample`
     instances, which keeps the batch's mix of sector shapes; the fastest is
-    kept and remembered for batches of the same shapes and dtype."""
+    kept and remembered for batches of the same set of distinct shapes and
+    dtype."""
     torch = _torch()
-    key = (str(dtype), tuple(sorted((s.nsup, s.nsdn) for s in sectors)))
+    key = (str(dtype), tuple(sorted({(s.nsup, s.nsdn) for s in sectors})))
     if key in _TUNED:
         return _TUNED[key]
     pick = [sectors[int(j)] for j in np.linspace(0, len(sectors) - 1, min(sample, len(sectors)))]
@@ -188,12 +189,12 @@ def batched_ground_states(sectors, nsteps: int = 120, tol: float = 1e-10, max_re
     torch = _torch()
     starts = [LZ.start_vector(sec, seed + i, dtype=torch.float64) for i, sec in enumerate(sectors)]
     if mixed:
-        b32 = BatchedLanczos(sectors, nsteps, dtype=torch.float32)
+        b32 = BatchedLanczos(sectors, nsteps, dtype=torch.float32, rows="auto")
         for i, v in enumerate(starts):
             b32.start(i).copy_(v)
         out32 = torch.zeros_like(b32.x0)
         _ritz_cycle(b32, out32)
-        bl = BatchedLanczos(sectors, refine_steps, dtype=torch.float64)
+        bl = BatchedLanczos(sectors, refine_steps, dtype=torch.float64, rows="auto")
         bl.x0.copy_(out32)
         del b32, out32
     else:

@@ -156,6 +156,7 @@ __global__ void batch_scalar_kernel(const BatchInst *__restrict__ inst, int nins
 
 constexpr int kMaxNb = 48;      // down-hop neighbours of a row staged in shared memory
 
+
 // 16-byte vectors: float4 / double2.
 template <typename T> struct V16;
 template <> struct V16<float> {
@@ -247,7 +248,7 @@ __device__ __forceinline__ void down_group(const NbEnt<T> *en, const T *__restri
 
 // y = s_k H u_k and partial <u_k, y> over R rows of one instance.
 // Phase A (diagonal + up hops): the rows are staged in shared memory one
-// column per string; a warp owns 32-string slices, loads each sliced-ELL
+// column per string (asynchronous copies, all in flight together); a warp owns 32-string slices, loads each sliced-ELL
 // slot once and applies it to all rows with 16-byte shared loads; the sums
 // go to y.  Phase B (down hops): each row adds its neighbour rows as
 // 16-byte-vector axpys read from L2 (the instances in flight keep their
@@ -282,7 +283,12 @@ __global__ void __launch_bounds__(kBatchThreads) batch_hv_kernel(const BatchInst
     const T *ded_t = (sizeof(T) == 4) ? reinterpret_cast<const T *>(a.dediag32) : reinterpret_cast<const T *>(a.dediag);
     for (int r = 0; r < R; ++r) {
         const T *src = ub + (int64_t)(r0 + r) * ld;
-        for (int c = threadIdx.x; c < nsup; c += blockDim.x) xs[c * S + r] = (r < nr) ? src[c] : (T)0;
+        for (int c = threadIdx.x; c < nsup; c += blockDim.x) {
+            if (r < nr)
+                cp_async_elem(xs + c * S + r, src + c);
+            else
+                xs[c * S + r] = (T)0;
+        }
     }
     for (int r = warp; r < R; r += nwarps) {
         int e0 = 0, nn = 0;
@@ -301,6 +307,7 @@ __global__ void __launch_bounds__(kBatchThreads) batch_hv_kernel(const BatchInst
             row_ed[r] = (r < nr) ? __ldg(ded_t + r0 + r) : (T)0;
         }
     }
+    cp_async_wait_all();
     __syncthreads();
     // ---- phase A
     for (int sl = warp; sl < a.nslice; sl += nwarps) {

@@ -156,6 +156,20 @@ namespace ed {
 
 // ------------------------------------------------------------ device helpers
 
+// Asynchronous global -> shared copy of one element (cp.async, 4 or 8 bytes):
+// a thread's copies are all in flight at once; cp_async_wait_all precedes the
+// barrier that publishes them to the CTA.
+template <typename T> __device__ __forceinline__ void cp_async_elem(T *smem, const T *gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    if constexpr (sizeof(T) == 4)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 __device__ __forceinline__ double warp_sum(double v)
 {
 #pragma unroll

@@ -348,7 +348,8 @@ __global__ void __launch_bounds__(kHeisRowThreads, 4) heis_row_kernel(const T *_
         const T db = __ldg(static_cast<const T *>(a.diagB) + row);
         const uint32_t rbits = a.ab_fast ? __ldg(a.row_bbits + row) : 0u;
         __syncthreads();   // the previous row's readers are done with xs / ab_*
-        for (int c = threadIdx.x; c < len; c += blockDim.x) xs[c] = x[off + c];
+        // asynchronous copies: the whole row in flight at once
+        for (int c = threadIdx.x; c < len; c += blockDim.x) cp_async_elem(xs + c, x + off + c);
         for (int q = threadIdx.x; q < a.nab; q += blockDim.x) {
             const uint32_t hk = (hb >> a.ab_pb[q]) & 1u;
             // the flip needs the A site opposite to the B site: hj = 1 - hk
@@ -359,6 +360,7 @@ __global__ void __launch_bounds__(kHeisRowThreads, 4) heis_row_kernel(const T *_
             ab_dsame[q] = (T)a.ab_zz[q];
             ab_w2[q] = (T)(2.0 * a.ab_zz[q]);
         }
+        cp_async_wait_all();
         __syncthreads();
         const int nsl = (len + 31) / 32;
         for (int sl = warp; sl < nsl; sl += nwarps) {
