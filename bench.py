@@ -66,7 +66,9 @@ def parse():
     p.add_argument("--lattice", default="4x8", help="c3: periodic LXxLY lattice (default 4x8)")
     p.add_argument("--fd-params", type=int, default=8, help="c5: parameters checked by central differences")
     p.add_argument("--probe", action="store_true",
-                   help="a few launches of each solve kernel on 4x4-sized vectors (about 4 GB), for profilers")
+                   help="for profilers: c2, a few launches of each solve kernel on 4x4-sized vectors (about "
+                        "4 GB); c4, two 3-step batched FP32 Lanczos runs (8 rows per CTA) over the particle/hole "
+                        "instances of --clusters clusters")
     return p.parse_args()
 
 
@@ -261,6 +263,29 @@ def probe(sec, torch, LZ, capi):
         capi.update(V, nv, coef, y, y, norm2=nrm, scratch=sc)
     torch.cuda.synchronize()
     print(json.dumps({"probe": "ok", "dim": sec.dim, "dots": out.cpu().tolist()[:2]}))
+
+
+def probe_c4(args):
+    """Two 3-step FP32 batched Lanczos runs (8 rows per CTA, fused form) over
+    the 48 particle/hole instances of each of the first --clusters C4
+    clusters: the launches profiled under ncu (6 H*v launches per run)."""
+    import numpy as np
+    import torch
+    from pyhub_gb300 import _build, _capi
+    from pyhub_gb300.core import greens_batched as GB
+    _build.build()
+    secs = []
+    for spec in GB.c4_clusters(args.clusters, seed=0):
+        N = spec["N"]
+        for key in [(N + 1, N), (N - 1, N), (N, N + 1), (N, N - 1)]:
+            s = _capi.Sector(12, key[0], key[1], _capi.ED_HUBBARD, t=spec["t"], U=np.full(12, spec["U"]))
+            secs += [s] * 12
+    bl = GB.BatchedLanczos(secs, 3, dtype=torch.float32, rows=8)
+    bl.x0.copy_(torch.rand(bl.batch.total, dtype=torch.float32, device="cuda"))
+    for _ in range(2):
+        bl.run()
+    torch.cuda.synchronize()
+    print(json.dumps({"probe": "ok", "instances": len(secs), "elements": int(bl.batch.total)}))
 
 
 def run_c4(args):
@@ -522,7 +547,10 @@ def main():
         run_reference(args)
         return
     if args.config == "c4":
-        run_c4(args)
+        if args.probe:
+            probe_c4(args)
+        else:
+            run_c4(args)
         return
     if args.config == "c3":
         run_c3(args)
