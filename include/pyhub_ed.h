@@ -115,6 +115,42 @@ int ed_update(void *stream, int dtype, int out_dtype, int64_t n, const void *V, 
               const double *coef, const void *w, void *out, double *norm2,
               void *scratch, int64_t scratch_bytes);
 
+/* ed_update with the w term scaled by a device scalar:
+ * out = wscale[0]*w - sum_j coef[j] V_j (wscale: device FP64, read by the
+ * kernel; NULL means 1, which is ed_update).  Lets a Lanczos step scale H*v by
+ * a norm that only the device knows. */
+int ed_update_wscaled(void *stream, int dtype, int out_dtype, int64_t n, const void *V, int64_t ldv, int nvec,
+                      const double *coef, const double *wscale, const void *w, void *out, double *norm2,
+                      void *scratch, int64_t scratch_bytes);
+
+/* Scalar work of step k of the full-reorthogonalisation Lanczos, on the
+ * device, so that a step needs no host synchronisation (the reference forms
+ * alpha and beta on the host, lanczos.f90:50-58, and has no
+ * reorthogonalisation).  One step is
+ *   ed_hv(u_k -> w, scale 1);  ed_multidot(V, k+1, w, z = u_k -> dots);
+ *   ed_lanczos_coef(k, ...);
+ *   ed_update_wscaled(V, k+1, coef, wscale = &state[2+k], w -> u_{k+1}, norm2 -> nrm)
+ * with V_j = u_j the unnormalised basis, s_j = 1/||u_j|| and G the Gram matrix
+ * of the normalised stored vectors, solved through its inverse Cholesky
+ * factor, which grows by one row per step.
+ * state: device FP64 array of ed_lanczos_state_doubles(mmax) entries, zeroed
+ *   before step 0 except state[2] = 1/||u_0||:
+ *   [0] stop code: 0 running, j > 0 breakdown (beta_{j-1} <= 1e-13 max(1,|alpha_{j-1}|),
+ *       j steps done), -j a non-finite norm after j steps;
+ *   [1] largest |G - I| entry seen;  [2 .. 2+mmax] s_0 .. s_mmax;
+ *   then the inverse Cholesky factor, (mmax+1)^2 entries, row-major, and
+ *   four work vectors of mmax+1 entries.
+ * dots: [2(k+1)] from the multidot (a_j = <u_j, w>, b_j = <u_j, u_k>); NULL
+ *   only closes step k-1 (beta[k-1], s_k and the stop test), as needed after
+ *   the last step.
+ * nrm: device ||u_k||^2 from the update of step k-1 (ignored at k = 0).
+ * Writes alpha[k] = <v_k, H v_k>, beta[k-1] = ||u_k|| (k >= 1; device FP64,
+ * mmax entries each) and coef[0..k].  After a stop, coef is zeros and the
+ * vectors that follow are zero.  mmax <= 8192. */
+int64_t ed_lanczos_state_doubles(int mmax);
+int ed_lanczos_coef(void *stream, int k, int mmax, const double *dots, const double *nrm, double *state,
+                    double *coef, double *alpha, double *beta);
+
 /* Device scratch bytes needed by ed_rdm for npairs site pairs. */
 int64_t ed_rdm_scratch_bytes(int npairs);
 

@@ -46,6 +46,9 @@ _SIGS = {
     "ed_batch_ritz": (_I, [_P, _P, _I, _P, _P, _I, _P, _P, _P, _P, _P, _I64]),
     "ed_batch_create_rows": (_I, [_I, _P, _I, ctypes.POINTER(_P)]),
     "ed_batch_rows": (_I, [_P]),
+    "ed_update_wscaled": (_I, [_P, _I, _I, _I64, _P, _I64, _I, _P, _P, _P, _P, _P, _P, _I64]),
+    "ed_lanczos_state_doubles": (_I64, [_I]),
+    "ed_lanczos_coef": (_I, [_P, _I, _I, _P, _P, _P, _P, _P, _P]),
 }
 
 GF_KINDS = {"h_up": 0, "h_down": 1, "e_up": 2, "e_down": 3}
@@ -354,13 +357,37 @@ def multidot(V, nvec: int, w, out, scratch, z=None, n: int | None = None, stream
                                            _ptr(scratch), int(sb)))
 
 
-def update(V, nvec: int, coef, w, out, norm2=None, scratch=None, n: int | None = None, stream=None):
-    """out = w - sum_j coef_j V_j (w may be None), optional <out,out> into norm2."""
+def update(V, nvec: int, coef, w, out, norm2=None, scratch=None, n: int | None = None, stream=None, wscale=None):
+    """out = ws w - sum_j coef_j V_j (w may be None), optional <out,out> into
+    norm2; ws = wscale[0] (a device FP64 scalar, read on the device) or 1."""
     n = out.numel() if n is None else n
     ldv = V.stride(0) if (V is not None and V.dim() > 1) else n
     sb = 0 if scratch is None else scratch.numel() * scratch.element_size()
     vdt = dtype_code(V.dtype) if V is not None else dtype_code(out.dtype)
     needV = (int(nvec) - 1) * int(ldv) + int(n) if (V is not None and int(nvec) > 0) else None
-    check("ed_update", lib().ed_update(_stream(stream), vdt, dtype_code(out.dtype), int(n), _ptr(V, needV, "V"),
-                                       int(ldv), int(nvec), _ptr(coef, int(nvec), "coef"), _ptr(w, n, "w"),
-                                       _ptr(out, n, "out"), _ptr(norm2, 1, "norm2"), _ptr(scratch), int(sb)))
+    if wscale is not None:
+        import torch
+        if wscale.dtype != torch.float64:
+            raise TypeError("wscale must be an FP64 device tensor")
+    check("ed_update_wscaled", lib().ed_update_wscaled(
+        _stream(stream), vdt, dtype_code(out.dtype), int(n), _ptr(V, needV, "V"), int(ldv), int(nvec),
+        _ptr(coef, int(nvec), "coef"), _ptr(wscale, 1, "wscale"), _ptr(w, n, "w"), _ptr(out, n, "out"),
+        _ptr(norm2, 1, "norm2"), _ptr(scratch), int(sb)))
+
+
+def lanczos_state_doubles(mmax: int) -> int:
+    """FP64 entries of the device state of ed_lanczos_coef for up to mmax steps."""
+    v = int(lib().ed_lanczos_state_doubles(int(mmax)))
+    if v < 0:
+        raise ValueError(f"no Lanczos state for {mmax} steps (1..8192)")
+    return v
+
+
+def lanczos_coef(k: int, mmax: int, dots, nrm, state, coef, alpha, beta, stream=None):
+    """Scalar work of step k of the full-reorthogonalisation Lanczos on the
+    device (ed_lanczos_coef); dots=None only closes step k-1 (beta, scale)."""
+    k, mmax = int(k), int(mmax)
+    check("ed_lanczos_coef", lib().ed_lanczos_coef(
+        _stream(stream), k, mmax, _ptr(dots, 2 * (k + 1), "dots"), _ptr(nrm, 1, "nrm"),
+        _ptr(state, lanczos_state_doubles(mmax), "state"), _ptr(coef, k + 1, "coef"),
+        _ptr(alpha, mmax, "alpha"), _ptr(beta, mmax, "beta")))

@@ -167,13 +167,16 @@ class CoreSolver(Basis, GreenFunction, StaticQuantities):
                 ritz, alpha, beta, steps_done, conv = r.ritz, r.alpha, r.beta, r.steps, r.converged
                 r.release()
             else:
-                r = LZ.lanczos_full(sec, v0.to(torch.float32), steps, torch.float32, rule=rule)
+                # mixed: the FP32 Ritz vector only starts the FP64 stage, so it is summed in FP32
+                r = LZ.lanczos_full(sec, v0.to(torch.float32), steps, torch.float32, rule=rule,
+                                    ritz_dtype=torch.float32 if dtype == "mixed" else None)
                 e32 = float(r.ritz[0])
                 psi = r.psi
                 r.release()
                 if dtype == "mixed":
-                    rr = LZ.EnergyRule(1e-13 * max(1.0, abs(e32)), min_steps=10)
-                    r2 = LZ.lanczos_full(sec, psi, refine_steps, torch.float64, rule=rr)
+                    # the FP64 stage as in lanczos.ground_state: energy checked every REFINE_CHECK steps
+                    rr = LZ.EnergyRule(1e-13 * max(1.0, abs(e32)), min_steps=2 * LZ.REFINE_CHECK)
+                    r2 = LZ.lanczos_full(sec, psi, refine_steps, torch.float64, rule=rr, check_every=LZ.REFINE_CHECK)
                     psi = r2.psi
                     ritz = np.concatenate([[r2.ritz[0]], r.ritz[1:]])
                     r2.release()

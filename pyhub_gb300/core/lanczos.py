@@ -169,7 +169,7 @@ class KernelTimer:
     algorithmic bytes and kernel launches per call; read after a
     synchronize."""
 
-    LAUNCHES = {"hv": 3, "multidot": 2, "update": 2}
+    LAUNCHES = {"hv": 3, "multidot": 2, "coef": 1, "update": 2, "ritz": 2}
 
     def __init__(self):
         self.ev = {}
@@ -210,20 +210,31 @@ class _Scratch:
 
 def lanczos_full(sec, v0, max_steps: int, dtype=None, rule=None, check_every: int = NADD,
                  min_steps: int = 0, want_vector: bool = True, vec_index: int = 0,
-                 keep_basis: bool = False, timer: KernelTimer = None) -> KrylovResult:
+                 keep_basis: bool = False, timer: KernelTimer = None, ritz_dtype=None) -> KrylovResult:
     """Lanczos with full reorthogonalisation (delayed CGS with the exact Gram
     matrix).  v0: start vector (device tensor, internal layout).  The basis
     of max_steps+1 vectors is stored in ``dtype`` (FP32 or FP64); scalars are
     FP64.  Stops after max_steps, on breakdown, or when ``rule`` is met at a
     check.  Returns the tridiagonal, its eigenpairs and (optionally) the Ritz
-    vector ``vec_index`` as an FP64 device tensor."""
+    vector ``vec_index`` as a device tensor of ``ritz_dtype`` (default FP64;
+    FP32 from an FP32 basis sums in FP32, at the HBM rate, where an FP64 sum
+    is bound by the FP64 pipe).
+
+    A step is four enqueued calls with no host synchronisation: the H*v, the
+    multi-dot of the basis with H u_k and u_k, the scalar work on the device
+    (ed_lanczos_coef: Gram row, inverse Cholesky row, projection
+    coefficients, alpha, beta) and the update, which scales H u_k by s_k on
+    the device.  The host reads alpha/beta only at rule checks and at the end."""
     torch = _torch()
     dtype = dtype or v0.dtype
     dev = v0.device
     n = sec.n
     m = int(max_steps)
     t_start = time.perf_counter()
-    V = torch.zeros((m + 1, n), dtype=dtype, device=dev)
+    # Row j of V is written (u_0 = v0, then u_{j} by the update of step j-1)
+    # before any call reads it, and keeps zero padding: v0 and w have zero
+    # padding, H*v leaves w's padding untouched, and the update combines them.
+    V = torch.empty((m + 1, n), dtype=dtype, device=dev)
     w = torch.zeros(n, dtype=dtype, device=dev)
     ws = _Scratch(n, m + 1, dev)
     V[0].copy_(v0)
@@ -231,87 +242,75 @@ def lanczos_full(sec, v0, max_steps: int, dtype=None, rule=None, check_every: in
     n0 = float(ws.dots[0].item())
     if not (n0 > 0.0 and math.isfinite(n0)):
         raise ValueError("start vector has zero or non-finite norm")
-    s = np.zeros(m + 2)
-    s[0] = 1.0 / math.sqrt(n0)
-    G = np.zeros((m + 2, m + 2))
-    G[0, 0] = s[0] * s[0] * n0
-    L = np.zeros((m + 2, m + 2))       # Cholesky factor of G, grown a row per step
-    alpha = np.zeros(m + 1)
-    beta = np.zeros(m + 1)
+    state = torch.zeros(_capi.lanczos_state_doubles(m), dtype=torch.float64, device=dev)
+    state[2] = 1.0 / math.sqrt(n0)
+    ab = torch.zeros((2, m), dtype=torch.float64, device=dev)   # alpha, beta
+    es = V.element_size()
     k_done = 0
     converged = breakdown = False
-    val = None
-    es = V.element_size()
+
+    def close(k):
+        """beta[k-1], s_k and the stop test of step k-1; host copies."""
+        _capi.lanczos_coef(k, m, None, ws.nrm, state, None, ab[0], ab[1])
+        hs = state[:2].cpu().numpy()
+        hab = ab[:, :k].cpu().numpy()
+        return int(hs[0]), float(hs[1]), hab[0].copy(), hab[1].copy()
+
     for k in range(m):
-        if timer is not None:
-            e = timer("hv", 2.0 * sec.dim * es)
-        # w = H v_k = s_k H u_k: every stored u_j keeps a norm of order ||H||
-        sec.hv(V[k], w, scale=float(s[k]))
-        if timer is not None:
+        e = timer("hv", 2.0 * sec.dim * es) if timer is not None else None
+        sec.hv(V[k], w)
+        if e is not None:
             e.record()
             e = timer("multidot", (k + 2) * sec.dim * es)
         _capi.multidot(V, k + 1, w, ws.dots, ws.buf, z=V[k])
-        if timer is not None:
+        if e is not None:
             e.record()
-        d = ws.dots[: 2 * (k + 1)].cpu().numpy()
-        a, b = d[: k + 1], d[k + 1:]
-        sv = s[: k + 1]
-        G[k, : k + 1] = sv * sv[k] * b
-        G[: k + 1, k] = G[k, : k + 1]
-        # grow the Cholesky factor by row k
-        if k == 0:
-            L[0, 0] = math.sqrt(G[0, 0])
-        else:
-            l = sla.solve_triangular(L[:k, :k], G[k, :k], lower=True, check_finite=False)
-            L[k, :k] = l
-            L[k, k] = math.sqrt(max(G[k, k] - float(l @ l), 1e-300))
-        c = sv * a                      # v_j . H v_k
-        y = sla.cho_solve((L[: k + 1, : k + 1], True), c, check_finite=False)
-        coef = y * sv                   # w - sum_j y_j v_j = w - sum_j (y_j s_j) u_j
-        ws.coef[: k + 1].copy_(torch.from_numpy(coef))
-        if timer is not None:
+            e = timer("coef", 0.0)
+        _capi.lanczos_coef(k, m, ws.dots, ws.nrm, state, ws.coef, ab[0], ab[1])
+        if e is not None:
+            e.record()
             e = timer("update", (k + 3) * sec.dim * es)
-        _capi.update(V, k + 1, ws.coef, w, V[k + 1], norm2=ws.nrm, scratch=ws.buf)
-        if timer is not None:
+        _capi.update(V, k + 1, ws.coef, w, V[k + 1], norm2=ws.nrm, scratch=ws.buf, wscale=state[2 + k: 3 + k])
+        if e is not None:
             e.record()
-        nw2 = float(ws.nrm[0].item())
-        alpha[k] = c[k]
-        bk = math.sqrt(max(nw2, 0.0))
-        beta[k] = bk
         k_done = k + 1
-        if not math.isfinite(nw2):
-            raise FloatingPointError(f"non-finite norm at Lanczos step {k}")
-        if bk <= 1e-13 * max(1.0, abs(alpha[k])):
-            breakdown = True
-        else:
-            s[k + 1] = 1.0 / math.sqrt(nw2)
-            G[k + 1, k + 1] = 1.0
-        if rule is not None and (k_done % check_every == 0 or breakdown) and k_done >= min_steps:
+        if rule is not None and k_done % check_every == 0 and k_done >= min_steps:
+            stop, _, alpha, beta = close(k_done)
+            if stop != 0:
+                break
             if getattr(rule, "wants_vectors", False):
                 val, vecs_t = _tridiag_eigs(alpha, beta, k_done, vectors=True)
-                stop = rule(val, k_done, vec=vecs_t, beta_last=beta[k_done - 1])
+                ok = rule(val, k_done, vec=vecs_t, beta_last=beta[k_done - 1])
             else:
                 val = _tridiag_eigs(alpha, beta, k_done)
-                stop = rule(val, k_done)
-            if stop:
+                ok = rule(val, k_done)
+            if ok:
                 converged = True
                 break
-        if breakdown:
-            converged = True
-            break
+    stop, gram_off, alpha, beta = close(k_done)
+    if stop < 0:
+        raise FloatingPointError(f"non-finite norm at Lanczos step {-stop - 1}")
+    if stop > 0:
+        k_done = min(k_done, stop)
+        breakdown = converged = True
+        alpha, beta = alpha[:k_done], beta[:k_done]
+    s = state[2: 3 + k_done].cpu().numpy()
     t_loop = time.perf_counter()
     val, vec = _tridiag_eigs(alpha, beta, k_done, vectors=True)
     res = KrylovResult(alpha=alpha[:k_done].copy(), beta=beta[:k_done].copy(), ritz=val, ritz_vectors=vec,
                        steps=k_done, converged=converged, breakdown=breakdown,
                        ndeg=getattr(rule, "ndeg", 0) if rule is not None else 0)
-    gi = G[:k_done, :k_done] - np.eye(k_done)
-    res.gram_offdiag = float(np.abs(gi).max()) if k_done > 0 else 0.0
+    res.gram_offdiag = gram_off
     if want_vector:
         z = vec[:, vec_index]
         coef = -(z * s[:k_done])
         ws.coef[:k_done].copy_(torch.from_numpy(coef))
-        psi = torch.zeros(n, dtype=torch.float64, device=dev)
+        rdt = ritz_dtype or torch.float64
+        psi = torch.empty(n, dtype=rdt, device=dev)
+        e = timer("ritz", (k_done * es + psi.element_size()) * sec.dim) if timer is not None else None
         _capi.update(V, k_done, ws.coef, None, psi, norm2=ws.nrm, scratch=ws.buf)
+        if e is not None:
+            e.record()
         nrm = math.sqrt(float(ws.nrm[0].item()))
         psi.mul_(1.0 / nrm)
         res.psi = psi
@@ -460,8 +459,10 @@ def ground_state(sec, mode: str = "mixed", steps: int = 200, seed: int = 0, v0=N
                            refine_steps=0, converged=r.converged, ndeg=r.ndeg,
                            times={"total": time.perf_counter() - t0, "fp64": r.times["total"]}, mode=mode,
                            e0_unrefined=float(r.ritz[0]), ritz_vectors=r.ritz_vectors)
+    # in mixed mode the FP32 Ritz vector only starts the FP64 stage: its error is that of the
+    # FP32 Krylov space, far above the rounding of an FP32 sum
     r32 = lanczos_full(sec, v0.to(torch.float32), steps, torch.float32, rule=rule, check_every=check_every,
-                       timer=timer)
+                       timer=timer, ritz_dtype=torch.float32 if mode == "mixed" else None)
     t1 = time.perf_counter()
     if mode == "f32":
         return GroundState(e0=float(r32.ritz[0]), psi=r32.psi, ritz=r32.ritz, alpha=r32.alpha, beta=r32.beta,

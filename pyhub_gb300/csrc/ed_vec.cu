@@ -102,16 +102,19 @@ __global__ void __launch_bounds__(kVecThreads) multidot_kernel(int64_t n, const 
     }
 }
 
-// out = w - sum_j coef_j V_j (w may be NULL), optional partial <out,out>.
+// out = ws w - sum_j coef_j V_j (w may be NULL; ws = wscale[0], a device
+// scalar, or 1 when wscale is NULL), optional partial <out,out>.
 // Accumulation type A: FP32 for an FP32 basis with FP32 output, FP64 otherwise.
 template <typename T, typename O, typename A>
 __global__ void __launch_bounds__(kVecThreads) update_kernel(int64_t n, const T *__restrict__ V, int64_t ldv,
                                                              int nvec, const double *__restrict__ coef,
-                                                             const O *w, O *out, double *__restrict__ partials)
+                                                             const double *__restrict__ wscale, const O *w, O *out,
+                                                             double *__restrict__ partials)
 {
     extern __shared__ double cs_raw[];
     A *cs = reinterpret_cast<A *>(cs_raw);
     for (int j = threadIdx.x; j < nvec; j += blockDim.x) cs[j] = (A)coef[j];
+    const A ws = wscale ? (A)wscale[0] : (A)1;
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     double nrm = 0.0;
@@ -123,7 +126,7 @@ __global__ void __launch_bounds__(kVecThreads) update_kernel(int64_t n, const T 
             O rw[kEPT];
             load_chunk<O>(rw, w, base, n);
 #pragma unroll
-            for (int k = 0; k < kEPT; ++k) r[k] = (A)rw[k];
+            for (int k = 0; k < kEPT; ++k) r[k] = ws * (A)rw[k];
         } else {
 #pragma unroll
             for (int k = 0; k < kEPT; ++k) r[k] = (A)0;
@@ -224,9 +227,9 @@ extern "C" int ed_multidot(void *stream, int dtype, int64_t n, const void *V, in
     return launch_reduce(part, grid, m, out, st);
 }
 
-extern "C" int ed_update(void *stream, int dtype, int out_dtype, int64_t n, const void *V, int64_t ldv, int nvec,
-                         const double *coef, const void *w, void *out, double *norm2, void *scratch,
-                         int64_t scratch_bytes)
+extern "C" int ed_update_wscaled(void *stream, int dtype, int out_dtype, int64_t n, const void *V, int64_t ldv,
+                                 int nvec, const double *coef, const double *wscale, const void *w, void *out,
+                                 double *norm2, void *scratch, int64_t scratch_bytes)
 {
     clear_error();
     ED_REQUIRE(dtype == ED_F32 || dtype == ED_F64, "dtype must be ED_F32 or ED_F64");
@@ -253,24 +256,32 @@ extern "C" int ed_update(void *stream, int dtype, int out_dtype, int64_t n, cons
     const size_t smem = sizeof(double) * (size_t)(nvec > 0 ? nvec : 1);
     if (dtype == ED_F32 && out_dtype == ED_F32) {
         update_kernel<float, float, float><<<grid, kVecThreads, smem, st>>>(
-            n, static_cast<const float *>(V), ldv, nvec, coef, static_cast<const float *>(w),
+            n, static_cast<const float *>(V), ldv, nvec, coef, wscale, static_cast<const float *>(w),
             static_cast<float *>(out), part);
     } else if (dtype == ED_F32 && out_dtype == ED_F64) {
         update_kernel<float, double, double><<<grid, kVecThreads, smem, st>>>(
-            n, static_cast<const float *>(V), ldv, nvec, coef, static_cast<const double *>(w),
+            n, static_cast<const float *>(V), ldv, nvec, coef, wscale, static_cast<const double *>(w),
             static_cast<double *>(out), part);
     } else if (dtype == ED_F64 && out_dtype == ED_F64) {
         update_kernel<double, double, double><<<grid, kVecThreads, smem, st>>>(
-            n, static_cast<const double *>(V), ldv, nvec, coef, static_cast<const double *>(w),
+            n, static_cast<const double *>(V), ldv, nvec, coef, wscale, static_cast<const double *>(w),
             static_cast<double *>(out), part);
     } else {
         update_kernel<double, float, double><<<grid, kVecThreads, smem, st>>>(
-            n, static_cast<const double *>(V), ldv, nvec, coef, static_cast<const float *>(w),
+            n, static_cast<const double *>(V), ldv, nvec, coef, wscale, static_cast<const float *>(w),
             static_cast<float *>(out), part);
     }
     ED_CHECK_LAUNCH();
     if (norm2) return launch_reduce(part, grid, 1, norm2, st);
     return ED_OK;
+}
+
+extern "C" int ed_update(void *stream, int dtype, int out_dtype, int64_t n, const void *V, int64_t ldv, int nvec,
+                         const double *coef, const void *w, void *out, double *norm2, void *scratch,
+                         int64_t scratch_bytes)
+{
+    return ed_update_wscaled(stream, dtype, out_dtype, n, V, ldv, nvec, coef, nullptr, w, out, norm2, scratch,
+                             scratch_bytes);
 }
 
 // ---------------------------------------------------------------------------
