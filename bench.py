@@ -439,7 +439,8 @@ def run_c3(args):
                 "residual_fp64": res, "fp32_steps": int(gs.steps), "refine_steps": int(gs.refine_steps),
                 "nn_smatrix_mean": float(np.mean(sij)), "nn_sisj_energy_gauge_mean": float(np.mean(raw[:, 1] - raw[:, 0])),
                 "bond_energy_identity_err": gs.e0 - e_bonds,
-                "times_s": {k: float(v) for k, v in gs.times.items()}, "sector_create_s": t_sector,
+                "times_s": {k: (v if isinstance(v, bool) else float(v)) for k, v in gs.times.items()},
+                "sector_create_s": t_sector,
                 "hv_ms": hv_ms,
                 "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
                              "traffic": None, "kernel": "structured Heisenberg H*v (FP32), x read + y written",

@@ -186,15 +186,21 @@ class CoreSolver(Basis, GreenFunction, StaticQuantities):
                 alpha, beta, steps_done, conv = r.alpha, r.beta, r.steps, r.converged
         else:
             vt = torch.float64 if dtype == "f64" else torch.float32
-            r = LZ.lanczos_plain(sec, v0.to(vt), steps, rule=rule, nvec=nvec)
+            # the Krylov rows are kept where they fit (one block shared by both stages),
+            # else the Ritz vectors are rebuilt by a second run
+            storage = LZ.kept_storage(v0.device, max((steps + 1) * sec.n * (8 if dtype == "f64" else 4),
+                                                     (refine_steps + 1) * sec.n * 8 if dtype == "mixed" else 0),
+                                      min_bytes=4 * sec.n * 8)
+            r = LZ.lanczos_plain(sec, v0.to(vt), steps, rule=rule, nvec=nvec, storage=storage)
             psis = r.psis
             ritz, alpha, beta, steps_done, conv = r.ritz, r.alpha, r.beta, r.steps, r.converged
             if dtype == "mixed":
-                # FP64 three-term refinement from the FP32 Ritz vector (memory: four vectors)
+                # FP64 three-term refinement from the FP32 Ritz vector
                 rr = LZ.EnergyRule(1e-13 * max(1.0, abs(float(ritz[0]))), min_steps=10)
-                r2 = LZ.lanczos_plain(sec, psis[0], refine_steps, rule=rr, nvec=1)
+                r2 = LZ.lanczos_plain(sec, psis[0], refine_steps, rule=rr, nvec=1, storage=storage)
                 psis = [r2.psis[0]] + list(psis[1:])
                 ritz = np.concatenate([[r2.ritz[0]], ritz[1:]])
+            del storage
         return {"eigenvalues": np.asarray(ritz), "psis": psis, "is_lanczos": True, "deg": rule.ndeg,
                 "alpha": alpha, "beta": beta, "nb_lcz": steps_done, "conv": rule.conv,
                 "converged": conv, "H": None, "nstates": sec.dim, "precision": dtype, "reorth": reorth}

@@ -335,45 +335,111 @@ class PlainResult:
     times: dict
 
 
+def kept_storage(dev, need: int, frac: float = 0.85, min_bytes: int = 1 << 20):
+    """One device byte block for the kept Krylov rows of lanczos_plain: need
+    bytes, or ``frac`` of the free memory if less (None if not even min_bytes
+    can be had).  Stages that run one after the other (FP32, then FP64
+    refinement) share one block: the caching allocator would otherwise split
+    the large cached block of the first stage with vectors that outlive it,
+    and the second stage could not get one."""
+    torch = _torch()
+    # first from the driver's free memory plus what the allocator holds unused (a block a
+    # previous solve left cached is reused as it is); failing that, with the cache returned
+    free = torch.cuda.mem_get_info(dev)[0]
+    cached = torch.cuda.memory_reserved(dev) - torch.cuda.memory_allocated(dev)
+    nbytes = min(int(need), int(frac * (free + cached))) // 256 * 256
+    if nbytes >= min_bytes:
+        try:
+            return torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        except torch.OutOfMemoryError:
+            pass
+    torch.cuda.empty_cache()
+    nbytes = min(int(need), int(frac * torch.cuda.mem_get_info(dev)[0])) // 256 * 256
+    while nbytes >= min_bytes:
+        try:
+            return torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        except torch.OutOfMemoryError:
+            nbytes = nbytes // 2 // 256 * 256
+    return None
+
+
 def lanczos_plain(sec, v0, max_steps: int, rule=None, check_every: int = NADD, nvec: int = 1,
-                  want_vectors: bool = True) -> PlainResult:
+                  want_vectors: bool = True, keep: bool = True, ritz_dtype=None, storage=None) -> PlainResult:
     """The reference's three-term recurrence without reorthogonalisation
-    (lanczos.f90:52-58) on three device vectors, alpha fused into the H*v
-    pass.  Ritz vectors are rebuilt by running the same (deterministic)
-    recurrence a second time and accumulating sum_k z_k v_k in FP64, instead
-    of storing every Krylov vector as the reference does (lanczos.f90:42-49)."""
+    (lanczos.f90:52-58), alpha fused into the H*v pass.
+
+    Ritz vectors: the reference stores every Krylov vector (in HDF5,
+    lanczos.f90:42-49) and sums them.  Here, when the whole run fits in the
+    free device memory (keep=True), the recurrence runs on rows of a kept
+    basis and each Ritz vector is one update pass over it (summed in
+    ``ritz_dtype``, FP64 by default).  Otherwise (or keep=False) the run uses
+    three rotating vectors and the Ritz vectors are rebuilt by running the same
+    deterministic recurrence a second time, accumulating sum_k z_k v_k in FP64.
+    An integer ``keep`` caps the kept rows: a run longer than that moves to
+    the rotating vectors when the rows run out and rebuilds by replay.
+    ``storage`` (a device uint8 block, see kept_storage) holds the kept rows;
+    without it a block of the free memory is taken for this call."""
     torch = _torch()
     dev = v0.device
     n = sec.n
     m = int(max_steps)
     t0 = time.perf_counter()
-    ws = _Scratch(n, 4, dev)
+    ws = _Scratch(n, max(4, nvec), dev)
     R = torch.zeros((3, n), dtype=v0.dtype, device=dev)
+    t_alloc = time.perf_counter()
+    V = None
+    if want_vectors and keep:
+        es = v0.element_size()
+        if storage is None:
+            storage = kept_storage(dev, (m + 1) * n * es, min_bytes=4 * n * es)
+        cap = 0 if storage is None else min(m + 1, storage.numel() // (n * es))
+        if not isinstance(keep, bool):
+            cap = min(cap, int(keep))
+        if cap >= 4:
+            V = storage[: cap * n * es].view(v0.dtype).view(cap, n)
+            if n != sec.dim:
+                V.zero_()   # the H*v leaves row padding untouched: padded layouts start at zero
+    cap = 0 if V is None else V.shape[0]
+    t_alloc = time.perf_counter() - t_alloc
 
     def run(steps, z=None, psis=None):
+        # a replay (psis given) follows the first run's schedule of kept rows and rotating
+        # vectors, so that it recomputes the same vectors bit for bit
+        kept = V is not None
         R.zero_()
-        R[0].copy_(v0)
-        _capi.multidot(R, 1, R[0], ws.dots, ws.buf)
+        if kept:
+            V[0].copy_(v0)
+        else:
+            R[0].copy_(v0)
+        _capi.multidot(R if not kept else V, 1, v0, ws.dots, ws.buf)
         s_prev, s_cur = 0.0, 1.0 / math.sqrt(float(ws.dots[0].item()))
-        alpha, beta = [], []
+        alpha, beta, scales = [], [], [s_cur]
         bprev = 0.0
         done = 0
         conv = False
         for k in range(steps):
-            cur, nxt, prv = k % 3, (k + 1) % 3, (k + 2) % 3
+            if kept and k + 1 >= cap:
+                # the kept rows are used up: continue on the rotating vectors
+                R[(k + 2) % 3].copy_(V[k - 1])
+                R[k % 3].copy_(V[k])
+                kept = False
+            if kept:
+                W, cur, nxt, prv = (V[0:2], 0, 1, None) if k == 0 else (V[k - 1:k + 2], 1, 2, 0)
+            else:
+                W, cur, nxt, prv = R, k % 3, (k + 1) % 3, (k + 2) % 3
             if psis is not None:
                 for j, p in enumerate(psis):
                     ws.coef[0] = -z[k, j] * s_cur
-                    _capi.update(R[cur:cur + 1], 1, ws.coef, p, p)
-            # R[nxt] = H v_k with v_k = s_cur u_k; dots[0] = <u_k, H v_k>
-            sec.hv(R[cur], R[nxt], scale=s_cur, dots=ws.dots, scratch=ws.buf)
+                    _capi.update(W[cur:cur + 1], 1, ws.coef, p, p)
+            # W[nxt] = H v_k with v_k = s_cur u_k; dots[0] = <u_k, H v_k>
+            sec.hv(W[cur], W[nxt], scale=s_cur, dots=ws.dots, scratch=ws.buf)
             a = s_cur * float(ws.dots[0].item())
-            coef = np.zeros(3)
+            coef = np.zeros(W.shape[0])
             coef[cur] = a * s_cur
             if k > 0:
                 coef[prv] = bprev * s_prev
-            ws.coef[:3].copy_(torch.from_numpy(coef))
-            _capi.update(R, 3, ws.coef, R[nxt], R[nxt], norm2=ws.nrm, scratch=ws.buf)
+            ws.coef[: W.shape[0]].copy_(torch.from_numpy(coef))
+            _capi.update(W, W.shape[0], ws.coef, W[nxt], W[nxt], norm2=ws.nrm, scratch=ws.buf)
             nw2 = float(ws.nrm[0].item())
             b = math.sqrt(max(nw2, 0.0))
             alpha.append(a)
@@ -385,6 +451,7 @@ def lanczos_plain(sec, v0, max_steps: int, rule=None, check_every: int = NADD, n
                 conv = True
                 break
             s_prev, s_cur, bprev = s_cur, 1.0 / math.sqrt(nw2), b
+            scales.append(s_cur)
             if psis is None and rule is not None and done % check_every == 0:
                 if getattr(rule, "wants_vectors", False):
                     val, vec = _tridiag_eigs(np.array(alpha), np.array(beta), done, vectors=True)
@@ -394,19 +461,31 @@ def lanczos_plain(sec, v0, max_steps: int, rule=None, check_every: int = NADD, n
                 if stop:
                     conv = True
                     break
-        return np.array(alpha), np.array(beta), done, conv
+        return np.array(alpha), np.array(beta), done, conv, (np.array(scales) if kept else None)
 
-    alpha, beta, done, conv = run(m)
+    alpha, beta, done, conv, scales = run(m)    # scales is None when the kept rows ran out
     val, vec = _tridiag_eigs(alpha, beta, done, vectors=True)
     psis = []
     if want_vectors:
-        psis = [torch.zeros(n, dtype=torch.float64, device=dev) for _ in range(min(nvec, done))]
-        run(done, z=vec[:, : len(psis)], psis=psis)
-        for p in psis:
-            _capi.multidot(p.view(1, -1), 1, p, ws.dots, ws.buf)
-            p.mul_(1.0 / math.sqrt(float(ws.dots[0].item())))
+        nv = min(nvec, done)
+        if scales is not None:
+            # u_0 .. u_{done-1} are rows of V: psi_j = sum_k z_kj s_k u_k in one pass each
+            rdt = ritz_dtype or torch.float64
+            for j in range(nv):
+                c = torch.from_numpy(-(vec[:, j] * scales[:done])).to(dev)
+                p = torch.empty(n, dtype=rdt, device=dev)
+                _capi.update(V, done, c, None, p, norm2=ws.nrm, scratch=ws.buf)
+                p.mul_(1.0 / math.sqrt(float(ws.nrm[0].item())))
+                psis.append(p)
+        else:
+            psis = [torch.zeros(n, dtype=torch.float64, device=dev) for _ in range(nv)]
+            run(done, z=vec[:, :nv], psis=psis)
+            for p in psis:
+                _capi.multidot(p.view(1, -1), 1, p, ws.dots, ws.buf)
+                p.mul_(1.0 / math.sqrt(float(ws.dots[0].item())))
     return PlainResult(alpha=alpha, beta=beta, ritz=val, ritz_vectors=vec, steps=done, converged=conv,
-                       psis=psis, times={"total": time.perf_counter() - t0})
+                       psis=psis, times={"total": time.perf_counter() - t0, "alloc": t_alloc, "kept_rows": cap,
+                                         "replayed": bool(want_vectors and scales is None)})
 
 
 @dataclass
@@ -488,7 +567,12 @@ def _ground_state_plain(sec, mode, steps, v0, rule, refine_steps, refine_tol, ch
                         refine_rule=None) -> GroundState:
     torch = _torch()
     vt = torch.float64 if mode == "f64" else torch.float32
-    r = lanczos_plain(sec, v0.to(vt), steps, rule=rule, check_every=check_every, nvec=1)
+    storage = kept_storage(v0.device, max((steps + 1) * sec.n * (8 if mode == "f64" else 4),
+                                          (refine_steps + 1) * sec.n * 8 if mode == "mixed" else 0),
+                           min_bytes=4 * sec.n * 8)
+    # mixed: the FP32 Ritz vector only starts the FP64 stage (summed in FP32 from a kept basis)
+    r = lanczos_plain(sec, v0.to(vt), steps, rule=rule, check_every=check_every, nvec=1,
+                      ritz_dtype=torch.float32 if mode == "mixed" else None, storage=storage)
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     e0u = float(r.ritz[0])
@@ -498,10 +582,16 @@ def _ground_state_plain(sec, mode, steps, v0, rule, refine_steps, refine_tol, ch
                            times={"total": t1 - t0, mode: t1 - t0}, mode=mode, e0_unrefined=e0u,
                            ritz_vectors=r.ritz_vectors)
     rr = refine_rule or EnergyRule(refine_tol * max(1.0, abs(e0u)), min_steps=2 * check_every)
-    r64 = lanczos_plain(sec, r.psis[0], refine_steps, rule=rr, check_every=check_every, nvec=1)
+    psi = r.psis[0].to(torch.float64)
+    r.psis = []
+    r64 = lanczos_plain(sec, psi, refine_steps, rule=rr, check_every=check_every, nvec=1, storage=storage)
+    del psi, storage
     torch.cuda.synchronize()
     t2 = time.perf_counter()
     return GroundState(e0=float(r64.ritz[0]), psi=r64.psis[0], ritz=r64.ritz, alpha=r.alpha, beta=r.beta,
                        steps=r.steps, refine_steps=r64.steps, converged=r.converged or rr.converged, ndeg=1,
-                       times={"total": t2 - t0, "fp32": t1 - t0, "refine": t2 - t1}, mode=mode,
-                       e0_unrefined=e0u, ritz_vectors=r64.ritz_vectors)
+                       times={"total": t2 - t0, "fp32": t1 - t0, "refine": t2 - t1,
+                              "fp32_alloc": r.times["alloc"], "fp32_kept_rows": r.times["kept_rows"],
+                              "fp32_replayed": r.times["replayed"], "refine_alloc": r64.times["alloc"],
+                              "refine_kept_rows": r64.times["kept_rows"], "refine_replayed": r64.times["replayed"]},
+                       mode=mode, e0_unrefined=e0u, ritz_vectors=r64.ritz_vectors)

@@ -188,6 +188,31 @@ def test_three_term_lanczos_matches_full(edlib, dt):
         assert abs(abs(ov) - 1) < 1e-8
 
 
+@pytest.mark.parametrize("layout", ["hubbard", "heisenberg"])
+def test_three_term_kept_basis_equals_replay(edlib, layout):
+    """The three-term Lanczos with its basis kept (Ritz vectors by one pass
+    over the kept rows), with a cap of 12 rows (rows run out mid-run: rotating
+    vectors, then a replay on the same schedule) and without keeping (replay)
+    runs the same recurrence.  The kept rows subtract u_{k-1} before u_k while
+    the rotating vectors take them in ring order, so the paths agree to
+    rounding: alpha/beta to 1e-12 relative, Ritz vectors to 1e-10 (FP64, 40
+    steps).  Padded (Hubbard) and unpadded (Heisenberg) layouts."""
+    import torch
+    from pyhub_gb300.core import lanczos as LZ
+    if layout == "hubbard":
+        sec = edlib.Sector(9, 4, 5, edlib.ED_HUBBARD, t=O.square_pbc(3, 3), U=np.full(9, 4.0))
+    else:
+        sec = edlib.Sector(16, 8, 0, edlib.ED_HEISENBERG, J=O.square_pbc(4, 4, 1.0))
+    v0 = LZ.start_vector(sec, 5, dtype=torch.float64)
+    runs = [LZ.lanczos_plain(sec, v0, 40, nvec=2, keep=k) for k in (True, 12, False)]
+    for r in runs[1:]:
+        assert r.steps == runs[0].steps == 40
+        assert np.allclose(r.alpha, runs[0].alpha, rtol=1e-12, atol=0)
+        assert np.allclose(r.beta, runs[0].beta, rtol=1e-12, atol=0)
+        for p, q in zip(r.psis, runs[0].psis):
+            assert float(torch.linalg.vector_norm(p - q)) < 1e-10
+
+
 def test_heisenberg_lattice_rdm_and_plain_mixed_ground_state(edlib):
     """4x4 periodic Heisenberg (dim 12,870): spin correlations of the row
     layout vs the oracle's J_SPIN on random bra/ket (all pairs, 1e-11); the
