@@ -407,8 +407,8 @@ def run_c3(args):
     RP.barrier()
     clock = StreamClock().start()
     # FP32 stage until E0 stalls at FP32 resolution; FP64 stage until the residual estimate is below 1e-9.
-    # Three-term form on four vectors: keeping the bases instead (55 x 2.4 GB FP32, 40 x 4.8 GB FP64) was
-    # measured no faster, the saved second passes being paid for by allocating and clearing the bases.
+    # Three-term recurrence (no reorthogonalisation) with its Krylov rows kept (55 x 2.4 GB FP32, then
+    # 40 x 4.8 GB FP64 in the same block), so each Ritz vector is one pass over the rows.
     steps32, steps64, reorth = args.lanczos_steps, 150, "none"
     gs = LZ.ground_state(sec, mode="mixed", steps=steps32, reorth=reorth, refine_steps=steps64,
                          rule=LZ.EnergyRule(1e-7, min_steps=20), refine_rule=LZ.ResidualRule(1e-9, 10))
