@@ -101,9 +101,11 @@ def solve(params: HubbardParams, theta, nup: int, ndn: int, mode: str = "f64", s
     the spin-resolved 1-RDM (computed, not copied, for both spins)."""
     t, U = params.unpack(theta)
     sec = _capi.Sector(params.norb, nup, ndn, _capi.ED_HUBBARD, t=t, U=U)
+    # f64: one Lanczos run to the residual; mixed: the FP64 refinement runs to the same residual
+    # (the 1-RDM and the adjoint need psi itself, which an energy criterion converges only to its root)
     rule = LZ.ResidualRule(tol, min_steps=10)
     gs = LZ.ground_state(sec, mode=mode, steps=steps, seed=seed, rule=rule if mode == "f64" else None,
-                         refine_tol=1e-14)
+                         refine_rule=None if mode == "f64" else LZ.ResidualRule(tol, min_steps=4))
     gamma = one_rdm(sec, gs.psi, params.norb)
     return Solution(e0=gs.e0, psi=gs.psi, sector=sec, gamma=gamma)
 
