@@ -217,6 +217,19 @@ int ed_batch_lanczos(ed_batch *b, void *stream, int dtype, void *work, const voi
 int ed_batch_ritz(ed_batch *b, void *stream, int dtype, void *work, const void *x0, int nsteps,
                   double *alpha, double *beta, const double *coef, void *out, void *scratch,
                   int64_t scratch_bytes);
+/* ed_batch_lanczos with every Krylov vector kept, as the reference keeps them
+ * for READ_PSI (lanczos.f90:42-49): u_k (unnormalised, ||u_k|| = beta[i][k])
+ * is written to slot k of basis ((nsteps+1)*total elements, slot k starting at
+ * k*total); y (total elements) takes the H*v.  Same alpha/beta as
+ * ed_batch_lanczos.  Then ed_batch_ritz_sum forms the Ritz vectors in one pass
+ * over the kept slots instead of a replay:
+ *   out_i = sum_{k<nsteps} coef[i][k] u_k / beta[i][k]  (terms with beta = 0
+ *   dropped; coef device FP64 [ninst][nsteps], beta as written by the run;
+ *   out written entirely, same dtype and layout as the basis). */
+int ed_batch_lanczos_kept(ed_batch *b, void *stream, int dtype, void *basis, void *y, const void *x0,
+                          int nsteps, double *alpha, double *beta, void *scratch, int64_t scratch_bytes);
+int ed_batch_ritz_sum(ed_batch *b, void *stream, int dtype, const void *basis, int nsteps,
+                      const double *coef, const double *beta, void *out);
 
 /* ed_multidot without a scratch buffer, for callers that cannot allocate
  * device memory: a host that hands all GPU memory to another runtime's pool,

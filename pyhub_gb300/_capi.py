@@ -48,6 +48,8 @@ _SIGS = {
     "ed_batch_rows": (_I, [_P]),
     "ed_update_wscaled": (_I, [_P, _I, _I, _I64, _P, _I64, _I, _P, _P, _P, _P, _P, _P, _I64]),
     "ed_lanczos_state_doubles": (_I64, [_I]),
+    "ed_batch_lanczos_kept": (_I, [_P, _P, _I, _P, _P, _P, _I, _P, _P, _P, _I64]),
+    "ed_batch_ritz_sum": (_I, [_P, _P, _I, _P, _I, _P, _P, _P]),
     "ed_lanczos_coef": (_I, [_P, _I, _I, _P, _P, _P, _P, _P, _P]),
 }
 
@@ -312,6 +314,26 @@ class Batch:
                                                          _ptr(x0), int(nsteps), _ptr(alpha), _ptr(beta), _ptr(scratch),
                                                          int(sb)))
 
+    def lanczos_kept(self, basis, y, x0, nsteps: int, alpha, beta, scratch, stream=None):
+        """lanczos() keeping every Krylov vector: u_k in basis[k*total:(k+1)*total]."""
+        sb = scratch.numel() * scratch.element_size()
+        self._check(basis, x0, nsteps, alpha, beta, work_need=(int(nsteps) + 1) * self.total)
+        if y.dtype != x0.dtype:
+            raise TypeError("y and x0 must have the same dtype")
+        tot = self.total
+        check("ed_batch_lanczos_kept", lib().ed_batch_lanczos_kept(
+            self._h, _stream(stream), dtype_code(x0.dtype), _ptr(basis, (int(nsteps) + 1) * tot, "basis"),
+            _ptr(y, tot, "y"), _ptr(x0, tot, "x0"), int(nsteps), _ptr(alpha), _ptr(beta), _ptr(scratch), int(sb)))
+
+    def ritz_sum(self, basis, nsteps: int, coef, beta, out, stream=None):
+        """out_i = sum_k coef[i, k] u_k / beta[i, k] from a kept basis."""
+        n, tot = len(self.sectors), self.total
+        if out.dtype != basis.dtype:
+            raise TypeError("out must have the dtype of the basis")
+        check("ed_batch_ritz_sum", lib().ed_batch_ritz_sum(
+            self._h, _stream(stream), dtype_code(basis.dtype), _ptr(basis, int(nsteps) * tot, "basis"), int(nsteps),
+            _ptr(coef, n * int(nsteps), "coef"), _ptr(beta, n * (int(nsteps) + 1), "beta"), _ptr(out, tot, "out")))
+
     def ritz(self, work, x0, nsteps: int, alpha, beta, coef, out, scratch, stream=None):
         """Replay of lanczos() accumulating out_i += sum_k coef[i, k] q_k."""
         sb = scratch.numel() * scratch.element_size()
@@ -324,14 +346,14 @@ class Batch:
                                                    _ptr(coef, n * int(nsteps), "coef"), _ptr(out, self.total, "out"),
                                                    _ptr(scratch), int(sb)))
 
-    def _check(self, work, x0, nsteps, alpha, beta):
+    def _check(self, work, x0, nsteps, alpha, beta, work_need=None):
         import torch
         n = len(self.sectors)
         if work.dtype != x0.dtype:
             raise TypeError("work and x0 must have the same dtype")
         if alpha.dtype != torch.float64 or beta.dtype != torch.float64:
             raise TypeError("alpha and beta are FP64")
-        _ptr(work, 3 * self.total, "work")
+        _ptr(work, 3 * self.total if work_need is None else work_need, "work")
         _ptr(x0, self.total, "x0")
         _ptr(alpha, n * int(nsteps), "alpha")
         _ptr(beta, n * (int(nsteps) + 1), "beta")

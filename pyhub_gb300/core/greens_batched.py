@@ -70,7 +70,7 @@ class BatchedLanczos:
     rows: rows of one instance per CTA of the H*v (4, 8 or 16), or "auto"
     to let autotune() pick it on this batch."""
 
-    def __init__(self, sectors, nsteps: int, dtype=None, device="cuda", rows=8):
+    def __init__(self, sectors, nsteps: int, dtype=None, device="cuda", rows=8, keep: bool = False):
         torch = _torch()
         self.dtype = dtype or torch.float32
         self.nsteps = int(nsteps)
@@ -81,7 +81,11 @@ class BatchedLanczos:
         self.sectors = list(sectors)
         n = len(self.sectors)
         tot = self.batch.total
-        self.work = torch.zeros(3 * tot, dtype=self.dtype, device=device)
+        # keep=True: every Krylov vector is kept (basis slot k = u_k, written before it is read)
+        # and Ritz vectors are one pass over them (ritz_sum) instead of a replay
+        self.keep = bool(keep)
+        self.basis = torch.empty((self.nsteps + 1) * tot, dtype=self.dtype, device=device) if keep else None
+        self.work = torch.zeros((1 if keep else 3) * tot, dtype=self.dtype, device=device)
         self.x0 = torch.zeros(tot, dtype=self.dtype, device=device)
         self.alpha = torch.zeros((n, self.nsteps), dtype=torch.float64, device=device)
         self.beta = torch.zeros((n, self.nsteps + 1), dtype=torch.float64, device=device)
@@ -92,7 +96,10 @@ class BatchedLanczos:
         return self.batch.view(self.x0, i)
 
     def run(self):
-        self.batch.lanczos(self.work, self.x0, self.nsteps, self.alpha, self.beta, self.scratch)
+        if self.keep:
+            self.batch.lanczos_kept(self.basis, self.work, self.x0, self.nsteps, self.alpha, self.beta, self.scratch)
+        else:
+            self.batch.lanczos(self.work, self.x0, self.nsteps, self.alpha, self.beta, self.scratch)
 
     def capture(self):
         """Record run() in a CUDA graph (the batch set its kernels' attributes
@@ -138,7 +145,8 @@ def _lowest_ritz(a, b, tol_break: float = 1e-12):
 
 def _ritz_cycle(bl, out):
     """One batched Lanczos run, the lowest Ritz pair of every instance, and
-    the replay that accumulates the Ritz vectors into `out` (normalised)."""
+    the Ritz vectors in `out` (normalised): one pass over the kept basis, or
+    a replay that accumulates them."""
     torch = _torch()
     n, nsteps = len(bl.sectors), bl.nsteps
     bl.run()
@@ -151,8 +159,11 @@ def _ritz_cycle(bl, out):
         e0[i] = theta
         C[i, :m] = y
     coef = torch.from_numpy(C).to(bl.x0.device)
-    out.zero_()
-    bl.batch.ritz(bl.work, bl.x0, nsteps, bl.alpha, bl.beta, coef, out, bl.scratch)
+    if bl.keep:
+        bl.batch.ritz_sum(bl.basis, nsteps, coef, bl.beta, out)
+    else:
+        out.zero_()
+        bl.batch.ritz(bl.work, bl.x0, nsteps, bl.alpha, bl.beta, coef, out, bl.scratch)
     for i in range(n):
         v = bl.batch.view(out, i)
         v /= torch.linalg.vector_norm(v)
@@ -174,11 +185,12 @@ def _true_residuals(bl, out, e0):
 def batched_ground_states(sectors, nsteps: int = 120, tol: float = 1e-10, max_restarts: int = 8, seed: int = 0,
                           mixed: bool = True, refine_steps: int = 60) -> BatchedGroundStates:
     """Ground states of many sectors at once.  Every sector is an instance of
-    the batched three-term Lanczos (ed_batch_lanczos); the lowest Ritz pair
-    of each tridiagonal matrix is found on the host and a replay of the same
-    run (ed_batch_ritz) accumulates the Ritz vectors -- the two-pass scheme
-    of the reference's ground-state solve (lanczos.f90:17-86 for the
-    coefficients, compute_solver.f90:270-290 for V*c).
+    the batched three-term Lanczos with its Krylov vectors kept
+    (ed_batch_lanczos_kept); the lowest Ritz pair of each tridiagonal matrix is
+    found on the host and one pass over the kept vectors (ed_batch_ritz_sum)
+    forms the Ritz vectors -- the reference's ground-state solve
+    (lanczos.f90:17-86 for the coefficients and the stored vectors,
+    compute_solver.f90:270-290 for V*c).
 
     mixed=True: a first cycle of nsteps with FP32 vectors, then FP64 cycles
     of refine_steps restarted from the previous Ritz vector; mixed=False:
@@ -189,16 +201,16 @@ def batched_ground_states(sectors, nsteps: int = 120, tol: float = 1e-10, max_re
     torch = _torch()
     starts = [LZ.start_vector(sec, seed + i, dtype=torch.float64) for i, sec in enumerate(sectors)]
     if mixed:
-        b32 = BatchedLanczos(sectors, nsteps, dtype=torch.float32, rows="auto")
+        b32 = BatchedLanczos(sectors, nsteps, dtype=torch.float32, rows="auto", keep=True)
         for i, v in enumerate(starts):
             b32.start(i).copy_(v)
         out32 = torch.zeros_like(b32.x0)
         _ritz_cycle(b32, out32)
-        bl = BatchedLanczos(sectors, refine_steps, dtype=torch.float64, rows="auto")
+        bl = BatchedLanczos(sectors, refine_steps, dtype=torch.float64, rows="auto", keep=True)
         bl.x0.copy_(out32)
         del b32, out32
     else:
-        bl = BatchedLanczos(sectors, nsteps, dtype=torch.float64)
+        bl = BatchedLanczos(sectors, nsteps, dtype=torch.float64, keep=True)
         for i, v in enumerate(starts):
             bl.start(i).copy_(v)
     out = torch.zeros_like(bl.x0)
@@ -210,7 +222,7 @@ def batched_ground_states(sectors, nsteps: int = 120, tol: float = 1e-10, max_re
     todo = np.nonzero(res > tol)[0]
     while todo.size and it < max_restarts:
         it += 1
-        sub = BatchedLanczos([bl.sectors[i] for i in todo], refine_steps, dtype=torch.float64)
+        sub = BatchedLanczos([bl.sectors[i] for i in todo], refine_steps, dtype=torch.float64, keep=True)
         for j, i in enumerate(todo):
             sub.start(j).copy_(bl.batch.view(out, int(i)))
         sout = torch.zeros_like(sub.x0)

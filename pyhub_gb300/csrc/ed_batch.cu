@@ -373,15 +373,16 @@ __global__ void __launch_bounds__(kBatchThreads) batch_hv_kernel(const BatchInst
     block_partial((double)dotp, part_out + b);
 }
 
-// u_next = y - c_cur u_k - c_prev u_prev (written over u_prev), partial
-// ||u_next||^2, in 16-byte vectors over the CTA's rows (padding is zero in
-// all three inputs, so it stays zero).  With ritz_coef, also
+// u_next = y - c_cur u_k - c_prev u_prev, written to un (which is u_prev
+// itself when only two Krylov vectors are kept, a new basis slot otherwise),
+// partial ||u_next||^2, in 16-byte vectors over the CTA's rows (padding is
+// zero in all three inputs, so it stays zero).  With ritz_coef, also
 // out += ritz_coef[i][k] s_k u_k (the Ritz vector sum_k y_k q_k of a replay).
 template <typename T>
 __global__ void __launch_bounds__(kBatchThreads) batch_update_kernel(const BatchInst *__restrict__ inst,
                                                                      const int32_t *__restrict__ blk_inst,
                                                                      const T *__restrict__ y, const T *__restrict__ u,
-                                                                     T *__restrict__ up, const double *__restrict__ scal,
+                                                                     const T *up, T *un, const double *__restrict__ scal,
                                                                      double *__restrict__ part_nrm,
                                                                      const double *__restrict__ ritz_coef,
                                                                      T *__restrict__ ritz_out, int k, int nsteps)
@@ -400,7 +401,8 @@ __global__ void __launch_bounds__(kBatchThreads) batch_update_kernel(const Batch
     const int nv = nr * (int)(a.ld / VN);
     const V *yv = reinterpret_cast<const V *>(y + base);
     const V *uv = reinterpret_cast<const V *>(u + base);
-    V *pv = reinterpret_cast<V *>(up + base);
+    const V *pv = reinterpret_cast<const V *>(up + base);
+    V *nv_out = reinterpret_cast<V *>(un + base);
     V *ov = ritz_out ? reinterpret_cast<V *>(ritz_out + base) : nullptr;
     T sp = 0;
     for (int q = threadIdx.x; q < nv; q += blockDim.x) {
@@ -414,7 +416,7 @@ __global__ void __launch_bounds__(kBatchThreads) batch_update_kernel(const Batch
             vat(nv_, e) = t;
             sp += t * t;
         }
-        pv[q] = nv_;
+        nv_out[q] = nv_;
         if (ov) {
             V o = ov[q];
 #pragma unroll
@@ -425,28 +427,87 @@ __global__ void __launch_bounds__(kBatchThreads) batch_update_kernel(const Batch
     block_partial((double)sp, part_nrm + b);
 }
 
+// Ritz vectors from a kept basis: out_i = sum_k coef[i][k] s_k u_k over the
+// CTA's rows, s_k = 1 / beta[i][k] (0 after a vanished beta), u_k the basis
+// slot k (k*total elements in).  The per-step factors of the instance are
+// staged in shared memory; each thread sums its 16-byte vectors over k.
+template <typename T>
+__global__ void __launch_bounds__(kBatchThreads) batch_ritz_sum_kernel(const BatchInst *__restrict__ inst,
+                                                                       const int32_t *__restrict__ blk_inst,
+                                                                       const T *__restrict__ basis, int64_t total,
+                                                                       int nsteps, const double *__restrict__ coef,
+                                                                       const double *__restrict__ beta,
+                                                                       T *__restrict__ out)
+{
+    using V = typename V16<T>::type;
+    constexpr int VN = V16<T>::n;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *cs = reinterpret_cast<T *>(smem_raw);   // [nsteps]
+    const int64_t b = blockIdx.x;
+    const int i = __ldg(blk_inst + b);
+    const BatchInst &a = inst[i];
+    for (int k = threadIdx.x; k < nsteps; k += blockDim.x) {
+        const double bk = beta[(int64_t)i * (nsteps + 1) + k];
+        cs[k] = (T)((bk > 1e-150) ? coef[(int64_t)i * nsteps + k] / bk : 0.0);
+    }
+    __syncthreads();
+    const int64_t r0 = (b - a.blk0) * a.rows;
+    const int nr = (int)min((int64_t)a.rows, a.nsdn - r0);
+    const int64_t base = a.off + r0 * a.ld;
+    const int nv = nr * (int)(a.ld / VN);
+    for (int q = threadIdx.x; q < nv; q += blockDim.x) {
+        V acc;
+#pragma unroll
+        for (int e = 0; e < VN; ++e) vat(acc, e) = (T)0;
+        const V *src = reinterpret_cast<const V *>(basis + base) + q;
+        const int64_t step = total / VN;
+        int k = 0;
+        for (; k + 4 <= nsteps; k += 4) {
+            V t[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) t[j] = __ldg(src + (int64_t)(k + j) * step);
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+#pragma unroll
+                for (int e = 0; e < VN; ++e) vat(acc, e) += cs[k + j] * reinterpret_cast<const T *>(&t[j])[e];
+        }
+        for (; k < nsteps; ++k) {
+            const V t = __ldg(src + (int64_t)k * step);
+#pragma unroll
+            for (int e = 0; e < VN; ++e) vat(acc, e) += cs[k] * reinterpret_cast<const T *>(&t)[e];
+        }
+        reinterpret_cast<V *>(out + base)[q] = acc;
+    }
+}
+
+// work: two Krylov vectors and y (3*total), or, with kept != NULL, y alone
+// (total) while u_k lives in slot k of kept ((nsteps+1)*total).
 template <typename T, int R>
 static int run_batch(ed_batch *bt, cudaStream_t st, T *work, const T *x0, int nsteps, double *alpha, double *beta,
-                     double *scratch, const double *ritz_coef, T *ritz_out)
+                     double *scratch, const double *ritz_coef, T *ritz_out, T *kept = nullptr)
 {
     const int64_t tot = bt->total;
     T *U[2] = {work, work + tot};
-    T *Y = work + 2 * tot;
+    T *Y = kept ? work : work + 2 * tot;
     double *pa = scratch, *pb = scratch + bt->nblocks, *scal = scratch + 2 * bt->nblocks;
     const size_t smem = (size_t)bt->max_ld * staged_stride<T, R>() * sizeof(T);
     const unsigned nb = (unsigned)bt->nblocks;
     const unsigned ns = (unsigned)((bt->ninst * 32 + 255) / 256);
-    // u_{k+1} overwrites u_{k-1} in place, so u_k lives in slot k % 2
-    ED_CHECK_CUDA(cudaMemcpyAsync(U[0], x0, sizeof(T) * tot, cudaMemcpyDeviceToDevice, st));
-    ED_CHECK_CUDA(cudaMemsetAsync(U[1], 0, sizeof(T) * tot, st));
+    // two kept vectors: u_{k+1} overwrites u_{k-1} in place, so u_k lives in slot k % 2
+    T *u0 = kept ? kept : U[0];
+    ED_CHECK_CUDA(cudaMemcpyAsync(u0, x0, sizeof(T) * tot, cudaMemcpyDeviceToDevice, st));
+    if (!kept) ED_CHECK_CUDA(cudaMemsetAsync(U[1], 0, sizeof(T) * tot, st));
     if (nb > 0) {
-        batch_norm_kernel<T><<<nb, kBatchThreads, 0, st>>>(bt->dev, bt->blk_inst, U[0], pb);
+        batch_norm_kernel<T><<<nb, kBatchThreads, 0, st>>>(bt->dev, bt->blk_inst, u0, pb);
         ED_CHECK_LAUNCH();
     }
     batch_scalar_kernel<<<ns, 256, 0, st>>>(bt->dev, bt->ninst, pb, scal, alpha, beta, 0, nsteps, 0);
     ED_CHECK_LAUNCH();
     for (int k = 0; k < nsteps; ++k) {
-        T *uk = U[k % 2], *uprev = U[(k + 1) % 2];
+        // with a kept basis, step 0's u_{-1} is u_0 itself (its coefficient is 0)
+        T *uk = kept ? kept + (int64_t)k * tot : U[k % 2];
+        T *uprev = kept ? kept + (int64_t)(k > 0 ? k - 1 : 0) * tot : U[(k + 1) % 2];
+        T *unext = kept ? kept + (int64_t)(k + 1) * tot : uprev;
         if (nb > 0) {
             batch_hv_kernel<T, R><<<nb, kBatchThreads, smem, st>>>(bt->dev, bt->blk_inst, uk, Y, scal, pa);
             ED_CHECK_LAUNCH();
@@ -454,8 +515,8 @@ static int run_batch(ed_batch *bt, cudaStream_t st, T *work, const T *x0, int ns
         batch_scalar_kernel<<<ns, 256, 0, st>>>(bt->dev, bt->ninst, pa, scal, alpha, beta, k, nsteps, 1);
         ED_CHECK_LAUNCH();
         if (nb > 0) {
-            batch_update_kernel<T><<<nb, kBatchThreads, 0, st>>>(bt->dev, bt->blk_inst, Y, uk, uprev, scal, pb,
-                                                                 ritz_coef, ritz_out, k, nsteps);
+            batch_update_kernel<T><<<nb, kBatchThreads, 0, st>>>(bt->dev, bt->blk_inst, Y, uk, uprev, unext, scal,
+                                                                 pb, ritz_coef, ritz_out, k, nsteps);
             ED_CHECK_LAUNCH();
         }
         batch_scalar_kernel<<<ns, 256, 0, st>>>(bt->dev, bt->ninst, pb, scal, alpha, beta, k + 1, nsteps, 0);
@@ -646,7 +707,8 @@ extern "C" int64_t ed_batch_scratch_bytes(const ed_batch *bt)
 }
 
 static int batch_launch(ed_batch *bt, void *stream, int dtype, void *work, const void *x0, int nsteps, double *alpha,
-                        double *beta, const double *ritz_coef, void *ritz_out, void *scratch, int64_t scratch_bytes)
+                        double *beta, const double *ritz_coef, void *ritz_out, void *scratch, int64_t scratch_bytes,
+                        void *kept = nullptr)
 {
     ED_REQUIRE(bt != nullptr && work != nullptr && x0 != nullptr && alpha != nullptr && beta != nullptr,
                "NULL argument");
@@ -659,17 +721,50 @@ static int batch_launch(ed_batch *bt, void *stream, int dtype, void *work, const
     if (rc != ED_OK) return rc;
     double *sc = (double *)scratch;
     if (dtype == ED_F32) {
-        float *w = (float *)work, *ro = (float *)ritz_out;
+        float *w = (float *)work, *ro = (float *)ritz_out, *kp = (float *)kept;
         const float *x = (const float *)x0;
-        if (bt->rows == 4) return run_batch<float, 4>(bt, st, w, x, nsteps, alpha, beta, sc, ritz_coef, ro);
-        if (bt->rows == 16) return run_batch<float, 16>(bt, st, w, x, nsteps, alpha, beta, sc, ritz_coef, ro);
-        return run_batch<float, 8>(bt, st, w, x, nsteps, alpha, beta, sc, ritz_coef, ro);
+        if (bt->rows == 4) return run_batch<float, 4>(bt, st, w, x, nsteps, alpha, beta, sc, ritz_coef, ro, kp);
+        if (bt->rows == 16) return run_batch<float, 16>(bt, st, w, x, nsteps, alpha, beta, sc, ritz_coef, ro, kp);
+        return run_batch<float, 8>(bt, st, w, x, nsteps, alpha, beta, sc, ritz_coef, ro, kp);
     }
-    double *w = (double *)work, *ro = (double *)ritz_out;
+    double *w = (double *)work, *ro = (double *)ritz_out, *kp = (double *)kept;
     const double *x = (const double *)x0;
-    if (bt->rows == 4) return run_batch<double, 4>(bt, st, w, x, nsteps, alpha, beta, sc, ritz_coef, ro);
-    if (bt->rows == 16) return run_batch<double, 16>(bt, st, w, x, nsteps, alpha, beta, sc, ritz_coef, ro);
-    return run_batch<double, 8>(bt, st, w, x, nsteps, alpha, beta, sc, ritz_coef, ro);
+    if (bt->rows == 4) return run_batch<double, 4>(bt, st, w, x, nsteps, alpha, beta, sc, ritz_coef, ro, kp);
+    if (bt->rows == 16) return run_batch<double, 16>(bt, st, w, x, nsteps, alpha, beta, sc, ritz_coef, ro, kp);
+    return run_batch<double, 8>(bt, st, w, x, nsteps, alpha, beta, sc, ritz_coef, ro, kp);
+}
+
+extern "C" int ed_batch_lanczos_kept(ed_batch *bt, void *stream, int dtype, void *basis, void *y, const void *x0,
+                                     int nsteps, double *alpha, double *beta, void *scratch, int64_t scratch_bytes)
+{
+    clear_error();
+    ED_REQUIRE(basis != nullptr && y != nullptr, "NULL argument");
+    return batch_launch(bt, stream, dtype, y, x0, nsteps, alpha, beta, nullptr, nullptr, scratch, scratch_bytes,
+                        basis);
+}
+
+extern "C" int ed_batch_ritz_sum(ed_batch *bt, void *stream, int dtype, const void *basis, int nsteps,
+                                 const double *coef, const double *beta, void *out)
+{
+    clear_error();
+    ED_REQUIRE(bt != nullptr && basis != nullptr && coef != nullptr && beta != nullptr && out != nullptr,
+               "NULL argument");
+    ED_REQUIRE(dtype == ED_F32 || dtype == ED_F64, "dtype must be ED_F32 or ED_F64");
+    ED_REQUIRE(nsteps >= 1 && nsteps <= 4096, "nsteps=%d outside 1..4096", nsteps);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const unsigned nb = (unsigned)bt->nblocks;
+    if (nb == 0) return ED_OK;
+    const size_t smem = (size_t)nsteps * (dtype == ED_F32 ? sizeof(float) : sizeof(double));
+    if (dtype == ED_F32)
+        batch_ritz_sum_kernel<float><<<nb, kBatchThreads, smem, st>>>(bt->dev, bt->blk_inst,
+                                                                       static_cast<const float *>(basis), bt->total,
+                                                                       nsteps, coef, beta, static_cast<float *>(out));
+    else
+        batch_ritz_sum_kernel<double><<<nb, kBatchThreads, smem, st>>>(bt->dev, bt->blk_inst,
+                                                                        static_cast<const double *>(basis), bt->total,
+                                                                        nsteps, coef, beta, static_cast<double *>(out));
+    ED_CHECK_LAUNCH();
+    return ED_OK;
 }
 
 extern "C" int ed_batch_lanczos(ed_batch *bt, void *stream, int dtype, void *work, const void *x0, int nsteps,

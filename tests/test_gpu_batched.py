@@ -194,3 +194,28 @@ def test_rows_per_cta_variants_agree(edlib):
             assert np.allclose(A[i, :n], a[:n], rtol=1e-9, atol=1e-9), (rows, key)
             assert np.allclose(B[i, :n + 1], bb[:n + 1], rtol=1e-9, atol=1e-9), (rows, key)
     assert GB.autotune(secs, torch.float32) in (4, 8, 16)
+
+
+@pytest.mark.parametrize("dtype", ["float32", "float64"])
+def test_kept_basis_matches_replay(edlib, dtype):
+    """The batched Lanczos with every Krylov vector kept runs the same
+    recurrence as the two-vector form (alpha/beta bit for bit), and the Ritz
+    vectors summed over the kept vectors equal the replay's (1e-13 FP64,
+    1e-6 FP32, relative)."""
+    import torch
+    from pyhub_gb300.core import greens_batched as GB
+    dt = getattr(torch, dtype)
+    t, U, src, gs, secs, inst, bl = _setup(edlib, nsteps=30)
+    outs, ab = [], []
+    for keep in (False, True):
+        b = GB.BatchedLanczos(secs, 30, dtype=dt, keep=keep)
+        b.x0.copy_(bl.x0.to(dt))
+        out = torch.zeros_like(b.x0)
+        GB._ritz_cycle(b, out)
+        torch.cuda.synchronize()
+        outs.append(out)
+        ab.append((b.alpha.cpu().numpy(), b.beta.cpu().numpy()))
+    assert np.array_equal(ab[0][0], ab[1][0]) and np.array_equal(ab[0][1], ab[1][1])
+    tol = 1e-13 if dtype == "float64" else 1e-6
+    assert float(torch.linalg.vector_norm((outs[0] - outs[1]).double())) <= tol * float(
+        torch.linalg.vector_norm(outs[0].double()))
