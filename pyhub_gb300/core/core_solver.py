@@ -358,12 +358,16 @@ class CoreSolver(Basis, GreenFunction, StaticQuantities):
         w = self.boltzmann / self.Z
         sec = self.sector(self.nup[0], self.ndown[0])
         acc = None
+        # the Boltzmann-weighted sum is formed on the device; one copy to the host
         for b, wb in enumerate(w):
             if wb == 0.0:
                 continue
-            v = sec.to_ref(self._state_device(b)).double().cpu().numpy() * wb
-            acc = v if acc is None else acc + v
-        return acc
+            v = sec.to_ref(self._state_device(b)).double()
+            if acc is None:
+                acc = v if wb == 1.0 else v * wb
+            else:
+                acc = acc + wb * v
+        return None if acc is None else acc.cpu().numpy()
 
     def psi(self, vector: int):
         sec = self.sector(self.nup[0], self.ndown[0])
