@@ -335,6 +335,18 @@ class PlainResult:
     times: dict
 
 
+def _zero_padding(sec, rows):
+    """Zero the padding of every row of a (rows, sec.n) block: the columns
+    past nsup of each down-string row (Hubbard), the tail past dim
+    (Heisenberg)."""
+    if sec.n == sec.dim:
+        return
+    if sec.kind == _capi.ED_HUBBARD:
+        rows.view(rows.shape[0], sec.nsdn, sec.ld)[:, :, sec.nsup:].zero_()
+    else:
+        rows[:, sec.dim:].zero_()
+
+
 def kept_storage(dev, need: int, frac: float = 0.85, min_bytes: int = 1 << 20):
     """One device byte block for the kept Krylov rows of lanczos_plain: need
     bytes, or ``frac`` of the free memory if less (None if not even min_bytes
@@ -347,14 +359,18 @@ def kept_storage(dev, need: int, frac: float = 0.85, min_bytes: int = 1 << 20):
     # previous solve left cached is reused as it is); failing that, with the cache returned
     free = torch.cuda.mem_get_info(dev)[0]
     cached = torch.cuda.memory_reserved(dev) - torch.cuda.memory_allocated(dev)
-    nbytes = min(int(need), int(frac * (free + cached))) // 256 * 256
+    # whole GiB when large, so that repeated solves ask for the block the previous one left cached
+    gib = 1 << 30
+    nbytes = min(int(need), int(frac * (free + cached)))
+    nbytes = nbytes // gib * gib if nbytes >= 4 * gib else nbytes // 256 * 256
     if nbytes >= min_bytes:
         try:
             return torch.empty(nbytes, dtype=torch.uint8, device=dev)
         except torch.OutOfMemoryError:
             pass
     torch.cuda.empty_cache()
-    nbytes = min(int(need), int(frac * torch.cuda.mem_get_info(dev)[0])) // 256 * 256
+    nbytes = min(int(need), int(frac * torch.cuda.mem_get_info(dev)[0]))
+    nbytes = nbytes // gib * gib if nbytes >= 4 * gib else nbytes // 256 * 256
     while nbytes >= min_bytes:
         try:
             return torch.empty(nbytes, dtype=torch.uint8, device=dev)
@@ -385,7 +401,7 @@ def lanczos_plain(sec, v0, max_steps: int, rule=None, check_every: int = NADD, n
     m = int(max_steps)
     t0 = time.perf_counter()
     ws = _Scratch(n, max(4, nvec), dev)
-    R = torch.zeros((3, n), dtype=v0.dtype, device=dev)
+    R = None       # the three rotating vectors, made when a run needs them
     t_alloc = time.perf_counter()
     V = None
     if want_vectors and keep:
@@ -397,16 +413,23 @@ def lanczos_plain(sec, v0, max_steps: int, rule=None, check_every: int = NADD, n
             cap = min(cap, int(keep))
         if cap >= 4:
             V = storage[: cap * n * es].view(v0.dtype).view(cap, n)
-            if n != sec.dim:
-                V.zero_()   # the H*v leaves row padding untouched: padded layouts start at zero
+            _zero_padding(sec, V)   # the H*v leaves the padding untouched
     cap = 0 if V is None else V.shape[0]
     t_alloc = time.perf_counter() - t_alloc
+
+    def rotating():
+        nonlocal R
+        if R is None:
+            R = torch.zeros((3, n), dtype=v0.dtype, device=dev)
+        else:
+            R.zero_()
+        return R
 
     def run(steps, z=None, psis=None):
         # a replay (psis given) follows the first run's schedule of kept rows and rotating
         # vectors, so that it recomputes the same vectors bit for bit
         kept = V is not None
-        R.zero_()
+        R = None if kept else rotating()
         if kept:
             V[0].copy_(v0)
         else:
@@ -420,6 +443,7 @@ def lanczos_plain(sec, v0, max_steps: int, rule=None, check_every: int = NADD, n
         for k in range(steps):
             if kept and k + 1 >= cap:
                 # the kept rows are used up: continue on the rotating vectors
+                R = rotating()
                 R[(k + 2) % 3].copy_(V[k - 1])
                 R[k % 3].copy_(V[k])
                 kept = False
@@ -463,8 +487,12 @@ def lanczos_plain(sec, v0, max_steps: int, rule=None, check_every: int = NADD, n
                     break
         return np.array(alpha), np.array(beta), done, conv, (np.array(scales) if kept else None)
 
+    t_run = time.perf_counter()
     alpha, beta, done, conv, scales = run(m)    # scales is None when the kept rows ran out
+    torch.cuda.synchronize()
+    t_run = time.perf_counter() - t_run
     val, vec = _tridiag_eigs(alpha, beta, done, vectors=True)
+    t_ritz = time.perf_counter()
     psis = []
     if want_vectors:
         nv = min(nvec, done)
@@ -483,8 +511,11 @@ def lanczos_plain(sec, v0, max_steps: int, rule=None, check_every: int = NADD, n
             for p in psis:
                 _capi.multidot(p.view(1, -1), 1, p, ws.dots, ws.buf)
                 p.mul_(1.0 / math.sqrt(float(ws.dots[0].item())))
+    torch.cuda.synchronize()
+    t_ritz = time.perf_counter() - t_ritz
     return PlainResult(alpha=alpha, beta=beta, ritz=val, ritz_vectors=vec, steps=done, converged=conv,
-                       psis=psis, times={"total": time.perf_counter() - t0, "alloc": t_alloc, "kept_rows": cap,
+                       psis=psis, times={"total": time.perf_counter() - t0, "alloc": t_alloc, "run": t_run,
+                                         "ritz": t_ritz, "kept_rows": cap,
                                          "replayed": bool(want_vectors and scales is None)})
 
 
@@ -567,9 +598,11 @@ def _ground_state_plain(sec, mode, steps, v0, rule, refine_steps, refine_tol, ch
                         refine_rule=None) -> GroundState:
     torch = _torch()
     vt = torch.float64 if mode == "f64" else torch.float32
+    ts = time.perf_counter()
     storage = kept_storage(v0.device, max((steps + 1) * sec.n * (8 if mode == "f64" else 4),
                                           (refine_steps + 1) * sec.n * 8 if mode == "mixed" else 0),
                            min_bytes=4 * sec.n * 8)
+    t_storage = time.perf_counter() - ts
     # mixed: the FP32 Ritz vector only starts the FP64 stage (summed in FP32 from a kept basis)
     r = lanczos_plain(sec, v0.to(vt), steps, rule=rule, check_every=check_every, nvec=1,
                       ritz_dtype=torch.float32 if mode == "mixed" else None, storage=storage)
@@ -590,8 +623,10 @@ def _ground_state_plain(sec, mode, steps, v0, rule, refine_steps, refine_tol, ch
     t2 = time.perf_counter()
     return GroundState(e0=float(r64.ritz[0]), psi=r64.psis[0], ritz=r64.ritz, alpha=r.alpha, beta=r.beta,
                        steps=r.steps, refine_steps=r64.steps, converged=r.converged or rr.converged, ndeg=1,
-                       times={"total": t2 - t0, "fp32": t1 - t0, "refine": t2 - t1,
-                              "fp32_alloc": r.times["alloc"], "fp32_kept_rows": r.times["kept_rows"],
+                       times={"total": t2 - t0, "fp32": t1 - t0, "refine": t2 - t1, "storage": t_storage,
+                              "fp32_alloc": r.times["alloc"], "fp32_run": r.times["run"],
+                              "fp32_total": r.times["total"], "fp32_ritz": r.times["ritz"],
+                              "fp32_kept_rows": r.times["kept_rows"],
                               "fp32_replayed": r.times["replayed"], "refine_alloc": r64.times["alloc"],
                               "refine_kept_rows": r64.times["kept_rows"], "refine_replayed": r64.times["replayed"]},
                        mode=mode, e0_unrefined=e0u, ritz_vectors=r64.ritz_vectors)
