@@ -716,7 +716,7 @@ def main():
         torch.cuda.empty_cache()
 
     cpu = None
-    if not args.no_cpu and rank == 0 and not args.small:
+    if not args.no_cpu and rank == 0 and ws == 1 and not args.small:   # the CPU sample: rank 0 at N=1 only
         hv_cpu, spent, desc, nth = cpu_sample(CPU_PAIRS_OURS, 16, args.U)
         n_hv = sum(r[1] + r[2] for r in res) / len(res)
         cpu = {"value": 1.0 / (hv_cpu * n_hv), "unit": UNIT, "cores": nth, "kind": "port",
