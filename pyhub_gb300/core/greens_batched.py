@@ -68,9 +68,11 @@ def autotune(sectors, dtype, steps: int = 3, sample: int = 192, device="cuda"):
 class BatchedLanczos:
     """Fixed-length three-term Lanczos of many instances in one enqueue.
     rows: rows of one instance per CTA of the H*v (4, 8 or 16), or "auto"
-    to let autotune() pick it on this batch."""
+    to let autotune() pick it on this batch.  keep: keep every Krylov vector
+    (Ritz vectors by one pass over them, _ritz_cycle) instead of two; "auto"
+    keeps them when they fit in half of the free device memory."""
 
-    def __init__(self, sectors, nsteps: int, dtype=None, device="cuda", rows=8, keep: bool = False):
+    def __init__(self, sectors, nsteps: int, dtype=None, device="cuda", rows=8, keep=False):
         torch = _torch()
         self.dtype = dtype or torch.float32
         self.nsteps = int(nsteps)
@@ -82,7 +84,13 @@ class BatchedLanczos:
         n = len(self.sectors)
         tot = self.batch.total
         # keep=True: every Krylov vector is kept (basis slot k = u_k, written before it is read)
-        # and Ritz vectors are one pass over them (ritz_sum) instead of a replay
+        # and Ritz vectors are one pass over them (ritz_sum) instead of a replay; "auto" keeps
+        # them when they take at most half of the free device memory
+        if keep == "auto":
+            es = torch.empty(0, dtype=self.dtype).element_size()
+            free = torch.cuda.mem_get_info(device)[0] + torch.cuda.memory_reserved(device) - \
+                torch.cuda.memory_allocated(device)
+            keep = (self.nsteps + 2) * tot * es <= 0.5 * free
         self.keep = bool(keep)
         self.basis = torch.empty((self.nsteps + 1) * tot, dtype=self.dtype, device=device) if keep else None
         self.work = torch.zeros((1 if keep else 3) * tot, dtype=self.dtype, device=device)
@@ -201,16 +209,16 @@ def batched_ground_states(sectors, nsteps: int = 120, tol: float = 1e-10, max_re
     torch = _torch()
     starts = [LZ.start_vector(sec, seed + i, dtype=torch.float64) for i, sec in enumerate(sectors)]
     if mixed:
-        b32 = BatchedLanczos(sectors, nsteps, dtype=torch.float32, rows="auto", keep=True)
+        b32 = BatchedLanczos(sectors, nsteps, dtype=torch.float32, rows="auto", keep="auto")
         for i, v in enumerate(starts):
             b32.start(i).copy_(v)
         out32 = torch.zeros_like(b32.x0)
         _ritz_cycle(b32, out32)
-        bl = BatchedLanczos(sectors, refine_steps, dtype=torch.float64, rows="auto", keep=True)
+        bl = BatchedLanczos(sectors, refine_steps, dtype=torch.float64, rows="auto", keep="auto")
         bl.x0.copy_(out32)
         del b32, out32
     else:
-        bl = BatchedLanczos(sectors, nsteps, dtype=torch.float64, keep=True)
+        bl = BatchedLanczos(sectors, nsteps, dtype=torch.float64, keep="auto")
         for i, v in enumerate(starts):
             bl.start(i).copy_(v)
     out = torch.zeros_like(bl.x0)
@@ -222,7 +230,7 @@ def batched_ground_states(sectors, nsteps: int = 120, tol: float = 1e-10, max_re
     todo = np.nonzero(res > tol)[0]
     while todo.size and it < max_restarts:
         it += 1
-        sub = BatchedLanczos([bl.sectors[i] for i in todo], refine_steps, dtype=torch.float64, keep=True)
+        sub = BatchedLanczos([bl.sectors[i] for i in todo], refine_steps, dtype=torch.float64, keep="auto")
         for j, i in enumerate(todo):
             sub.start(j).copy_(bl.batch.view(out, int(i)))
         sout = torch.zeros_like(sub.x0)
