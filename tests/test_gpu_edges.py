@@ -77,3 +77,28 @@ def test_batch_with_one_state_instance(edlib):
         n = np.count_nonzero(b[1:] > 1e-8)
         assert np.allclose(A[i, :n], a[:n], rtol=1e-9, atol=1e-9)
         assert np.allclose(B[i, :n + 1], b[:n + 1], rtol=1e-9, atol=1e-9)
+
+
+@pytest.mark.parametrize("dt", ["f64", "f32"])
+def test_full_lanczos_breakdown_on_small_sector(edlib, dt):
+    """A 24-state sector run for 40 full-reorthogonalisation steps.  FP64: the
+    Krylov space is exhausted and the device stop code ends the run at <= 24
+    steps.  FP32: the next vector is rounding noise (~1e-7 ||H||, above the
+    breakdown threshold), so the run goes on with noise directions, as the
+    reference's recurrence would.  Either way the lowest Ritz value is E0 of
+    the dense matrix (1e-10 FP64, 1e-5 FP32) and the Ritz vector is finite and
+    normalised."""
+    import torch
+    from pyhub_gb300.core import lanczos as LZ
+    t, U = _tu(4, 11)
+    sec = edlib.Sector(4, 2, 1, edlib.ED_HUBBARD, t=t, U=U)
+    assert sec.dim == 24
+    td = torch.float64 if dt == "f64" else torch.float32
+    r = LZ.lanczos_full(sec, LZ.start_vector(sec, 2, dtype=td), 40, td)
+    osec = O.Sector(4, 2, 1)
+    e = np.linalg.eigvalsh(O.dense_h(lambda v: O.hprod_hubbard(osec, t, U, v), osec.dim))[0]
+    if dt == "f64":
+        assert r.breakdown and r.steps <= 24
+    assert abs(r.ritz[0] - e) < (1e-10 if dt == "f64" else 1e-5)
+    assert bool(torch.isfinite(r.psi).all())
+    assert abs(float(torch.linalg.vector_norm(r.psi)) - 1.0) < 1e-12
