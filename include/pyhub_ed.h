@@ -135,8 +135,9 @@ int ed_update_wscaled(void *stream, int dtype, int out_dtype, int64_t n, const v
  * factor, which grows by one row per step.
  * state: device FP64 array of ed_lanczos_state_doubles(mmax) entries, zeroed
  *   before step 0 except state[2] = 1/||u_0||:
- *   [0] stop code: 0 running, j > 0 breakdown (beta_{j-1} <= 1e-13 max(1,|alpha_{j-1}|),
- *       j steps done), -j a non-finite norm after j steps;
+ *   [0] stop code: 0 running, j > 0 breakdown after j steps (beta_{j-1} <=
+ *       1e-13 max(1,|alpha_{j-1}|), or u_j numerically dependent on the basis: its
+ *       Gram pivot below half its squared norm), -j a non-finite norm after j steps;
  *   [1] largest |G - I| entry seen;  [2 .. 2+mmax] s_0 .. s_mmax;
  *   then the inverse Cholesky factor, (mmax+1)^2 entries, row-major, and
  *   four work vectors of mmax+1 entries.

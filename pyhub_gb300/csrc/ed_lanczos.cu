@@ -68,7 +68,8 @@ __device__ __forceinline__ double block_max_d(double v, double *red)
 
 // One CTA.  Part 1 (every call, k >= 1): beta_{k-1} and s_k from nrm, with
 // the breakdown test of the host loop (beta <= 1e-13 max(1, |alpha|)).  Part 2
-// (dots != NULL): G row k, Linv row k, coef and alpha_k.  Once stopped, coef is
+// (dots != NULL): G row k, Linv row k, coef and alpha_k; it also stops the run
+// when u_k is numerically dependent on the basis.  Once stopped, coef is
 // written as zeros (and s stays 0), so the vectors that follow are zero and
 // finite until the host sees the stop code.
 __global__ void __launch_bounds__(kCoefThreads) lanczos_coef_kernel(int k, int mmax, const double *__restrict__ dots,
@@ -137,6 +138,14 @@ __global__ void __launch_bounds__(kCoefThreads) lanczos_coef_kernel(int k, int m
     if (threadIdx.x == 0) off = fmax(off, fabs(g[k] - 1.0));
     ll = block_sum_d(ll, red);
     off = block_max_d(off, red);
+    // a healthy step has lam^2 = g_k - |l|^2 within rounding of 1; below g_k / 2 the stored
+    // vector lies mostly inside the span of the basis (a Krylov space exhausted to rounding
+    // noise): the run stops with k steps, before the inverse factor would blow up
+    if (k >= 1 && !(g[k] - ll >= 0.5 * g[k])) {
+        for (int j = threadIdx.x; j <= k; j += blockDim.x) coef[j] = 0.0;
+        if (threadIdx.x == 0) state[0] = (double)k;
+        return;
+    }
     const double lam = sqrt(fmax(g[k] - ll, 1e-300));
     // new row k of Linv: -(l^T Linv[0:k][0:k]) / lam, then 1 / lam
     double *rowk = Linv + (int64_t)k * ldl;
