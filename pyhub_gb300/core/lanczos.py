@@ -210,7 +210,8 @@ class _Scratch:
 
 def lanczos_full(sec, v0, max_steps: int, dtype=None, rule=None, check_every: int = NADD,
                  min_steps: int = 0, want_vector: bool = True, vec_index: int = 0,
-                 keep_basis: bool = False, timer: KernelTimer = None, ritz_dtype=None) -> KrylovResult:
+                 keep_basis: bool = False, timer: KernelTimer = None, ritz_dtype=None,
+                 lookahead=None) -> KrylovResult:
     """Lanczos with full reorthogonalisation (delayed CGS with the exact Gram
     matrix).  v0: start vector (device tensor, internal layout).  The basis
     of max_steps+1 vectors is stored in ``dtype`` (FP32 or FP64); scalars are
@@ -224,7 +225,11 @@ def lanczos_full(sec, v0, max_steps: int, dtype=None, rule=None, check_every: in
     multi-dot of the basis with H u_k and u_k, the scalar work on the device
     (ed_lanczos_coef: Gram row, inverse Cholesky row, projection
     coefficients, alpha, beta) and the update, which scales H u_k by s_k on
-    the device.  The host reads alpha/beta only at rule checks and at the end."""
+    the device.  The host reads alpha/beta only at rule checks and at the end.
+    With ``lookahead`` (default: when checks are at least 3 steps apart) a
+    check's alpha/beta are copied asynchronously and the next step is enqueued
+    before the host waits for them, so the GPU does not idle during the check;
+    a run that converges there has done one step more than it keeps."""
     torch = _torch()
     dtype = dtype or v0.dtype
     dev = v0.device
@@ -256,6 +261,31 @@ def lanczos_full(sec, v0, max_steps: int, dtype=None, rule=None, check_every: in
         hab = ab[:, :k].cpu().numpy()
         return int(hs[0]), float(hs[1]), hab[0].copy(), hab[1].copy()
 
+    def post(k):
+        """close(k) with the copies left in flight: (k, event, host buffers)."""
+        _capi.lanczos_coef(k, m, None, ws.nrm, state, None, ab[0], ab[1])
+        hs = torch.empty(2, dtype=torch.float64, pin_memory=True)
+        hab = torch.empty((2, k), dtype=torch.float64, pin_memory=True)
+        hs.copy_(state[:2], non_blocking=True)
+        hab.copy_(ab[:, :k], non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record()
+        return k, ev, hs, hab
+
+    def judge(k, stop, alpha, beta):
+        """The rule at check k: True to stop there."""
+        if stop != 0:
+            return True
+        if getattr(rule, "wants_vectors", False):
+            val, vecs_t = _tridiag_eigs(alpha, beta, k, vectors=True)
+            return rule(val, k, vec=vecs_t, beta_last=beta[k - 1])
+        return rule(_tridiag_eigs(alpha, beta, k), k)
+
+    if lookahead is None:
+        lookahead = check_every >= 3
+    pending = None
+    snap = None      # (k, stop, gram, alpha, beta) of the check the run stopped at
+
     for k in range(m):
         e = timer("hv", 2.0 * sec.dim * es) if timer is not None else None
         sec.hv(V[k], w)
@@ -274,20 +304,30 @@ def lanczos_full(sec, v0, max_steps: int, dtype=None, rule=None, check_every: in
         if e is not None:
             e.record()
         k_done = k + 1
+        if pending is not None:
+            # the check posted after the previous step, read while this step runs
+            kc, ev, hs, hab = pending
+            pending = None
+            ev.synchronize()
+            st_c, g_c = int(hs[0]), float(hs[1])
+            a_c, b_c = hab[0].numpy().copy(), hab[1].numpy().copy()
+            if judge(kc, st_c, a_c, b_c):
+                snap = (kc, st_c, g_c, a_c, b_c)
+                converged = st_c == 0
+                break
         if rule is not None and k_done % check_every == 0 and k_done >= min_steps:
-            stop, _, alpha, beta = close(k_done)
-            if stop != 0:
+            if lookahead and k_done < m:
+                pending = post(k_done)
+                continue
+            stop, gram_off, alpha, beta = close(k_done)
+            if judge(k_done, stop, alpha, beta):
+                snap = (k_done, stop, gram_off, alpha, beta)
+                converged = stop == 0
                 break
-            if getattr(rule, "wants_vectors", False):
-                val, vecs_t = _tridiag_eigs(alpha, beta, k_done, vectors=True)
-                ok = rule(val, k_done, vec=vecs_t, beta_last=beta[k_done - 1])
-            else:
-                val = _tridiag_eigs(alpha, beta, k_done)
-                ok = rule(val, k_done)
-            if ok:
-                converged = True
-                break
-    stop, gram_off, alpha, beta = close(k_done)
+    if snap is not None:
+        k_done, stop, gram_off, alpha, beta = snap
+    else:
+        stop, gram_off, alpha, beta = close(k_done)
     if stop < 0:
         raise FloatingPointError(f"non-finite norm at Lanczos step {-stop - 1}")
     if stop > 0:
