@@ -232,6 +232,18 @@ int ed_batch_lanczos_kept(ed_batch *b, void *stream, int dtype, void *basis, voi
 int ed_batch_ritz_sum(ed_batch *b, void *stream, int dtype, const void *basis, int nsteps,
                       const double *coef, const double *beta, void *out);
 
+/* Green's functions from Lanczos coefficients, as continued fractions:
+ *   out[i][j] = beta[i][0]^2 / (z - s a_0 - beta[i][1]^2 / (z - s a_1 - ...)),
+ *   z = z_j + shift[i], s = sign[i], a_k = alpha[i][k], m levels,
+ * i.e. <phi_i|(z - s H)^-1|phi_i> of each instance's start vector.  The
+ * reference evaluates the same G(w) from band-Lanczos poles,
+ * sum_p w_p / (w - p + i eta) (pole.py:81-88, positions from
+ * reduced_quantities.py:84-92).  alpha [n][m], beta [n][m+1], shift, sign [n]
+ * device FP64 (shift NULL: 0, sign NULL: +1); z [nz] and out [n][nz] device
+ * complex FP64 as (re, im) pairs, 16-byte aligned.  n <= 65535, m <= 3000. */
+int ed_cf_eval(void *stream, int n, int m, const double *alpha, const double *beta, int nz,
+               const double *z, const double *shift, const double *sign, double *out);
+
 /* ed_multidot without a scratch buffer, for callers that cannot allocate
  * device memory: a host that hands all GPU memory to another runtime's pool,
  * or a plug-in whose host forbids it to call the CUDA allocator, has no way

@@ -50,6 +50,7 @@ _SIGS = {
     "ed_lanczos_state_doubles": (_I64, [_I]),
     "ed_batch_lanczos_kept": (_I, [_P, _P, _I, _P, _P, _P, _I, _P, _P, _P, _I64]),
     "ed_batch_ritz_sum": (_I, [_P, _P, _I, _P, _I, _P, _P, _P]),
+    "ed_cf_eval": (_I, [_P, _I, _I, _P, _P, _I, _P, _P, _P, _P]),
     "ed_lanczos_coef": (_I, [_P, _I, _I, _P, _P, _P, _P, _P, _P]),
 }
 
@@ -395,6 +396,27 @@ def update(V, nvec: int, coef, w, out, norm2=None, scratch=None, n: int | None =
         _stream(stream), vdt, dtype_code(out.dtype), int(n), _ptr(V, needV, "V"), int(ldv), int(nvec),
         _ptr(coef, int(nvec), "coef"), _ptr(wscale, 1, "wscale"), _ptr(w, n, "w"), _ptr(out, n, "out"),
         _ptr(norm2, 1, "norm2"), _ptr(scratch), int(sb)))
+
+
+def cf_eval(alpha, beta, z, shift=None, sign=None, stream=None):
+    """Continued fractions of Lanczos coefficients (ed_cf_eval): [n, len(z)]
+    complex128, instance i at z + shift[i] with sign[i] on H."""
+    import torch
+    n, m = int(alpha.shape[0]), int(alpha.shape[1])
+    zc = z.to(torch.complex128).contiguous()
+    out = torch.empty((n, zc.numel()), dtype=torch.complex128, device=alpha.device)
+    a = alpha.to(torch.float64).contiguous()
+    b = beta.to(torch.float64).contiguous()
+    sh = None if shift is None else shift.to(torch.float64).contiguous()
+    sg = None if sign is None else sign.to(torch.float64).contiguous()
+    for i0 in range(0, n, 65535):
+        i1 = min(n, i0 + 65535)
+        check("ed_cf_eval", lib().ed_cf_eval(
+            _stream(stream), i1 - i0, m, _ptr(a[i0:i1], (i1 - i0) * m, "alpha"),
+            _ptr(b[i0:i1], (i1 - i0) * (m + 1), "beta"), zc.numel(), _ptr(torch.view_as_real(zc)),
+            None if sh is None else _ptr(sh[i0:i1], i1 - i0, "shift"),
+            None if sg is None else _ptr(sg[i0:i1], i1 - i0, "sign"), _ptr(torch.view_as_real(out[i0:i1]))))
+    return out
 
 
 def lanczos_state_doubles(mmax: int) -> int:

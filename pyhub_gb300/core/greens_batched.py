@@ -249,17 +249,11 @@ def batched_ground_states(sectors, nsteps: int = 120, tol: float = 1e-10, max_re
 def continued_fraction(alpha, beta, z, sign: float = 1.0):
     """beta_0^2 / (z - s a_0 - b_1^2 / (z - s a_1 - ...)) for every instance
     (rows of alpha [n, m], beta [n, m+1]) at every z (1-D complex tensor);
-    sign=-1 evaluates <phi|(z + H)^-1|phi>.  Returns [n, len(z)]."""
+    sign=-1 evaluates <phi|(z + H)^-1|phi>.  Returns [n, len(z)] (one thread
+    per instance and frequency, ed_cf_eval)."""
     torch = _torch()
-    a = alpha.to(torch.complex128)
-    b2 = (beta[:, 1:alpha.shape[1]] ** 2).to(torch.complex128)
-    zz = z.to(torch.complex128)[None, :]
-    g = torch.zeros((alpha.shape[0], zz.shape[1]), dtype=torch.complex128, device=alpha.device)
-    m = alpha.shape[1]
-    for k in range(m - 1, -1, -1):
-        tail = b2[:, k:k + 1] * g if k < m - 1 else 0.0
-        g = 1.0 / (zz - sign * a[:, k:k + 1] - tail)
-    return (beta[:, :1] ** 2).to(torch.complex128) * g
+    sg = torch.full((alpha.shape[0],), float(sign), dtype=torch.float64, device=alpha.device)
+    return _capi.cf_eval(alpha, beta, torch.as_tensor(z, device=alpha.device), sign=sg)
 
 
 def plain_coefficients(sec, phi, nsteps: int):
@@ -374,11 +368,11 @@ def sweep(clusters, nsteps: int = 150, chunk: int = 64, dtype=None, gs_steps: in
             bl.run()
         torch.cuda.synchronize()
         t3 = time.perf_counter()
+        # greater: <phi|(w + E0 + i eta - H)^-1|phi>; lesser: <phi|(w - E0 + i eta + H)^-1|phi>
+        sg = torch.tensor([1.0 if p == "greater" else -1.0 for (_, _, p, _) in inst], dtype=torch.float64,
+                          device="cuda")
         e0s = torch.tensor([gsb.e0[ci] for (ci, _, _, _) in inst], dtype=torch.float64, device="cuda")
-        greater = torch.tensor([p == "greater" for (_, _, p, _) in inst], device="cuda")
-        zg = omega[None, :] + e0s[:, None] + 1j * eta
-        zl = omega[None, :] - e0s[:, None] + 1j * eta
-        G = torch.where(greater[:, None], _cf_rows(bl.alpha, bl.beta, zg, 1.0), _cf_rows(bl.alpha, bl.beta, zl, -1.0))
+        G = _capi.cf_eval(bl.alpha, bl.beta, omega.to(torch.complex128) + 1j * eta, shift=sg * e0s, sign=sg)
         for ci in range(len(cl)):
             norb = cl[ci]["t"].shape[0]
             g = G[base[ci]: base[ci] + 4 * norb].view(2, 2, norb, -1).sum(dim=1)
@@ -415,14 +409,3 @@ def _build_sectors(jobs, workers: int = 8):
         return list(ex.map(make, jobs))
 
 
-def _cf_rows(alpha, beta, z, sign):
-    """continued_fraction with one z row per instance ([n, nw] complex)."""
-    torch = _torch()
-    a = alpha.to(torch.complex128)
-    b2 = (beta[:, 1:alpha.shape[1]] ** 2).to(torch.complex128)
-    g = torch.zeros_like(z, dtype=torch.complex128)
-    m = alpha.shape[1]
-    for k in range(m - 1, -1, -1):
-        tail = b2[:, k:k + 1] * g if k < m - 1 else 0.0
-        g = 1.0 / (z - sign * a[:, k:k + 1] - tail)
-    return (beta[:, :1] ** 2).to(torch.complex128) * g

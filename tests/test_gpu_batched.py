@@ -219,3 +219,30 @@ def test_kept_basis_matches_replay(edlib, dtype):
     tol = 1e-13 if dtype == "float64" else 1e-6
     assert float(torch.linalg.vector_norm((outs[0] - outs[1]).double())) <= tol * float(
         torch.linalg.vector_norm(outs[0].double()))
+
+
+def test_cf_eval_shift_and_sign(edlib):
+    """ed_cf_eval against a numpy continued fraction (complex128, bottom-up),
+    per-instance shift and sign, at 1e-12 relative."""
+    import torch
+    from pyhub_gb300 import _capi
+    rng = np.random.default_rng(3)
+    n, m = 7, 40
+    alpha = rng.uniform(-4, 4, (n, m))
+    beta = np.abs(rng.normal(1.0, 0.5, (n, m + 1)))
+    beta[3, 17:] = 0.0       # an exhausted Krylov space: the fraction ends there
+    z = np.linspace(-9, 9, 301) + 0.05j
+    shift = rng.uniform(-5, 5, n)
+    sign = np.where(rng.random(n) < 0.5, 1.0, -1.0)
+    dev = "cuda"
+    got = _capi.cf_eval(torch.tensor(alpha, device=dev), torch.tensor(beta, device=dev),
+                        torch.tensor(z, device=dev), shift=torch.tensor(shift, device=dev),
+                        sign=torch.tensor(sign, device=dev)).cpu().numpy()
+    for i in range(n):
+        zz = z + shift[i]
+        g = np.zeros_like(zz)
+        for k in range(m - 1, -1, -1):
+            tail = beta[i, k + 1] ** 2 * g if k < m - 1 else 0.0
+            g = 1.0 / (zz - sign[i] * alpha[i, k] - tail)
+        ref = beta[i, 0] ** 2 * g
+        assert np.abs(got[i] - ref).max() <= 1e-12 * np.abs(ref).max(), i
