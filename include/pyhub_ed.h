@@ -177,6 +177,13 @@ int ed_rdm(ed_sector *s, void *stream, int dtype, int64_t ld, const void *bra, c
  * operators. */
 int ed_gf_start(const ed_sector *src, const ed_sector *dst, void *stream, int kind, int site,
                 int dtype, int64_t ld0, const void *psi, int out_dtype, int64_t ld1, void *out);
+/* ed_gf_start for nsites sites (host array, 1-based, at most 32) in one
+ * launch: the vector of sites[j] starts j*out_stride elements into out
+ * (out_stride >= one vector of the target sector).  The loop over sites of
+ * LCZ_{H,E}_{UP,DOWN} (spgf_bandlanczos.f90:453-560) for one operator. */
+int ed_gf_start_sites(const ed_sector *src, const ed_sector *dst, void *stream, int kind, int nsites,
+                      const int32_t *sites, int dtype, int64_t ld0, const void *psi, int out_dtype,
+                      int64_t ld1, void *out, int64_t out_stride);
 
 /* A batch of independent three-term Lanczos runs, one per instance, each on
  * its own Hubbard sector (e.g. every particle/hole start vector of every

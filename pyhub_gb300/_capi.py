@@ -51,6 +51,7 @@ _SIGS = {
     "ed_batch_lanczos_kept": (_I, [_P, _P, _I, _P, _P, _P, _I, _P, _P, _P, _I64]),
     "ed_batch_ritz_sum": (_I, [_P, _P, _I, _P, _I, _P, _P, _P]),
     "ed_cf_eval": (_I, [_P, _I, _I, _P, _P, _I, _P, _P, _P, _P]),
+    "ed_gf_start_sites": (_I, [_P, _P, _P, _I, _I, _P, _I, _I64, _P, _I, _I64, _P, _I64]),
     "ed_lanczos_coef": (_I, [_P, _I, _I, _P, _P, _P, _P, _P, _P]),
 }
 
@@ -366,6 +367,17 @@ def gf_start(src: "Sector", dst: "Sector", kind: str, site: int, psi, out, strea
     check("ed_gf_start", lib().ed_gf_start(src.handle, dst.handle, _stream(stream), GF_KINDS[kind], int(site),
                                            dtype_code(psi.dtype), src.ld, _ptr(psi, src._need(src.ld), "psi"),
                                            dtype_code(out.dtype), dst.ld, _ptr(out, dst._need(dst.ld), "out")))
+
+
+def gf_start_sites(src: "Sector", dst: "Sector", kind: str, sites, psi, out, stride: int, stream=None):
+    """gf_start for several sites in one launch: site sites[j]'s vector starts
+    j*stride elements into out (a 1-D tensor)."""
+    sites = np.ascontiguousarray(np.asarray(sites, dtype=np.int32))
+    ns = len(sites)
+    need = (ns - 1) * int(stride) + dst._need(dst.ld) if ns else 0
+    check("ed_gf_start_sites", lib().ed_gf_start_sites(
+        src.handle, dst.handle, _stream(stream), GF_KINDS[kind], ns, sites.ctypes.data, dtype_code(psi.dtype), src.ld,
+        _ptr(psi, src._need(src.ld), "psi"), dtype_code(out.dtype), dst.ld, _ptr(out, need, "out"), int(stride)))
 
 
 def multidot(V, nvec: int, w, out, scratch, z=None, n: int | None = None, stream=None):

@@ -93,7 +93,9 @@ class BatchedLanczos:
             keep = (self.nsteps + 2) * tot * es <= 0.5 * free
         self.keep = bool(keep)
         self.basis = torch.empty((self.nsteps + 1) * tot, dtype=self.dtype, device=device) if keep else None
-        self.work = torch.zeros((1 if keep else 3) * tot, dtype=self.dtype, device=device)
+        # the run fills its Krylov slots itself (a copy of x0, a cleared u_{-1}) and the H*v
+        # writes every element of y, row padding included
+        self.work = torch.empty((1 if keep else 3) * tot, dtype=self.dtype, device=device)
         self.x0 = torch.zeros(tot, dtype=self.dtype, device=device)
         self.alpha = torch.zeros((n, self.nsteps), dtype=torch.float64, device=device)
         self.beta = torch.zeros((n, self.nsteps + 1), dtype=torch.float64, device=device)
@@ -356,9 +358,24 @@ def sweep(clusters, nsteps: int = 150, chunk: int = 64, dtype=None, gs_steps: in
         t1 = time.perf_counter()
         bl = BatchedLanczos(secs, nsteps, dtype=dtype, rows=rows)
         rows_used.append(bl.rows)
-        for i, (ci, spin, part, site) in enumerate(inst):
+        # one launch per (cluster, spin, part): its sites are consecutive instances of one sector,
+        # equally spaced in the batch
+        i = 0
+        while i < len(inst):
+            ci, spin, part, _ = inst[i]
+            j = i
+            while j < len(inst) and inst[j][:3] == (ci, spin, part):
+                j += 1
             kind = ("e_" if part == "greater" else "h_") + spin
-            _capi.gf_start(srcs[ci], secs[i], kind, site, gsb.psi[ci], bl.start(i))
+            off = bl.batch.offsets
+            stride = int(off[i + 1] - off[i]) if j - i > 1 else 0
+            if j - i > 1 and any(int(off[q + 1] - off[q]) != stride for q in range(i, j - 1)):
+                for q in range(i, j):
+                    _capi.gf_start(srcs[ci], secs[q], kind, inst[q][3], gsb.psi[ci], bl.start(q))
+            else:
+                _capi.gf_start_sites(srcs[ci], secs[i], kind, [inst[q][3] for q in range(i, j)], gsb.psi[ci],
+                                     bl.x0[int(off[i]):], stride)
+            i = j
         torch.cuda.synchronize()
         t2 = time.perf_counter()
         if graph:

@@ -17,12 +17,22 @@ struct GfArgs {
     double sgn_dn_parity;     // (-1)^(N_down of psi) for the up operators
 };
 
+// Sites of one multi-site launch (blockIdx.y picks one; its vector starts
+// blockIdx.y * out_stride elements into out).
+struct GfSites {
+    int n;
+    int site[kMaxSites];
+    int64_t out_stride;
+};
+
 template <typename T, typename O>
-__global__ void gf_start_kernel(const T *__restrict__ psi, O *__restrict__ out, const GfArgs a)
+__global__ void gf_start_kernel(const T *__restrict__ psi, O *__restrict__ out, const GfArgs a, const GfSites ss)
 {
-    const uint32_t bi = 1u << (a.norb - a.site);
+    const int site = ss.site[blockIdx.y];
+    out += (int64_t)blockIdx.y * ss.out_stride;
+    const uint32_t bi = 1u << (a.norb - site);
     // string bits of the sites before `site`: bits norb-1 .. norb-site+1
-    const uint32_t above = (a.site >= 2) ? (((a.norb >= 32) ? 0xFFFFFFFFu : ((1u << a.norb) - 1u)) & ~((bi << 1) - 1u)) : 0u;
+    const uint32_t above = (site >= 2) ? (((a.norb >= 32) ? 0xFFFFFFFFu : ((1u << a.norb) - 1u)) & ~((bi << 1) - 1u)) : 0u;
     const int64_t n = a.nsup1 * a.nsdn1;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t d = e / a.nsup1, u = e - d * a.nsup1;
@@ -53,15 +63,15 @@ __global__ void gf_start_kernel(const T *__restrict__ psi, O *__restrict__ out, 
 
 using namespace ed;
 
-extern "C" int ed_gf_start(const ed_sector *src, const ed_sector *dst, void *stream, int kind, int site,
+static int gf_start_launch(const ed_sector *src, const ed_sector *dst, void *stream, int kind, const GfSites &ss,
                            int dtype, int64_t ld0, const void *psi, int out_dtype, int64_t ld1, void *out)
 {
-    clear_error();
     ED_REQUIRE(src != nullptr && dst != nullptr && psi != nullptr && out != nullptr, "NULL argument");
     ED_REQUIRE(src->kind == ED_HUBBARD && dst->kind == ED_HUBBARD, "Green's function start vectors need Hubbard sectors");
     ED_REQUIRE(src->norb == dst->norb, "sectors of different sizes");
     ED_REQUIRE(kind >= 0 && kind <= 3, "kind must be 0..3");
-    ED_REQUIRE(site >= 1 && site <= src->norb, "site %d outside 1..%d", site, src->norb);
+    for (int j = 0; j < ss.n; ++j)
+        ED_REQUIRE(ss.site[j] >= 1 && ss.site[j] <= src->norb, "site %d outside 1..%d", ss.site[j], src->norb);
     const int dup = (kind == 0) ? -1 : (kind == 2 ? 1 : 0);
     const int ddn = (kind == 1) ? -1 : (kind == 3 ? 1 : 0);
     ED_REQUIRE(dst->nup == src->nup + dup && dst->ndn == src->ndn + ddn,
@@ -69,9 +79,9 @@ extern "C" int ed_gf_start(const ed_sector *src, const ed_sector *dst, void *str
     ED_REQUIRE(ld0 >= src->nsup && ld1 >= dst->nsup, "ld below nsup");
     ED_REQUIRE(dtype == ED_F32 || dtype == ED_F64, "bad dtype");
     ED_REQUIRE(out_dtype == ED_F32 || out_dtype == ED_F64, "bad out_dtype");
-    if (dst->dim == 0) return ED_OK;
+    if (dst->dim == 0 || ss.n == 0) return ED_OK;
     GfArgs a;
-    a.norb = src->norb; a.kind = kind; a.site = site;
+    a.norb = src->norb; a.kind = kind; a.site = ss.site[0];
     a.nsup1 = dst->nsup; a.nsdn1 = dst->nsdn; a.ld1 = ld1; a.ld0 = ld0;
     a.ustr1 = dst->up.str; a.dstr1 = dst->dn.str; a.lut = dst->lut;
     a.sgn_dn_parity = (src->ndn & 1) ? -1.0 : 1.0;
@@ -79,14 +89,42 @@ extern "C" int ed_gf_start(const ed_sector *src, const ed_sector *dst, void *str
     int64_t blocks = (dst->dim + 255) / 256;
     const int64_t cap = (int64_t)num_sms() * 16;
     if (blocks > cap) blocks = cap;
+    const dim3 grid((unsigned)blocks, (unsigned)ss.n);
     if (dtype == ED_F64 && out_dtype == ED_F64)
-        gf_start_kernel<double, double><<<(unsigned)blocks, 256, 0, st>>>((const double *)psi, (double *)out, a);
+        gf_start_kernel<double, double><<<grid, 256, 0, st>>>((const double *)psi, (double *)out, a, ss);
     else if (dtype == ED_F64)
-        gf_start_kernel<double, float><<<(unsigned)blocks, 256, 0, st>>>((const double *)psi, (float *)out, a);
+        gf_start_kernel<double, float><<<grid, 256, 0, st>>>((const double *)psi, (float *)out, a, ss);
     else if (out_dtype == ED_F64)
-        gf_start_kernel<float, double><<<(unsigned)blocks, 256, 0, st>>>((const float *)psi, (double *)out, a);
+        gf_start_kernel<float, double><<<grid, 256, 0, st>>>((const float *)psi, (double *)out, a, ss);
     else
-        gf_start_kernel<float, float><<<(unsigned)blocks, 256, 0, st>>>((const float *)psi, (float *)out, a);
+        gf_start_kernel<float, float><<<grid, 256, 0, st>>>((const float *)psi, (float *)out, a, ss);
     ED_CHECK_LAUNCH();
     return ED_OK;
+}
+
+extern "C" int ed_gf_start(const ed_sector *src, const ed_sector *dst, void *stream, int kind, int site,
+                           int dtype, int64_t ld0, const void *psi, int out_dtype, int64_t ld1, void *out)
+{
+    clear_error();
+    GfSites ss;
+    ss.n = 1;
+    ss.site[0] = site;
+    ss.out_stride = 0;
+    return gf_start_launch(src, dst, stream, kind, ss, dtype, ld0, psi, out_dtype, ld1, out);
+}
+
+extern "C" int ed_gf_start_sites(const ed_sector *src, const ed_sector *dst, void *stream, int kind, int nsites,
+                                 const int32_t *sites, int dtype, int64_t ld0, const void *psi, int out_dtype,
+                                 int64_t ld1, void *out, int64_t out_stride)
+{
+    clear_error();
+    ED_REQUIRE(nsites >= 0 && nsites <= kMaxSites, "nsites=%d outside 0..%d", nsites, kMaxSites);
+    ED_REQUIRE(nsites == 0 || sites != nullptr, "sites is NULL");
+    ED_REQUIRE(dst != nullptr && (nsites <= 1 || out_stride >= (dst->nsdn - 1) * ld1 + dst->nsup),
+               "out_stride below one vector");
+    GfSites ss;
+    ss.n = nsites;
+    for (int j = 0; j < nsites; ++j) ss.site[j] = sites[j];
+    ss.out_stride = out_stride;
+    return gf_start_launch(src, dst, stream, kind, ss, dtype, ld0, psi, out_dtype, ld1, out);
 }

@@ -82,6 +82,26 @@ def test_gf_start_vectors_exact(edlib, case):
             assert np.array_equal(got, ref[site - 1])
 
 
+def test_gf_start_sites_equals_per_site(edlib):
+    """ed_gf_start_sites (all sites in one launch, vectors a stride apart)
+    writes exactly what ed_gf_start writes site by site."""
+    import torch
+    norb, nu, nd = 6, 3, 2
+    t, U, rng = _state(norb, nu, nd, 5)
+    src = edlib.Sector(norb, nu, nd, edlib.ED_HUBBARD, t=t, U=U)
+    psi = src.from_ref(torch.tensor(rng.standard_normal(src.dim), device="cuda"))
+    for kind, (du, dd) in (("h_up", (-1, 0)), ("e_down", (0, 1))):
+        dst = edlib.Sector(norb, nu + du, nd + dd, edlib.ED_HUBBARD, t=t, U=U)
+        stride = dst.n + 32
+        out = torch.full((norb * stride,), float("nan"), dtype=torch.float32, device="cuda")
+        edlib.gf_start_sites(src, dst, kind, list(range(1, norb + 1)), psi, out, stride)
+        for site in range(1, norb + 1):
+            ref = torch.zeros(dst.n, dtype=torch.float32, device="cuda")
+            edlib.gf_start(src, dst, kind, site, psi, ref)
+            got = out[(site - 1) * stride: (site - 1) * stride + dst.n]
+            assert torch.equal(dst.to_ref(got), dst.to_ref(ref)), (kind, site)
+
+
 def test_gf_poles_match_lehmann(edlib):
     """Small 6-site cluster: the continued-fraction poles give the exact
     Lehmann G_ij(w) of SPGF_ED on a frequency grid, and fh.gf -- which, like
