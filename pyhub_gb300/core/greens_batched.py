@@ -321,7 +321,7 @@ def sweep(clusters, nsteps: int = 150, chunk: int = 64, dtype=None, gs_steps: in
     timings = {} if timings is None else timings
     omega = omega if omega is not None else torch.linspace(-10.0, 10.0, 2048, dtype=torch.float64, device="cuda")
     results = {}
-    t_gs = t_start = t_lz = t_cf = 0.0
+    t_gs = t_start = t_lz = t_cf = t_sec = 0.0
     n_inst = 0
     restarts = 0
     rows_used = []
@@ -337,6 +337,7 @@ def sweep(clusters, nsteps: int = 150, chunk: int = 64, dtype=None, gs_steps: in
             N = spec["N"]
             shapes.append([(N, N), (N + 1, N), (N - 1, N), (N, N + 1), (N, N - 1)])
         built = _build_sectors([(spec, key) for spec, keys in zip(cl, shapes) for key in keys])
+        t_sec += time.perf_counter() - t0
         srcs = []
         for ci, spec in enumerate(cl):
             norb = spec["t"].shape[0]
@@ -403,7 +404,7 @@ def sweep(clusters, nsteps: int = 150, chunk: int = 64, dtype=None, gs_steps: in
         n_inst += len(inst)
         del bl, secs, srcs, gsb, built
         torch.cuda.empty_cache()
-    timings.update({"ground_states_s": t_gs, "start_vectors_s": t_start, "lanczos_s": t_lz, "cf_eval_s": t_cf,
+    timings.update({"ground_states_s": t_gs, "sectors_s": t_sec, "start_vectors_s": t_start, "lanczos_s": t_lz, "cf_eval_s": t_cf,
                     "instances": n_inst, "total_s": t_gs + t_start + t_lz + t_cf, "gs_restarts": restarts,
                     "rows_per_cta": rows_used})
     return results
