@@ -12,9 +12,16 @@ Differences from the reference, by design:
     G = V^T V is known exactly and the projection w - V G^-1 V^T w costs one
     more pass over V (delayed classical Gram-Schmidt, "DCGS2", Bielich,
     Langou, Thomas, Swirydowicz, Yamazaki, Boman, Parallel Computing 2022);
+  * the scalar work of a step (Gram row, inverse-Cholesky row, projection
+    coefficients, alpha, beta) runs on the device (ed_lanczos_coef), so the
+    steps enqueue without host synchronisation; the host reads alpha/beta at
+    convergence checks only;
   * vectors may be stored in FP32 while every scalar (dots, norms, the
     tridiagonal, its eigensolve) is FP64, followed by an FP64 refinement
     Lanczos started from the FP32 Ritz vector;
+  * the three-term form (no reorthogonalisation, for bases too large for
+    full reorthogonalisation) keeps its Krylov vectors in HBM where they fit,
+    else rebuilds Ritz vectors by a second run;
   * the start vector is a seeded uniform[-0.5,0.5) draw (the reference's
     RAND()-0.5 is unseeded, lanczos.f90:22-25).
 
