@@ -136,10 +136,14 @@ class BatchedGroundStates:
     restarts: int           # FP64 cycles after the first (on the unconverged instances only)
 
 
-def _lowest_ritz(a, b, tol_break: float = 1e-12):
+def _lowest_ritz(a, b, tol_break: float = 1e-12, every: int = 10):
     """Lowest eigenpair of one instance's tridiagonal matrix, cut at the first
     vanishing beta (an exhausted Krylov space); returns (theta, y, estimate, m)
-    with the usual estimate beta_m |y_m| of the residual."""
+    with the usual estimate beta_m |y_m| of the residual.  The leading
+    m x m blocks, m = every, 2*every, ... and the whole run, are compared and
+    the one with the smallest estimate is kept: without reorthogonalisation
+    the lost orthogonality spoils the Ritz vector once the pair has converged
+    (a kept basis sums any prefix of its vectors)."""
     import scipy.linalg as sla
     scale = max(1.0, float(np.abs(a).max()) if a.size else 1.0)
     m = len(a)
@@ -149,8 +153,15 @@ def _lowest_ritz(a, b, tol_break: float = 1e-12):
             break
     if m == 1:
         return float(a[0]), np.ones(1), float(b[1]), 1
-    w, y = sla.eigh_tridiagonal(a[:m], b[1:m], select="i", select_range=(0, 0))
-    return float(w[0]), y[:, 0], float(b[m] * abs(y[m - 1, 0])), m
+    best = None
+    for mm in sorted(set(list(range(every, m, every)) + [m])):
+        if mm < 2:
+            continue
+        w, y = sla.eigh_tridiagonal(a[:mm], b[1:mm], select="i", select_range=(0, 0))
+        est = float(b[mm] * abs(y[mm - 1, 0]))
+        if best is None or est < best[2]:
+            best = (float(w[0]), y[:, 0], est, mm)
+    return best
 
 
 def _ritz_cycle(bl, out):
