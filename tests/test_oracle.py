@@ -236,3 +236,4 @@ def test_operator_algebra_recognises_hubbard_form():
     op.set_basis(Basis(5, (2, 3)))
     assert op._hubbard() is None          # spin-dependent one-body terms: averages only
     assert str(c_dagger_c((0, "u"), (1, "u"))) == "1.0*c^\\dagger_{0,u}c_{1,u}"
+
