@@ -101,11 +101,15 @@ def solve(params: HubbardParams, theta, nup: int, ndn: int, mode: str = "f64", s
     the spin-resolved 1-RDM (computed, not copied, for both spins)."""
     t, U = params.unpack(theta)
     sec = _capi.Sector(params.norb, nup, ndn, _capi.ED_HUBBARD, t=t, U=U)
-    # f64: one Lanczos run to the residual; mixed: the FP64 refinement runs to the same residual
-    # (the 1-RDM and the adjoint need psi itself, which an energy criterion converges only to its root)
-    rule = LZ.ResidualRule(tol, min_steps=10)
-    gs = LZ.ground_state(sec, mode=mode, steps=steps, seed=seed, rule=rule if mode == "f64" else None,
-                         refine_rule=None if mode == "f64" else LZ.ResidualRule(tol, min_steps=4))
+    # f64: one Lanczos run to the residual.  mixed: the FP32 stage stops near its own floor
+    # (Ritz residual estimate 1e-5; the basis traffic grows with the square of the steps), and the
+    # FP64 refinement runs to the residual tol (the 1-RDM and the adjoint need psi itself, which an
+    # energy criterion converges only to its root)
+    if mode == "f64":
+        rule, refine = LZ.ResidualRule(tol, min_steps=10), None
+    else:
+        rule, refine = LZ.ResidualRule(max(tol, 1e-5), min_steps=20), LZ.ResidualRule(tol, min_steps=4)
+    gs = LZ.ground_state(sec, mode=mode, steps=steps, seed=seed, rule=rule, refine_rule=refine)
     gamma = one_rdm(sec, gs.psi, params.norb)
     return Solution(e0=gs.e0, psi=gs.psi, sector=sec, gamma=gamma)
 
