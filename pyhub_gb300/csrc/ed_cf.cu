@@ -44,9 +44,9 @@ __global__ void __launch_bounds__(kCfThreads) cf_eval_kernel(int m, const double
     for (int k = m - 1; k >= 0; --k) {
         const double wr = zz.x - sa[k] - sb[k] * gr;
         const double wi = zz.y - sb[k] * gi;
-        const double d = wr * wr + wi * wi;
-        gr = wr / d;
-        gi = -wi / d;
+        const double inv = 1.0 / (wr * wr + wi * wi);   // one division per level (the FP64 pipe binds)
+        gr = wr * inv;
+        gi = -wi * inv;
     }
     const double b0 = beta[i * (m + 1)];
     out[i * nz + j] = make_double2(b0 * b0 * gr, b0 * b0 * gi);
