@@ -11,7 +11,7 @@
 namespace ed {
 
 struct GfArgs {
-    int norb, kind, site;     // kind 0 h_up, 1 h_down, 2 e_up, 3 e_down; site 1-based
+    int norb, kind;           // kind 0 h_up, 1 h_down, 2 e_up, 3 e_down (the sites: GfSites)
     int64_t nsup1, nsdn1, ld1, ld0;
     const uint32_t *ustr1, *dstr1, *lut;
     double sgn_dn_parity;     // (-1)^(N_down of psi) for the up operators
@@ -81,7 +81,7 @@ static int gf_start_launch(const ed_sector *src, const ed_sector *dst, void *str
     ED_REQUIRE(out_dtype == ED_F32 || out_dtype == ED_F64, "bad out_dtype");
     if (dst->dim == 0 || ss.n == 0) return ED_OK;
     GfArgs a;
-    a.norb = src->norb; a.kind = kind; a.site = ss.site[0];
+    a.norb = src->norb; a.kind = kind;
     a.nsup1 = dst->nsup; a.nsdn1 = dst->nsdn; a.ld1 = ld1; a.ld0 = ld0;
     a.ustr1 = dst->up.str; a.dstr1 = dst->dn.str; a.lut = dst->lut;
     a.sgn_dn_parity = (src->ndn & 1) ? -1.0 : 1.0;
