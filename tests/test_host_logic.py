@@ -1,5 +1,6 @@
 """CPU tests of host-side logic of the engine that needs no GPU: the choice
-of Ritz pairs for the batched ground states."""
+of Ritz pairs for the batched ground states and the padding of kept Krylov
+rows."""
 import numpy as np
 
 
@@ -24,3 +25,26 @@ def test_lowest_ritz_takes_the_best_prefix():
     b2[25] = 0.0                       # Krylov space exhausted after 25 steps
     theta2, y2, est2, m2 = GB._lowest_ritz(a, b2, every=10)
     assert m2 <= 25
+
+
+def test_zero_padding_of_kept_rows():
+    """lanczos._zero_padding clears exactly the padding of each kept row: the
+    columns past nsup of every down-string row (Hubbard layout) or the tail
+    past dim (Heisenberg), and leaves every element of the vector alone."""
+    import torch
+    from types import SimpleNamespace
+    from pyhub_gb300 import _capi
+    from pyhub_gb300.core import lanczos as LZ
+    hub = SimpleNamespace(kind=_capi.ED_HUBBARD, nsup=5, nsdn=3, ld=8, n=24, dim=15)
+    rows = torch.full((4, hub.n), 7.0)
+    LZ._zero_padding(hub, rows)
+    v = rows.view(4, hub.nsdn, hub.ld)
+    assert bool((v[:, :, hub.nsup:] == 0).all()) and bool((v[:, :, :hub.nsup] == 7).all())
+    heis = SimpleNamespace(kind=_capi.ED_HEISENBERG, nsup=70, nsdn=1, ld=70, n=96, dim=70)
+    rows = torch.full((3, heis.n), 7.0)
+    LZ._zero_padding(heis, rows)
+    assert bool((rows[:, heis.dim:] == 0).all()) and bool((rows[:, :heis.dim] == 7).all())
+    flat = SimpleNamespace(kind=_capi.ED_HEISENBERG, nsup=64, nsdn=1, ld=64, n=64, dim=64)
+    rows = torch.full((2, 64), 7.0)
+    LZ._zero_padding(flat, rows)
+    assert bool((rows == 7).all())
