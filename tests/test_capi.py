@@ -70,3 +70,35 @@ def test_pointer_checks_refuse_host_and_short_tensors():
     with pytest.raises(ValueError, match="CUDA tensor"):
         _capi._ptr(torch.zeros(8), 4, "x")
     assert _capi._ptr(None) is None
+
+
+def test_lanczos_state_size_and_limits(edlib):
+    """ed_lanczos_state_doubles: stop code, Gram maximum, mmax+1 scales, the
+    (mmax+1)^2 inverse Cholesky factor and four work vectors; -1 outside
+    1..8192 (and the Python wrapper raises)."""
+    L = edlib.lib()
+    for m in (1, 200, 8192):
+        assert L.ed_lanczos_state_doubles(m) == 3 + m + (m + 1) ** 2 + 4 * (m + 1)
+    assert L.ed_lanczos_state_doubles(0) == -1 and L.ed_lanczos_state_doubles(8193) == -1
+    with pytest.raises(ValueError):
+        edlib.lanczos_state_doubles(9000)
+
+
+def test_new_entry_points_reject_bad_arguments(edlib):
+    """The device Lanczos step, the continued fractions, the multi-site start
+    vectors and the kept-basis batch refuse bad arguments on the host, with a
+    message, before any launch."""
+    L = edlib.lib()
+    ARG = edlib.ED_ERR_ARG
+    assert L.ed_lanczos_coef(None, 0, 0, None, None, None, None, None, None) == ARG
+    assert "mmax" in L.ed_last_error().decode()
+    assert L.ed_lanczos_coef(None, 5, 4, None, None, None, None, None, None) == ARG   # k > mmax
+    assert L.ed_cf_eval(None, 1, 0, None, None, 4, None, None, None, None) == ARG    # no levels
+    assert L.ed_cf_eval(None, 1, 5000, None, None, 4, None, None, None, None) == ARG  # > 3000 levels
+    assert "3000" in L.ed_last_error().decode()
+    assert L.ed_cf_eval(None, 0, 10, None, None, 4, None, None, None, None) == edlib.ED_OK   # nothing to do
+    sites = (ctypes.c_int32 * 40)(*range(1, 41))
+    assert L.ed_gf_start_sites(None, None, None, 0, 40, sites, 0, 0, None, 0, 0, None, 0) == ARG
+    assert "nsites" in L.ed_last_error().decode()
+    assert L.ed_batch_ritz_sum(None, None, 0, None, 10, None, None, None) == ARG
+    assert L.ed_batch_lanczos_kept(None, None, 0, None, None, None, 10, None, None, None, 0) == ARG
