@@ -271,12 +271,15 @@ def lanczos_full(sec, v0, max_steps: int, dtype=None, rule=None, check_every: in
     def post(k):
         """close(k) with the copies left in flight: (k, event, host buffers)."""
         _capi.lanczos_coef(k, m, None, ws.nrm, state, None, ab[0], ab[1])
-        hs = torch.empty(2, dtype=torch.float64, pin_memory=True)
-        hab = torch.empty((2, k), dtype=torch.float64, pin_memory=True)
-        hs.copy_(state[:2], non_blocking=True)
-        hab.copy_(ab[:, :k], non_blocking=True)
-        ev = torch.cuda.Event()
-        ev.record()
+        cuda = state.is_cuda
+        hs = torch.empty(2, dtype=torch.float64, pin_memory=cuda)
+        hab = torch.empty((2, k), dtype=torch.float64, pin_memory=cuda)
+        hs.copy_(state[:2], non_blocking=cuda)
+        hab.copy_(ab[:, :k], non_blocking=cuda)
+        ev = None
+        if cuda:
+            ev = torch.cuda.Event()
+            ev.record()
         return k, ev, hs, hab
 
     def judge(k, stop, alpha, beta):
@@ -315,7 +318,8 @@ def lanczos_full(sec, v0, max_steps: int, dtype=None, rule=None, check_every: in
             # the check posted after the previous step, read while this step runs
             kc, ev, hs, hab = pending
             pending = None
-            ev.synchronize()
+            if ev is not None:
+                ev.synchronize()
             st_c, g_c = int(hs[0]), float(hs[1])
             a_c, b_c = hab[0].numpy().copy(), hab[1].numpy().copy()
             if judge(kc, st_c, a_c, b_c):
