@@ -540,7 +540,8 @@ def lanczos_plain(sec, v0, max_steps: int, rule=None, check_every: int = NADD, n
 
     t_run = time.perf_counter()
     alpha, beta, done, conv, scales = run(m)    # scales is None when the kept rows ran out
-    torch.cuda.synchronize()
+    if v0.is_cuda:
+        torch.cuda.synchronize()
     t_run = time.perf_counter() - t_run
     val, vec = _tridiag_eigs(alpha, beta, done, vectors=True)
     t_ritz = time.perf_counter()
@@ -562,7 +563,8 @@ def lanczos_plain(sec, v0, max_steps: int, rule=None, check_every: int = NADD, n
             for p in psis:
                 _capi.multidot(p.view(1, -1), 1, p, ws.dots, ws.buf)
                 p.mul_(1.0 / math.sqrt(float(ws.dots[0].item())))
-    torch.cuda.synchronize()
+    if v0.is_cuda:
+        torch.cuda.synchronize()
     t_ritz = time.perf_counter() - t_ritz
     return PlainResult(alpha=alpha, beta=beta, ritz=val, ritz_vectors=vec, steps=done, converged=conv,
                        psis=psis, times={"total": time.perf_counter() - t0, "alloc": t_alloc, "run": t_run,

@@ -1,6 +1,7 @@
-"""CPU tests of the host control flow of the full-reorthogonalisation Lanczos
-(core.lanczos.lanczos_full): rule checks with and without the one-step
-lookahead, the device stop codes, truncation at a breakdown.  The C-ABI calls
+"""CPU tests of the host control flow of the Lanczos drivers
+(core.lanczos): for lanczos_full, rule checks with and without the one-step
+lookahead, the device stop codes, truncation at a breakdown; for
+lanczos_plain, the kept rows, the move to rotating vectors and the replay.  The C-ABI calls
 are replaced by torch stand-ins on CPU tensors; the stand-in of
 ed_lanczos_coef restates the kernel's arithmetic (csrc/ed_lanczos.cu) so the
 device state follows the same protocol."""
@@ -20,6 +21,9 @@ class FakeSector:
 
     def hv(self, x, y, scale=1.0, dots=None, scratch=None, ld=None, stream=None):
         y.copy_((scale * (self.H @ x.double())).to(y.dtype))
+        if dots is not None:
+            dots[0] = float(x.double() @ y.double())
+            dots[1] = float(y.double() @ y.double())
 
 
 def fake_multidot(V, nvec, w, out, scratch, z=None, n=None, stream=None):
@@ -141,3 +145,25 @@ def test_exhausted_krylov_space_stops_the_run(stand_ins):
         assert r.breakdown and r.converged and r.steps <= 12
         assert abs(r.ritz[0] - e) < 1e-10
         assert bool(torch.isfinite(r.psi).all())
+
+
+def test_three_term_schedules_agree(stand_ins):
+    """lanczos_plain with all rows kept, with 12 rows (the run moves to the
+    rotating vectors, then replays on the same schedule) and with none
+    (replay): the same coefficients to rounding and the same Ritz vectors."""
+    LZ = stand_ins
+    H = _matrix(90, 7)
+    sec = FakeSector(H)
+    v0 = torch.tensor(np.random.default_rng(8).uniform(-0.5, 0.5, 90))
+    storage = torch.empty(41 * 90 * 8, dtype=torch.uint8)
+    runs = [LZ.lanczos_plain(sec, v0, 40, nvec=2, keep=k, storage=storage) for k in (True, 12, False)]
+    assert [r.times["replayed"] for r in runs] == [False, True, True]
+    assert runs[0].times["kept_rows"] == 41 and runs[1].times["kept_rows"] == 12
+    for r in runs[1:]:
+        assert r.steps == runs[0].steps == 40
+        assert np.allclose(r.alpha, runs[0].alpha, rtol=1e-12, atol=0)
+        assert np.allclose(r.beta, runs[0].beta, rtol=1e-12, atol=0)
+        for p, q in zip(r.psis, runs[0].psis):
+            assert float(torch.linalg.vector_norm(p - q)) < 1e-10
+    e = np.linalg.eigvalsh(H.numpy())[0]
+    assert abs(runs[0].ritz[0] - e) < 1e-6
