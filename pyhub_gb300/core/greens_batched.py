@@ -372,22 +372,16 @@ def sweep(clusters, nsteps: int = 150, chunk: int = 64, dtype=None, gs_steps: in
         rows_used.append(bl.rows)
         # one launch per (cluster, spin, part): its sites are consecutive instances of one sector,
         # equally spaced in the batch
-        i = 0
-        while i < len(inst):
+        off = bl.batch.offsets
+        for i, j, stride in _site_groups(inst, off):
             ci, spin, part, _ = inst[i]
-            j = i
-            while j < len(inst) and inst[j][:3] == (ci, spin, part):
-                j += 1
             kind = ("e_" if part == "greater" else "h_") + spin
-            off = bl.batch.offsets
-            stride = int(off[i + 1] - off[i]) if j - i > 1 else 0
-            if j - i > 1 and any(int(off[q + 1] - off[q]) != stride for q in range(i, j - 1)):
+            if stride is None:
                 for q in range(i, j):
                     _capi.gf_start(srcs[ci], secs[q], kind, inst[q][3], gsb.psi[ci], bl.start(q))
             else:
                 _capi.gf_start_sites(srcs[ci], secs[i], kind, [inst[q][3] for q in range(i, j)], gsb.psi[ci],
                                      bl.x0[int(off[i]):], stride)
-            i = j
         torch.cuda.synchronize()
         t2 = time.perf_counter()
         if graph:
@@ -419,6 +413,25 @@ def sweep(clusters, nsteps: int = 150, chunk: int = 64, dtype=None, gs_steps: in
                     "instances": n_inst, "total_s": t_gs + t_start + t_lz + t_cf, "gs_restarts": restarts,
                     "rows_per_cta": rows_used})
     return results
+
+
+def _site_groups(inst, offsets):
+    """Runs [i, j) of consecutive instances with the same (cluster, spin,
+    part), and the constant distance of their slots in the batch (0 for a
+    single instance), or None when the slots are not equally spaced.
+    inst: [(cluster, spin, part, site)]; offsets: slot offsets by instance."""
+    out = []
+    i = 0
+    while i < len(inst):
+        j = i
+        while j < len(inst) and inst[j][:3] == inst[i][:3]:
+            j += 1
+        stride = int(offsets[i + 1] - offsets[i]) if j - i > 1 else 0
+        if j - i > 1 and any(int(offsets[q + 1] - offsets[q]) != stride for q in range(i, j - 1)):
+            stride = None
+        out.append((i, j, stride))
+        i = j
+    return out
 
 
 def _build_sectors(jobs, workers: int = 8):

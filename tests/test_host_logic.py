@@ -48,3 +48,15 @@ def test_zero_padding_of_kept_rows():
     rows = torch.full((2, 64), 7.0)
     LZ._zero_padding(flat, rows)
     assert bool((rows == 7).all())
+
+
+def test_site_groups_of_the_sweep():
+    """greens_batched._site_groups: runs of one (cluster, spin, part) and the
+    distance of their slots; irregular slots fall back to per-site launches."""
+    from pyhub_gb300.core import greens_batched as GB
+    inst = [(0, "up", "greater", s) for s in (1, 2, 3)] + [(0, "up", "lesser", 1)] + \
+        [(1, "down", "greater", s) for s in (1, 2)]
+    offsets = [0, 64, 128, 192, 224, 288]
+    assert GB._site_groups(inst, offsets) == [(0, 3, 64), (3, 4, 0), (4, 6, 64)]
+    irregular = [0, 64, 160, 192, 224, 288]
+    assert GB._site_groups(inst, irregular)[0] == (0, 3, None)
