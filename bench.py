@@ -57,6 +57,7 @@ def parse():
     p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison solve")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-c4", action="store_true", help="skip the batched Green's-function part of the default line")
     p.add_argument("--small", action="store_true", help="3x3 cluster, for a quick functional run")
     p.add_argument("--config", default="c2", choices=["c2", "c3", "c4", "c5"],
                    help="c2: 4x4 Hubbard ground-state solve (default); c3: 4x8 Heisenberg ground state and "
@@ -213,11 +214,41 @@ def cpu_sample(pairs_per_sample: int, n_udiag: int, U: float, nthreads: int = 0)
     return hv, tp + tu, f"{pairs_per_sample} of {len(pairs)} hop pairs + {n_udiag} of 16 U sites of one H*v", nthreads
 
 
+C2_REFINE_STEPS = 4   # FP64 refinement steps of the engine's C2 solve (measured: E0 settles after 4)
+
+
+def c2_config(args, dim: int, ws: int) -> dict:
+    """The workload description both arms print for the 4x4 solve."""
+    return {"workload": ("4x4 periodic Hubbard t=1 U=%g N_up=N_down=8 (D=%d) ground state: "
+                         "%d-step full-reorth Lanczos FP32 + FP64 refinement") % (args.U, dim, args.lanczos_steps),
+            "parallelism": f"replicas x{ws}", "l2": "vectors 0.66 GB >> L2; no flush needed"}
+
+
+def e0_oracle_check(t, U, psi, e0: float) -> dict:
+    """|dE0| of the mixed solve against the FP64 oracle: the Rayleigh quotient
+    <psi|H|psi>/<psi|psi> and the residual ||H psi - E0 psi|| / ||psi|| of the
+    engine's psi0 (reference layout, FP64 on the host), with H psi from the
+    reference's HPROD loop restated in C (hprod_hubbard.f90:17-118) on all
+    host threads."""
+    import numpy as np
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    osec = O.Sector(16, 8, 8)
+    hpsi = O.hprod_hubbard_mt(osec, t, U, psi)
+    nn = float(np.dot(psi, psi))
+    rq = float(np.dot(psi, hpsi)) / nn
+    r = hpsi - e0 * psi
+    return {"rayleigh_quotient": rq, "abs_dE0_vs_oracle": abs(rq - e0),
+            "residual": float(np.sqrt(np.dot(r, r) / nn)), "oracle_hv_seconds": time.perf_counter() - t0,
+            "oracle": f"reference HPROD loop restated in C on {host_threads()} host threads"}
+
+
 def run_reference(args):
     ws, rank, local = dist()
     if rank != 0:
         return
-    n_hv = args.lanczos_steps + 30   # same H*v count as one engine solve (FP32 steps + typical refinement)
+    # the same H*v count as one engine solve: the FP32 steps plus the FP64 refinement steps
+    n_hv = args.lanczos_steps + C2_REFINE_STEPS
     times = []
     for i in range(args.warmup + args.steps):
         hv, spent, desc, nth = cpu_sample(CPU_PAIRS_REF, 4, args.U)
@@ -228,12 +259,12 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": solve_s * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded uniform start vector)",
-            "config": {"workload": "4x4 periodic Hubbard t=1 U=8 N_up=N_down=8 (D=165,636,900) ground state",
-                       "lanczos_steps": args.lanczos_steps, "hv_per_solve": n_hv},
+            "data": "synthetic (seeded uniform[-0.5,0.5) start vector)",
+            "config": c2_config(args, 12870 * 12870, 1),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": nth, "kind": "port",
-                             "sample": f"{desc} per step; extrapolated to {n_hv} H*v (reference loop order, "
-                                       f"linear-search rank, on {nth} host threads; its HDF5 I/O is not counted)"},
+                             "sample": f"{desc} per step; extrapolated to the {n_hv} H*v of one solve (reference "
+                                       f"loop order, linear-search rank, on {nth} host threads; its HDF5 I/O is "
+                                       f"not counted)"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -288,74 +319,151 @@ def probe_c4(args):
     print(json.dumps({"probe": "ok", "instances": len(secs), "elements": int(bl.batch.total)}))
 
 
-def run_c4(args):
-    """Batched Green's functions: 256 seeded 12-site open clusters (2x6, 3x4),
-    ground state then 48 particle/hole start vectors x 150 Lanczos steps each,
-    G_ii(w) on 2048 points of [-10, 10] with eta = 0.05.  Timed: the batched
-    run (one CUDA-graph replay per chunk of 64 clusters) against the
-    per-instance three-term Lanczos on a sample of the same start vectors."""
+def c4_batched(args, ws: int, rank: int, local: int, warmup: int = 1) -> dict:
+    """Batched Green's functions (the metric's third part): 256 seeded 12-site
+    open clusters (2x6, 3x4), ground state then 48 particle/hole start vectors
+    x 150 Lanczos steps each, G_ii(w) on 2048 points of [-10, 10], eta = 0.05.
+    Clusters are sharded over the ranks (every rank sweeps its share, then
+    rank 0 gathers every cluster's G(w)).  Timed: the sweep (CUDA events on
+    the current stream); the batched Lanczos (one CUDA-graph replay per chunk
+    of 64 clusters) against per-instance runs of the same kernels on the same
+    start vectors, one instance per launch sequence with its scalars on the
+    device (no host synchronisation inside a run); and ed_batch_hv alone for
+    the roofline of the batched H*v kernel.  Returns the rank-0 summary (None
+    on other ranks)."""
     import numpy as np
     import torch
-    from pyhub_gb300 import _build
-    from pyhub_gb300.core import greens_batched as GB
+    from pyhub_gb300 import _capi
     from pyhub_gb300 import replicas as RP
-    _build.build()
-    ws, rank, local = RP.world()
-    torch.cuda.set_device(local)
-    RP.init("nccl")
+    from pyhub_gb300.core import greens_batched as GB
+    from pyhub_gb300.core import lanczos as LZ
     clusters = GB.c4_clusters(args.clusters, seed=0)
-    # every rank sweeps its own share of the clusters (no collective on the data path)
     mine = RP.shard(clusters, rank, ws)
     # warm-up on one cluster of each filling: the batched H*v form is tuned there
     # for every sector shape of the sweep (autotune keys on the distinct shapes)
     warm = list({spec["N"]: spec for spec in reversed(mine)}.values())
-    for _ in range(max(args.warmup, 1)):
+    for _ in range(max(warmup, 1)):
         GB.sweep(warm, nsteps=150, chunk=len(warm))
     RP.barrier()
-    clocks = ClockSampler(local)
-    clocks.start()
     tim = {}
     clock = StreamClock().start()
-    res = GB.sweep(mine, nsteps=150, chunk=64, timings=tim)
+    merged = GB.sharded_sweep(clusters, rank, ws, nsteps=150, chunk=64, timings=tim)
     elapsed_local = clock.stop()
     RP.barrier()
-    clk = clocks.stop()
     rate, total_gf, elapsed = RP.aggregate_rate(tim["instances"], elapsed_local)
-    # per-instance path on the start vectors of the first cluster
-    from pyhub_gb300 import _capi
-    from pyhub_gb300.core import lanczos as LZ
-    spec = mine[0]
+    lz_rate = RP.sum_over_ranks(tim["instances"]) / RP.max_over_ranks(tim["lanczos_s"])
+    if rank != 0:
+        return None
+    # G(w) of every cluster is on rank 0 now
+    gsum = float(sum(np.abs(v["G"]).sum() for v in merged.values()))
+    # per-instance runs: the 48 start vectors of the first cluster, one batch of one instance each
+    spec = clusters[0]
     norb, N = spec["t"].shape[0], spec["N"]
     U = np.full(norb, spec["U"])
     src = _capi.Sector(norb, N, N, _capi.ED_HUBBARD, t=spec["t"], U=U)
     gs = LZ.ground_state(src, mode="f64", steps=200, rule=LZ.ResidualRule(1e-10, 10))
-    sample = []
+    rows = tim["rows_per_cta"][0] if tim.get("rows_per_cta") else 8
+    singles, starts, secs = [], [], []
     for spin, part in (("up", "greater"), ("up", "lesser"), ("down", "greater"), ("down", "lesser")):
         d = 1 if part == "greater" else -1
         key = (N + d, N) if spin == "up" else (N, N + d)
         dst = _capi.Sector(norb, key[0], key[1], _capi.ED_HUBBARD, t=spec["t"], U=U)
         for site in range(1, norb + 1):
-            phi = torch.zeros(dst.n, dtype=torch.float64, device="cuda")
-            _capi.gf_start(src, dst, ("e_" if part == "greater" else "h_") + spin, site, gs.psi, phi)
-            sample.append((dst, phi.float()))
+            bl1 = GB.BatchedLanczos([dst], 150, dtype=torch.float32, rows=rows)
+            _capi.gf_start(src, dst, ("e_" if part == "greater" else "h_") + spin, site, gs.psi, bl1.start(0))
+            singles.append(bl1)
+            secs.append(dst)
+    for bl1 in singles[:2]:
+        bl1.run()
     torch.cuda.synchronize()
     clock = StreamClock().start()
-    coef = [GB.plain_coefficients(dst, phi, 150) for dst, phi in sample]
-    t_plain = clock.stop() / len(sample)
+    for bl1 in singles:
+        bl1.run()
+    t_single = clock.stop() / len(singles)
+    # the same instances batched together (equal accuracy: the same kernels and sums)
+    blb = GB.BatchedLanczos(secs, 150, dtype=torch.float32, rows=rows)
+    for i, bl1 in enumerate(singles):
+        blb.start(i).copy_(bl1.start(0))
+    blb.run()
+    torch.cuda.synchronize()
+    a1 = torch.stack([b1.alpha[0] for b1 in singles]).cpu().numpy()
+    b1_ = torch.stack([b1.beta[0] for b1 in singles]).cpu().numpy()
+    same = bool(np.array_equal(a1, blb.alpha.cpu().numpy()) and np.array_equal(b1_, blb.beta.cpu().numpy()))
+    # batched H*v kernel alone on the last chunk's shape mix (one of every sector of 64 clusters)
+    hb = GB.BatchedLanczos(_c4_hv_sample(clusters[:64]), 1, dtype=torch.float32, rows=rows)
+    x = torch.rand(hb.batch.total, dtype=torch.float32, device="cuda")
+    for i in range(len(hb.sectors)):      # zero row padding, as every engine vector has
+        v = hb.batch.view(x, i).view(hb.sectors[i].nsdn, -1)
+        v[:, hb.sectors[i].nsup:] = 0
+    y = torch.empty_like(x)
+    for _ in range(3):
+        hb.batch.hv(x, y, hb.scratch)
+    torch.cuda.synchronize()
+    reps = 10
+    clock = StreamClock().start()
+    for _ in range(reps):
+        hb.batch.hv(x, y, hb.scratch)
+    t_hv = clock.stop() / reps
+    peak, src_kind = peaks()
+    alg = sum(s.dim for s in hb.sectors) * 8.0
     n_gf = tim["instances"]
-    gf_rate = n_gf / tim["lanczos_s"]
+    per_step_bytes = 24.0 * sum(s.dim for s in blb.sectors) / len(blb.sectors)   # H*v 8 B + update 16 B per element
+    out = {"workload": "256 clusters (128 2x6 + 128 3x4 open), t=1, t'~U[-0.3,0.3], U~U[0,8], N_up=N_down in "
+                       "{5,6}; GS + 48 start vectors x 150 Lanczos steps; 2048-point w grid, eta=0.05",
+           "value": rate, "unit": "GF/s", "seconds": elapsed, "gf_instances": int(total_gf),
+           "clusters_gathered_on_rank0": len(merged), "G_abs_sum": gsum, "timings": tim,
+           "batched_lanczos_gf_per_s": lz_rate, "per_instance_gf_per_s": 1.0 / t_single,
+           "batched_over_per_instance": lz_rate * t_single,
+           "per_instance_arm": ("the first cluster's 48 start vectors, each its own ed_batch_lanczos run "
+                                "(4 launches per step, scalars on the device, no host synchronisation), "
+                                "back to back on one stream; CUDA events"),
+           "per_instance_alpha_beta_equal_batched": same,
+           "batch_hv_roofline": {"kernel": "batch_hv_kernel", "bound": "hbm",
+                                 "achieved": alg / t_hv / 1e9, "peak": peak, "unit": "GB/s",
+                                 "frac": alg / t_hv / 1e9 / peak, "peak_kind": f"of {src_kind}",
+                                 "alg_bytes_per_launch": alg, "ms": t_hv * 1e3,
+                                 "instances": len(hb.sectors), "traffic": None},
+           "lanczos_step_bytes_per_instance": per_step_bytes}
+    del singles, blb, hb, x, y
+    torch.cuda.empty_cache()
+    return out
+
+
+def _c4_hv_sample(clusters):
+    """The particle/hole sectors of the given clusters (one per cluster, spin
+    and part): the shape mix of one sweep chunk, for timing the batched H*v."""
+    import numpy as np
+    from pyhub_gb300 import _capi
+    out = []
+    for spec in clusters:
+        norb, N = spec["t"].shape[0], spec["N"]
+        U = np.full(norb, spec["U"])
+        for key in [(N + 1, N), (N - 1, N), (N, N + 1), (N, N - 1)]:
+            out.append(_capi.Sector(norb, key[0], key[1], _capi.ED_HUBBARD, t=spec["t"], U=U))
+    return out
+
+
+def run_c4(args):
+    """The batched Green's-function sweep as its own JSON line."""
+    import torch
+    from pyhub_gb300 import _build
+    from pyhub_gb300 import replicas as RP
+    _build.build()
+    ws, rank, local = RP.world()
+    torch.cuda.set_device(local)
+    RP.init("nccl")
+    clocks = ClockSampler(local)
+    clocks.start()
+    r = c4_batched(args, ws, rank, local, warmup=args.warmup)
+    clk = clocks.stop()
     if rank == 0:
-        line = {"metric": METRIC, "value": rate, "unit": "GF/s", "n_gpus": ws, "steps": 1,
-                "warmup": max(args.warmup, 1), "ms_per_step": elapsed * 1e3, "higher_is_better": True,
+        line = {"metric": METRIC, "value": r["value"], "unit": "GF/s", "n_gpus": ws, "steps": 1,
+                "warmup": max(args.warmup, 1), "ms_per_step": r["seconds"] * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 vectors / f64 scalars",
                 "data": "synthetic (seeded cluster parameters)",
-                "config": {"workload": "256 clusters (128 2x6 + 128 3x4 open), t=1, t'~U[-0.3,0.3], U~U[0,8], "
-                                       "N_up=N_down in {5,6}; GS + 48 start vectors x 150 Lanczos steps; "
-                                       "2048-point w grid, eta=0.05", "clusters": len(mine),
+                "config": {"workload": r["workload"], "clusters": args.clusters,
                            "parallelism": f"clusters sharded over {ws} ranks"},
-                "gf_instances": int(total_gf), "gf_instances_rank0": n_gf, "timings": tim,
-                "batched_gf_per_s": gf_rate, "per_instance_gf_per_s": 1.0 / t_plain,
-                "batched_over_per_instance": gf_rate * t_plain, "clocks": clk}
+                "batched_gf": r, "roofline": r["batch_hv_roofline"], "clocks": clk}
         print(json.dumps(line), flush=True)
     RP.finish()
 
@@ -600,11 +708,17 @@ def main():
     timer = LZ.KernelTimer()
     clock = StreamClock().start()
     res = []
-    for _ in range(args.steps):
+    psi_last = None
+    for i in range(args.steps):
         g = solve(timer)
         res.append((g.e0, g.steps, g.refine_steps, g.e0_unrefined))
+        if i == args.steps - 1:
+            psi_last = g.psi
         del g
     elapsed = clock.stop()
+    # the last solve's psi0 (FP64) goes to the host for the oracle check below
+    psi_host = sec.to_ref(psi_last).cpu().numpy() if (rank == 0 and not args.small) else None
+    del psi_last
     barrier()
     clk = clocks.stop()
     elapsed = max_over_ranks(elapsed)
@@ -715,6 +829,13 @@ def main():
         del fh, psi
         torch.cuda.empty_cache()
 
+    # the metric's third part: batched Green's functions, sharded by cluster over the ranks
+    batched = None
+    if not args.no_c4 and not args.small:
+        torch.cuda.empty_cache()
+        batched = c4_batched(args, ws, rank, local)
+        torch.cuda.empty_cache()
+
     cpu = None
     if not args.no_cpu and rank == 0 and ws == 1 and not args.small:   # the CPU sample: rank 0 at N=1 only
         hv_cpu, spent, desc, nth = cpu_sample(CPU_PAIRS_OURS, 16, args.U)
@@ -723,18 +844,21 @@ def main():
                "sample": f"{desc} ({spent:.1f} s); extrapolated to the {n_hv:.0f} H*v of one solve",
                "hv_seconds": hv_cpu}
 
+    oracle_check = None
+    if psi_host is not None and not args.no_cpu:
+        oracle_check = e0_oracle_check(t, U, psi_host, e0_mixed)
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 vectors / f64 scalars + f64 refinement",
                 "data": "synthetic (seeded uniform[-0.5,0.5) start vector)",
-                "config": {"workload": ("4x4 periodic Hubbard t=1 U=%g N_up=N_down=8 (D=%d) ground state: "
-                                        "%d-step full-reorth Lanczos FP32 + FP64 refinement") %
-                                       (args.U, sec.dim, args.lanczos_steps),
-                           "parallelism": f"replicas x{ws}", "l2": "vectors 0.66 GB >> L2; no flush needed"},
+                "config": c2_config(args, sec.dim, ws),
                 "e0": e0_mixed, "e0_fp32_phase": res[-1][3], "refine_steps": res[-1][2],
-                "fp64_plain": fp64, "roofline": roofline, "hv_roofline_in_solve": hv_roof,
-                "hv_alone": hv_alone, "kernels": ksum, "e2e": e2e, "cpu_baseline": cpu, "clocks": clk,
+                "fp64_plain": fp64, "e0_oracle_check": oracle_check, "roofline": roofline,
+                "hv_roofline_in_solve": hv_roof,
+                "hv_alone": hv_alone, "batched_gf": batched, "kernels": ksum, "e2e": e2e, "cpu_baseline": cpu,
+                "clocks": clk,
                 "gpu_launches": timer.launches()}
         print(json.dumps(line), flush=True)
     RP.finish()

@@ -206,6 +206,12 @@ int ed_batch_destroy(ed_batch *b);
  * (nsdn_i*ld_i), and the CTA count of one step (scratch sizing). */
 int ed_batch_layout(const ed_batch *b, int64_t *total, int64_t *offsets, int64_t *sizes, int64_t *nblocks);
 int64_t ed_batch_scratch_bytes(const ed_batch *b);
+/* y_i = H_i x_i for every instance in one launch (the batched Lanczos
+ * step's H*v kernel alone), x and y concatenated in the batch layout with
+ * zero row padding (y's padding is written as zero).  HPROD
+ * (hprod_hubbard.f90:17-118) applied to each instance's sector; scratch as
+ * for ed_batch_lanczos. */
+int ed_batch_hv(ed_batch *b, void *stream, int dtype, const void *x, void *y, void *scratch, int64_t scratch_bytes);
 /* Run nsteps Lanczos steps of every instance from the start vectors x0
  * (concatenated, zero padding).  work: 3*total elements (two Krylov vectors
  * and H*v).  alpha: device FP64 [ninst][nsteps]; beta: device FP64

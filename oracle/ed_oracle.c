@@ -771,3 +771,151 @@ void orc_gf_start(int kind, int norb, int ncomp, int ndn0,
         }
     }
 }
+
+/* -------------------------------------- sampled rows of large sectors --- */
+
+/* The r-th k-subset of {0..n-1} in orc_rank's order (its inverse): at each
+ * step the next element j is the first whose C(n-1-j, left-1) subsets
+ * (those taking j here) contain r; the others are skipped by subtracting
+ * their counts. */
+uint32_t orc_unrank(int n, int k, int64_t r)
+{
+    uint32_t s = 0;
+    int prev = -1, left = k;
+    while (left > 0) {
+        for (int j = prev + 1; j < n; ++j) {
+            int64_t c = bnm(n - 1 - j, left - 1);
+            if (r < c) {
+                s |= (uint32_t)1u << j;
+                prev = j;
+                break;
+            }
+            r -= c;
+        }
+        left--;
+    }
+    return s;
+}
+
+/* Input vectors of the sampled-row checks, as a function of the element
+ * index alone, so that a 6e8-element vector never has to exist on the host:
+ * h = (i * 2654435761 + seed * 40503) mod 2^32;
+ *   kind 0: h / 2^32 - 0.5 (an exact double in [-0.5, 0.5));
+ *   kind 1: (h mod 7) - 3 (an integer in [-3, 3]).
+ * The device side forms the same numbers with int64 arithmetic. */
+double orc_hashval(int64_t i, int64_t seed, int kind)
+{
+    uint64_t h = ((uint64_t)i * 2654435761ull + (uint64_t)seed * 40503ull) & 0xffffffffull;
+    if (kind == 0) return (double)h / 4294967296.0 - 0.5;
+    return (double)(int)(h % 7ull) - 3.0;
+}
+
+/* HPROD of the Sz=0 Heisenberg sector (hprod_heis.f90:1-61) read from the
+ * output side for a list of rows, with x_i = orc_hashval(i, xseed, xkind).
+ * The reference scatters every source I into V1(POS); row p receives, in the
+ * reference's (J, K) loop order: the J_MATRIX(J,J) single-occupancy term of
+ * J (:11-20), then for each K the flip from the one source whose up string
+ * maps onto p's (KINOP(BUP(I),J,K) = BUP(p): BUP(I) is BUP(p) with the
+ * particle moved back from K to J, :23-49) and the SZ*SZ term (:53-57).
+ * The sums are therefore the full restatement's, bit for bit, and the rank
+ * is the closed form orc_rank (the reference's linear search finds the same
+ * position).  absout[r] = the sum of the terms' magnitudes. */
+void orc_hprod_heis_rows(int norb, const double *jm, int64_t nrows, const int64_t *rows,
+                         int64_t xseed, int xkind, double *out, double *absout, int nthreads)
+{
+    const uint32_t full = (norb >= 32) ? 0xFFFFFFFFu : (((uint32_t)1u << norb) - 1u);
+    const int ne = norb / 2;
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t r = 0; r < nrows; ++r) {
+        const int64_t p = rows[r];
+        const uint32_t sp = orc_unrank(norb, ne, p), dnp = full - sp;
+        const double xp = orc_hashval(p, xseed, xkind);
+        double acc = 0.0, aab = 0.0;
+        for (int J = 1; J <= norb; ++J) {
+            const double jjj = TF(jm, norb, J, J);
+            if (fabs(jjj) > TOL14) {
+                int pu = is_part(norb, J, sp), pd = is_part(norb, J, dnp);
+                if ((pu && !pd) || (!pu && pd)) {
+                    acc = acc + xp * 0.5 * jjj;
+                    aab += fabs(xp * 0.5 * jjj);
+                }
+            }
+            for (int K = 1; K <= norb; ++K) {
+                const double jjk = TF(jm, norb, J, K);
+                if (fabs(jjk) > TOL14 && J != K && is_part(norb, K, sp) && !is_part(norb, J, sp)) {
+                    const uint32_t s = sp - site_bit(norb, K) + site_bit(norb, J);
+                    const int64_t i = orc_rank(norb, ne, s);
+                    const uint32_t dn = full - s;
+                    double ac = orc_anticom(norb, J, s);
+                    ac = ac * orc_anticom(norb, K, sp);
+                    const uint32_t nw2 = orc_kinop(norb, dn, K, J);
+                    if (nw2 == full - sp) {
+                        ac = ac * orc_anticom(norb, J, dn);
+                        ac = ac * orc_anticom(norb, K, nw2);
+                        const double xi = orc_hashval(i, xseed, xkind);
+                        acc = acc - ac * xi * jjk;
+                        aab += fabs(xi * jjk);
+                    }
+                }
+                const double t = xp * sz_site(norb, J, sp, dnp) * sz_site(norb, K, sp, dnp) * jjk;
+                acc = acc + t;
+                aab += fabs(t);
+            }
+        }
+        out[r] = acc;
+        if (absout) absout[r] = aab;
+    }
+}
+
+/* J_SPIN of the Sz=0 Heisenberg sector (static_rq_heis.f90:58-116) for a bra
+ * supported on a list of rows R: bra_p = orc_hashval(p, bseed, kind) for p in
+ * R and 0 elsewhere, ket_i = orc_hashval(i, kseed, kind) for every i.  Each
+ * term of SMATRIX(J,K) carries bra at its row (BRA(I) in the diagonal sums,
+ * BRA(POS) in the flip sum), so only rows in R contribute; the flip into row
+ * p comes from the source whose up string KINOP maps onto p's, with J_SPIN's
+ * sign, ANTICOM(J,BUP(I)) ANTICOM(K,NEW) ANTICOM(K,BDOWNELEM) ANTICOM(J,NEW2)
+ * (:84-97).  pairs: npairs (J,K), 1-based; out[q] = SMATRIX(J,K) restricted
+ * to R, absout[q] = the sum of its terms' magnitudes. */
+void orc_j_spin_heis_rows(int norb, int64_t nrows, const int64_t *rows, int64_t bseed, int64_t kseed, int kind,
+                          int npairs, const int32_t *pairs, double *out, double *absout, int nthreads)
+{
+    const uint32_t full = (norb >= 32) ? 0xFFFFFFFFu : (((uint32_t)1u << norb) - 1u);
+    const int ne = norb / 2;
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int q = 0; q < npairs; ++q) {
+        const int J = pairs[2 * q], K = pairs[2 * q + 1];
+        double acc = 0.0, aab = 0.0;
+        for (int64_t r = 0; r < nrows; ++r) {
+            const int64_t p = rows[r];
+            const uint32_t sp = orc_unrank(norb, ne, p), dnp = full - sp;
+            const double bp = orc_hashval(p, bseed, kind), kp = orc_hashval(p, kseed, kind);
+            if (J == K) {
+                int pu = is_part(norb, J, sp), pd = is_part(norb, J, dnp);
+                if ((pu && !pd) || (!pu && pd)) {
+                    acc = acc + 0.5 * bp * kp;
+                    aab += fabs(0.5 * bp * kp);
+                }
+            } else if (is_part(norb, K, sp) && !is_part(norb, J, sp)) {
+                const uint32_t s = sp - site_bit(norb, K) + site_bit(norb, J);
+                const int64_t i = orc_rank(norb, ne, s);
+                const uint32_t dn = full - s;
+                double ac = orc_anticom(norb, J, s) * orc_anticom(norb, K, sp);
+                const uint32_t nw2 = orc_kinop(norb, dn, K, J);
+                if (nw2 == full - sp) {
+                    ac = ac * orc_anticom(norb, K, dn);
+                    ac = ac * orc_anticom(norb, J, nw2);
+                    const double ki = orc_hashval(i, kseed, kind);
+                    acc = acc - ac * bp * ki;
+                    aab += fabs(bp * ki);
+                }
+            }
+            const double t = bp * kp * sz_site(norb, J, sp, dnp) * sz_site(norb, K, sp, dnp);
+            acc = acc + t;
+            aab += fabs(t);
+        }
+        out[q] = acc;
+        if (absout) absout[q] = aab;
+    }
+}

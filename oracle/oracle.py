@@ -84,6 +84,12 @@ def lib():
             L.orc_j_spin.argtypes = [i32, P, i64, P, i64, P, P, P]
             L.orc_j_spin_heis.argtypes = [i32, P, i64, P, P, P]
             L.orc_gf_start.argtypes = [i32, i32, i32, i32, P, i64, P, i64, P, i64, P, i64, P, P]
+            L.orc_unrank.restype = ctypes.c_uint32
+            L.orc_unrank.argtypes = [i32, i32, i64]
+            L.orc_hashval.restype = ctypes.c_double
+            L.orc_hashval.argtypes = [i64, i64, i32]
+            L.orc_hprod_heis_rows.argtypes = [i32, P, i64, P, i64, i32, P, P, i32]
+            L.orc_j_spin_heis_rows.argtypes = [i32, i64, P, i64, i64, i32, i32, P, P, P, i32]
             _lib = L
     return _lib
 
@@ -174,6 +180,68 @@ def hprod_hubbard_udiag(sec: Sector, J: int, uj: float, x, y, nthreads: int = 1)
     else:
         lib().orc_hprod_hubbard_ref_udiag_mt(sec.norb, _p(sec.bup), sec.nsup, _p(sec.bdn), sec.nsdn, int(J),
                                              float(uj), _p(x), _p(y), int(nthreads))
+
+
+def hprod_hubbard_mt(sec: Sector, t, U, x, nthreads: int = 0) -> np.ndarray:
+    """The reference loop of hprod_hubbard_ref (hprod_hubbard.f90:17-118) on
+    host threads: for J = 1..norb its U term, then each (J, K) pair, in the
+    serial order; each piece is the threaded loop that equals the one-thread
+    loop bit for bit, so y equals hprod_hubbard(fast=False) bit for bit.
+    nthreads = 0: all the cores the process may use."""
+    t = _f64(t)
+    U = _f64(np.broadcast_to(np.asarray(U, dtype=np.float64), (sec.norb,)))
+    x = _f64(x)
+    y = np.zeros_like(x)
+    nt = int(nthreads) if nthreads else len(os.sched_getaffinity(0))
+    for J in range(1, sec.norb + 1):
+        hprod_hubbard_udiag(sec, J, float(U[J - 1]), x, y, nthreads=nt)
+        for K in range(1, sec.norb + 1):
+            hprod_hubbard_pairs(sec, t, [(J, K)], x, y, nthreads=nt)
+    return y
+
+
+# ------------------------------------------- sampled rows of large sectors ---
+
+def unrank(norb: int, ne: int, r: int) -> int:
+    """String at position r of hilbert(norb, ne) (inverse of rank)."""
+    return int(lib().orc_unrank(norb, ne, int(r)))
+
+
+def hashvec(idx, seed: int, kind: int) -> np.ndarray:
+    """orc_hashval for an array of element indices: the inputs of the
+    sampled-row checks as a function of the index alone (kind 0: exact doubles
+    in [-0.5, 0.5); kind 1: integers in [-3, 3])."""
+    i = np.asarray(idx, dtype=np.uint64)
+    h = (i * np.uint64(2654435761) + np.uint64(seed) * np.uint64(40503)) & np.uint64(0xFFFFFFFF)
+    if kind == 0:
+        return h.astype(np.float64) / 4294967296.0 - 0.5
+    return (h % np.uint64(7)).astype(np.float64) - 3.0
+
+
+def hprod_heis_rows(norb: int, J, rows, xseed: int, xkind: int, nthreads: int = 0):
+    """Rows of y = H x (hprod_heis.f90:1-61) for x = hashvec(., xseed, xkind),
+    summed in the reference's order (equal to hprod_heis(fast=False) at those
+    rows, bit for bit).  Returns (y[rows], sum of |terms| per row)."""
+    J = _f64(J)
+    rows = np.ascontiguousarray(rows, dtype=np.int64)
+    out = np.empty(len(rows))
+    ab = np.empty(len(rows))
+    lib().orc_hprod_heis_rows(norb, _p(J), len(rows), _p(rows), int(xseed), int(xkind), _p(out), _p(ab),
+                              int(nthreads))
+    return out, ab
+
+
+def j_spin_heis_rows(norb: int, rows, bseed: int, kseed: int, kind: int, pairs, nthreads: int = 0):
+    """SMATRIX(J,K) of J_SPIN (static_rq_heis.f90:58-116) for bra = hashvec(.,
+    bseed, kind) restricted to rows and ket = hashvec(., kseed, kind).
+    Returns (SMATRIX per pair, sum of |terms| per pair)."""
+    rows = np.ascontiguousarray(rows, dtype=np.int64)
+    pr = np.ascontiguousarray(np.asarray(pairs, dtype=np.int32).reshape(-1, 2))
+    out = np.empty(len(pr))
+    ab = np.empty(len(pr))
+    lib().orc_j_spin_heis_rows(norb, len(rows), _p(rows), int(bseed), int(kseed), int(kind), len(pr), _p(pr),
+                               _p(out), _p(ab), int(nthreads))
+    return out, ab
 
 
 def heis_sector(norb: int) -> Sector:
@@ -371,6 +439,52 @@ def lehmann_gf_diag(sec: Sector, t, U, psi0: np.ndarray, e0: float, ncomp: int):
             pos = (val - e0) if part == "greater" else (e0 - val)
             res[part] = (pos, Q)
         out[spin] = res
+    return out
+
+
+def spgf_ed(sec: Sector, t, U, psis, ncomp: int) -> dict:
+    """What SPGF_ED stores (spgf_ed.f90:66-290), for the states psis (each a
+    reference-layout vector of the (nup, ndn) sector): per spin and part the
+    eigenvalues of the N+1 (greater) / N-1 (lesser) sector as
+    'positions_{part}_{spin}' and the overlaps 'Q_{part}_{spin}'[i, n, b] =
+    <n|c^+_i|psi_b> (greater) or <n|c_i|psi_b> (lesser), sites i < ncomp."""
+    out = {}
+    for spin in ("up", "down"):
+        for part, kind in (("greater", "e_" + spin), ("lesser", "h_" + spin)):
+            starts = []
+            sec1 = None
+            for psi in psis:
+                sec1, st = gf_start(kind, sec, ncomp, psi)
+                starts.append(st)
+            if sec1 is None or sec1.dim == 0:
+                out[f"positions_{part}_{spin}"] = np.zeros(0)
+                out[f"Q_{part}_{spin}"] = np.zeros((ncomp, 0, len(psis)))
+                continue
+            H1 = dense_h(lambda v: hprod_hubbard(sec1, t, U, v), sec1.dim)
+            val, vec = np.linalg.eigh(H1)
+            out[f"positions_{part}_{spin}"] = val
+            out[f"Q_{part}_{spin}"] = np.stack([st @ vec for st in starts], axis=2)
+    return out
+
+
+def self_energy_ref(Vk, ek, e, wgt, spgf: dict, w: float, eta: float, same_spin: bool) -> dict:
+    """GreenFunction.self_energy at one frequency (reduced_quantities.py:
+    139-161): pinv(sum_k Vk_ik Vk_jk / (w - ek + i eta)) minus pinv(G), with G
+    summed over the states b from the stored Q and positions, greater poles at
+    -e_b + position, lesser at e_b - position; weighted by wgt_b/sum(wgt) when
+    N_up == N_down, unweighted (the reference's other branch) otherwise."""
+    g0i = np.linalg.pinv(np.einsum("ik,jk,k->ij", Vk, Vk, 1. / (w - ek + 1j * eta)))
+    out = {}
+    for spin in ("up", "down"):
+        src = "up" if same_spin else spin
+        G = 0
+        for b, bltz in enumerate(wgt):
+            f = bltz / np.sum(wgt) if same_spin else 1.0
+            Qg, pg = spgf[f"Q_greater_{src}"][:, :, b], spgf[f"positions_greater_{src}"]
+            Ql, pl = spgf[f"Q_lesser_{src}"][:, :, b], spgf[f"positions_lesser_{src}"]
+            G = G + np.einsum("ik,jk,k->ij", Qg, Qg, 1. / (w - (-e[b] + pg) + 1j * eta)) * f \
+                + np.einsum("ik,jk,k->ij", Ql, Ql, 1. / (w - (e[b] - pl) + 1j * eta)) * f
+        out[spin] = g0i - np.linalg.pinv(G)
     return out
 
 

@@ -43,6 +43,7 @@ _SIGS = {
     "ed_batch_layout": (_I, [_P, ctypes.POINTER(_I64), _P, _P, ctypes.POINTER(_I64)]),
     "ed_batch_scratch_bytes": (_I64, [_P]),
     "ed_batch_lanczos": (_I, [_P, _P, _I, _P, _P, _I, _P, _P, _P, _I64]),
+    "ed_batch_hv": (_I, [_P, _P, _I, _P, _P, _P, _I64]),
     "ed_batch_ritz": (_I, [_P, _P, _I, _P, _P, _I, _P, _P, _P, _P, _P, _I64]),
     "ed_batch_create_rows": (_I, [_I, _P, _I, ctypes.POINTER(_P)]),
     "ed_batch_rows": (_I, [_P]),
@@ -308,6 +309,14 @@ class Batch:
 
     def scratch_bytes(self):
         return int(lib().ed_batch_scratch_bytes(self._h))
+
+    def hv(self, x, y, scratch, stream=None):
+        """y_i = H_i x_i for every instance (concatenated batch layout)."""
+        if y.dtype != x.dtype:
+            raise TypeError("x and y must have the same dtype")
+        check("ed_batch_hv", lib().ed_batch_hv(self._h, _stream(stream), dtype_code(x.dtype),
+                                               _ptr(x, self.total, "x"), _ptr(y, self.total, "y"), _ptr(scratch),
+                                               int(scratch.numel() * scratch.element_size())))
 
     def lanczos(self, work, x0, nsteps: int, alpha, beta, scratch, stream=None):
         sb = scratch.numel() * scratch.element_size()

@@ -415,6 +415,32 @@ def sweep(clusters, nsteps: int = 150, chunk: int = 64, dtype=None, gs_steps: in
     return results
 
 
+def sharded_sweep(clusters, rank: int = 0, ws: int = 1, sweep_fn=None, **kw):
+    """A sweep over clusters sharded across ranks: rank r sweeps clusters r,
+    r+ws, ... (no collective on the data path), then rank 0 gathers every
+    rank's results (reduced_quantities.py:84-92 builds G from the poles of
+    each cluster; here each cluster's G_ii(w) and E0 come back as host arrays).
+    Returns {cluster index: {'e0': float, 'G': complex128 ndarray [2, norb,
+    nw]}} for all clusters on rank 0, None on the other ranks.  sweep_fn
+    (default: sweep) maps a list of cluster specs to {local index: result}."""
+    from .. import replicas as RP
+    sweep_fn = sweep if sweep_fn is None else sweep_fn
+    mine = RP.shard(range(len(clusters)), rank, ws)
+    res = sweep_fn([clusters[i] for i in mine], **kw)
+    local = {}
+    for k, v in res.items():
+        g = v["G"]
+        local[mine[k]] = {"e0": float(v["e0"]),
+                          "G": g.cpu().numpy() if hasattr(g, "cpu") else np.asarray(g)}
+    parts = RP.gather_to_root(local)
+    if parts is None:
+        return None
+    merged = {}
+    for p in parts:
+        merged.update(p)
+    return merged
+
+
 def _site_groups(inst, offsets):
     """Runs [i, j) of consecutive instances with the same (cluster, spin,
     part), and the constant distance of their slots in the batch (0 for a

@@ -191,26 +191,48 @@ class GreenFunction:
                 "down": np.array([[Pole({"positions": self.ek, "weights": self.Vk[i, :] * self.Vk[j, :]})
                                    for i in range(self.nb_sites)] for j in range(self.nb_sites)])}
 
-    def gf_matrix(self, w, eta=0.05, device=None):
+    def gf_matrix(self, w, eta=0.05, device=None, raw=False):
         """G_s(w)[k, i, j] = sum_p weight_p / (w_k - position_p + i eta) for all
         frequencies at once: every (i, j) pole set is padded into one [n, n, P]
         array and the sum runs as one tensor contraction (on the GPU when there
-        is one).  Returns {spin: complex128 torch tensor [nw, n, n]}."""
+        is one).  raw=False reads the poles of self.gf (after Pole.clean, as
+        compute_gf leaves them); raw=True sums the uncleaned poles of every
+        computed state, as the reference's self_energy forms G from the stored
+        Q and positions (reduced_quantities.py:134-161): weighted by
+        wgt/sum(wgt) when N_up == N_down, unweighted otherwise.
+        Returns {spin: complex128 torch tensor [nw, n, n]}."""
         import torch
         dev = device or ("cuda" if torch.cuda.is_available() else "cpu")
         wv = torch.as_tensor(np.atleast_1d(np.asarray(w, dtype=np.float64)), device=dev)
         n = self.nb_sites_comp
         out = {}
         for s in ("up", "down"):
-            P = max(1, max(len(self.gf[s][i, j].pole["positions"]) for i in range(n) for j in range(n)))
+            sets = [[None] * n for _ in range(n)]
+            for i in range(n):
+                for j in range(n):
+                    if not raw:
+                        pl = self.gf[s][i, j].pole
+                        sets[i][j] = (np.asarray(pl["positions"]), np.asarray(pl["weights"]))
+                        continue
+                    same = self.nup[0] == self.ndown[0]
+                    wn = self._wnorm() if same else np.ones(len(self.wgt))
+                    ps, ws = [], []
+                    for b, wb in enumerate(wn):
+                        if self._spgf[b] is None:
+                            continue
+                        for part in ("greater", "lesser"):
+                            pos, wts = self._spgf[b][s][part].pole(i, j)
+                            ps.append(pos)
+                            ws.append(wts * wb)
+                    sets[i][j] = (np.concatenate(ps) if ps else np.zeros(0), np.concatenate(ws) if ws else np.zeros(0))
+            P = max(1, max(len(sets[i][j][0]) for i in range(n) for j in range(n)))
             pos = np.zeros((n, n, P))
             wts = np.zeros((n, n, P))
             for i in range(n):
                 for j in range(n):
-                    pl = self.gf[s][i, j].pole
-                    k = len(pl["positions"])
-                    pos[i, j, :k] = pl["positions"]
-                    wts[i, j, :k] = pl["weights"]
+                    k = len(sets[i][j][0])
+                    pos[i, j, :k] = sets[i][j][0]
+                    wts[i, j, :k] = sets[i][j][1]
             pos_t = torch.as_tensor(pos, device=dev)
             wts_t = torch.as_tensor(wts, device=dev).to(torch.complex128)
             den = wv[:, None, None, None] - pos_t[None] + 1j * eta
@@ -218,30 +240,26 @@ class GreenFunction:
         return out
 
     def self_energy(self, w, eta=0.05):
-        """Sigma(w) = G0^-1 - G^-1 with the reference's pseudo-inverses
-        (reduced_quantities.py:134-161), G evaluated from its poles.  For an
-        array of frequencies all of them are done at once (gf_matrix and
-        batched pseudo-inverses); the result keeps the reference's layout
-        [j][i][k] = Sigma(w_k)[i, j]."""
-        if isinstance(w, (list, np.ndarray)):
-            import torch
-            wv = np.asarray(w, dtype=np.float64)
-            G = self.gf_matrix(wv, eta=eta)
-            dev = G["up"].device
-            n = self.nb_sites_comp
-            Vk = torch.as_tensor(self.Vk, device=dev).to(torch.complex128)
-            ek = torch.as_tensor(self.ek, device=dev)
-            wt = torch.as_tensor(wv, device=dev)
-            d0 = 1.0 / (wt[:, None] - ek[None, :] + 1j * eta)                 # [nw, nk]
-            g0 = torch.einsum("ik,jk,wk->wij", Vk, Vk, d0)
-            g0i = torch.linalg.pinv(g0, rtol=1e-15)[:, :n, :n]
-            return {s: (g0i - torch.linalg.pinv(G[s], rtol=1e-15)).permute(2, 1, 0).cpu().numpy()
-                    for s in ("up", "down")}
-        g0 = np.linalg.pinv(np.einsum("ik,jk,k->ij", self.Vk, self.Vk, 1. / (w - self.ek + 1j * eta)))
-        out = {}
-        for s in ("up", "down"):
-            G = np.array([[self.gf[s][i, j].retarded(w, eta=eta) for j in range(self.nb_sites_comp)]
-                          for i in range(self.nb_sites_comp)])
-            n = self.nb_sites_comp
-            out[s] = g0[:n, :n] - np.linalg.pinv(G)
-        return out
+        """Sigma(w) = pinv(G0(w)) - pinv(G(w)) (reduced_quantities.py:134-161):
+        G0 from the hopping matrix's eigenpairs (ek, Vk), G from the uncleaned
+        poles of every computed state (gf_matrix(raw=True)), as the reference
+        forms it from the stored Q and positions.  For an array of frequencies
+        all of them are done at once (batched pseudo-inverses) and the result
+        keeps the reference's layout [j][i][k] = Sigma(w_k)[i, j]; for one
+        frequency it returns {spin: [n, n]}."""
+        import torch
+        scalar = not isinstance(w, (list, np.ndarray))
+        wv = np.atleast_1d(np.asarray(w, dtype=np.float64))
+        G = self.gf_matrix(wv, eta=eta, raw=True)
+        dev = G["up"].device
+        n = self.nb_sites_comp
+        Vk = torch.as_tensor(self.Vk, device=dev).to(torch.complex128)
+        ek = torch.as_tensor(self.ek, device=dev)
+        wt = torch.as_tensor(wv, device=dev)
+        d0 = 1.0 / (wt[:, None] - ek[None, :] + 1j * eta)                 # [nw, nk]
+        g0 = torch.einsum("ik,jk,wk->wij", Vk, Vk, d0)
+        g0i = torch.linalg.pinv(g0, rtol=1e-15)[:, :n, :n]
+        sig = {s: g0i - torch.linalg.pinv(G[s], rtol=1e-15) for s in ("up", "down")}
+        if scalar:
+            return {s: v[0].cpu().numpy() for s, v in sig.items()}
+        return {s: v.permute(2, 1, 0).cpu().numpy() for s, v in sig.items()}

@@ -767,6 +767,50 @@ extern "C" int ed_batch_ritz_sum(ed_batch *bt, void *stream, int dtype, const vo
     return ED_OK;
 }
 
+namespace ed {
+// s_k = 1 for every instance: the H*v kernel's scale when it runs alone.
+__global__ void batch_unit_scale_kernel(int ninst, double *__restrict__ scal)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ninst) scal[(int64_t)i * kScal + kS] = 1.0;
+}
+}  // namespace ed
+
+extern "C" int ed_batch_hv(ed_batch *bt, void *stream, int dtype, const void *x, void *y, void *scratch,
+                           int64_t scratch_bytes)
+{
+    clear_error();
+    ED_REQUIRE(bt != nullptr && x != nullptr && y != nullptr, "NULL argument");
+    ED_REQUIRE(x != y, "x and y must not alias");
+    ED_REQUIRE(dtype == ED_F32 || dtype == ED_F64, "dtype must be ED_F32 or ED_F64");
+    ED_REQUIRE(scratch != nullptr && scratch_bytes >= ed_batch_scratch_bytes(bt), "scratch of %lld bytes is below %lld",
+               (long long)scratch_bytes, (long long)ed_batch_scratch_bytes(bt));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int rc = ensure_hv_smem(dtype, bt->rows, hv_smem_bytes(dtype, bt->max_ld, bt->rows));
+    if (rc != ED_OK) return rc;
+    const unsigned nb = (unsigned)bt->nblocks;
+    if (nb == 0) return ED_OK;
+    double *pa = static_cast<double *>(scratch), *scal = pa + 2 * bt->nblocks;
+    batch_unit_scale_kernel<<<(bt->ninst + 255) / 256, 256, 0, st>>>(bt->ninst, scal);
+    ED_CHECK_LAUNCH();
+    const size_t smem = hv_smem_bytes(dtype, bt->max_ld, bt->rows);
+    if (dtype == ED_F32) {
+        const float *xx = static_cast<const float *>(x);
+        float *yy = static_cast<float *>(y);
+        if (bt->rows == 4) batch_hv_kernel<float, 4><<<nb, kBatchThreads, smem, st>>>(bt->dev, bt->blk_inst, xx, yy, scal, pa);
+        else if (bt->rows == 16) batch_hv_kernel<float, 16><<<nb, kBatchThreads, smem, st>>>(bt->dev, bt->blk_inst, xx, yy, scal, pa);
+        else batch_hv_kernel<float, 8><<<nb, kBatchThreads, smem, st>>>(bt->dev, bt->blk_inst, xx, yy, scal, pa);
+    } else {
+        const double *xx = static_cast<const double *>(x);
+        double *yy = static_cast<double *>(y);
+        if (bt->rows == 4) batch_hv_kernel<double, 4><<<nb, kBatchThreads, smem, st>>>(bt->dev, bt->blk_inst, xx, yy, scal, pa);
+        else if (bt->rows == 16) batch_hv_kernel<double, 16><<<nb, kBatchThreads, smem, st>>>(bt->dev, bt->blk_inst, xx, yy, scal, pa);
+        else batch_hv_kernel<double, 8><<<nb, kBatchThreads, smem, st>>>(bt->dev, bt->blk_inst, xx, yy, scal, pa);
+    }
+    ED_CHECK_LAUNCH();
+    return ED_OK;
+}
+
 extern "C" int ed_batch_lanczos(ed_batch *bt, void *stream, int dtype, void *work, const void *x0, int nsteps,
                                 double *alpha, double *beta, void *scratch, int64_t scratch_bytes)
 {

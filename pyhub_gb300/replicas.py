@@ -4,9 +4,10 @@ A single Hubbard or Heisenberg sector does not shard without an all-to-all
 transpose of the vector per H*v (the down hops mix rows, the up hops mix
 columns), so single-sector workloads run as independent replicas.  Batched
 Green's-function sweeps shard by cluster: clusters are independent, each
-rank sweeps its own share.  The only collectives are host bookkeeping:
-barriers around a timed region, the maximum time over ranks and the sum of
-the units processed.
+rank sweeps its own share.  The collectives are host bookkeeping -- barriers
+around a timed region, the maximum time over ranks, the sum of the units
+processed -- and, after a sweep, one gather of every rank's results to rank
+0, outside the data path.
 
 The launch follows torchrun's environment (WORLD_SIZE, RANK, LOCAL_RANK,
 MASTER_ADDR, MASTER_PORT); the rendezvous address defaults to 127.0.0.1.
@@ -90,3 +91,15 @@ def aggregate_rate(units: float, seconds: float) -> tuple[float, float, float]:
     total = sum_over_ranks(units)
     tmax = max_over_ranks(seconds)
     return (total / tmax if tmax > 0 else float("inf")), total, tmax
+
+
+def gather_to_root(obj):
+    """Every rank's obj, in rank order, as a list on rank 0 (None on the other
+    ranks); [obj] without a process group."""
+    import torch.distributed as D
+    if not (D.is_available() and D.is_initialized()) or D.get_world_size() == 1:
+        return [obj]
+    rank = D.get_rank()
+    out = [None] * D.get_world_size() if rank == 0 else None
+    D.gather_object(obj, out, dst=0)
+    return out

@@ -1,7 +1,7 @@
 """Generate golden vectors from the reference's own Python modules.
 
-Run in a container where the reference is checked out (default
-/root/reference, or the path given as the first argument).  Only
+Run where the reference is checked out: its path is the first argument, or
+the environment variable PYHUB_REFERENCE.  Only
 pyhub/tools/pole.py and pyhub/solver/bethe_anzatz.py are imported, by file
 path: the package __init__ needs h5py and the Fortran executables, which are
 not available.  Output: pole_golden.npz beside this script.
@@ -12,7 +12,7 @@ import sys
 
 import numpy as np
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PYHUB_REFERENCE", "")
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -24,6 +24,8 @@ def load(rel, name):
 
 
 def main():
+    if not REF or not os.path.isfile(os.path.join(REF, "pyhub", "tools", "pole.py")):
+        sys.exit("usage: make_golden.py <reference checkout> (or set PYHUB_REFERENCE)")
     pole = load("pyhub/tools/pole.py", "ref_pole")
     ba = load("pyhub/solver/bethe_anzatz.py", "ref_bethe")
     rng = np.random.default_rng(2024)

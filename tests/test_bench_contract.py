@@ -21,3 +21,19 @@ def test_reference_arm_json_line():
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert "workload" in d["config"]
+
+
+def test_reference_arm_config_matches_engine_arm():
+    """Both arms describe the same workload: the config dicts are equal, and the
+    reference arm extrapolates to the engine's H*v count (FP32 steps + FP64
+    refinement)."""
+    sys.path.insert(0, ROOT)
+    import argparse
+    import bench
+    args = argparse.Namespace(U=8.0, lanczos_steps=200)
+    cfg = bench.c2_config(args, 12870 * 12870, 1)
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                          "--warmup", "0"], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    d = json.loads([ln for ln in out.stdout.splitlines() if ln.startswith("{")][0])
+    assert d["config"] == cfg
+    assert f"the {200 + bench.C2_REFINE_STEPS} H*v of one solve" in d["cpu_baseline"]["sample"]

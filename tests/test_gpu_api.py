@@ -287,3 +287,38 @@ def test_self_energy_array_matches_per_frequency(edlib):
         for s in ("up", "down"):
             got = S[s][:, :, k].T
             assert np.abs(got - one[s]).max() <= 1e-10 * max(1.0, np.abs(one[s]).max()), (s, k)
+
+
+@pytest.mark.parametrize("nu,nd", [(3, 3), (3, 2)])
+def test_self_energy_matches_reference_formula(edlib, nu, nd):
+    """Sigma(w) and G(w) against the oracle's restatement of the reference's
+    self_energy (reduced_quantities.py:134-161) on exact SPGF_ED poles (full ED
+    of the N+-1 sectors): G to 1e-9, Sigma to 1e-7 of its largest entry (the
+    pseudo-inverses amplify the pole error)."""
+    from pyhub_gb300.solver import FermiHubbard
+    norb = 6
+    t = O.ring(norb)
+    t[0, 3] = t[3, 0] = -0.3
+    U = 3.0
+    fh = FermiHubbard(norb, nu, nd, t, U)
+    fh.kernel(max_lcz=300, acc_lcz=1e-13, compute_rq=False)
+    fh.spgf(nsteps=400)
+    osec = O.Sector(norb, nu, nd)
+    H = O.dense_h(lambda v: O.hprod_hubbard(osec, t, U, v, fast=True), osec.dim)
+    e, v = np.linalg.eigh(H)
+    sp = O.spgf_ed(osec, t, U, [v[:, 0]], norb)
+    ek, Vk = np.linalg.eigh(t)
+    w = np.array([-3.1, -0.7, 0.2, 1.9, 4.4])
+    eta = 0.1
+    G = fh.gf_matrix(w, eta=eta, raw=True)
+    S = fh.self_energy(w, eta=eta)
+    for k, wk in enumerate(w):
+        ref = O.self_energy_ref(Vk, ek, e[:1], [1.0], sp, wk, eta, nu == nd)
+        for s in ("up", "down"):
+            src = "up" if nu == nd else s
+            Gr = sum(np.einsum("ik,jk,k->ij", sp[f"Q_{p}_{src}"][:, :, 0], sp[f"Q_{p}_{src}"][:, :, 0],
+                               1.0 / (wk - (sg * (sp[f"positions_{p}_{src}"] - e[0])) + 1j * eta))
+                     for p, sg in (("greater", 1.0), ("lesser", -1.0)))
+            assert np.abs(G[s][k].cpu().numpy() - Gr).max() <= 1e-9 * np.abs(Gr).max(), (s, k)
+            got = S[s][:, :, k].T
+            assert np.abs(got - ref[s]).max() <= 1e-7 * np.abs(ref[s]).max(), (s, k, np.abs(got - ref[s]).max())

@@ -237,3 +237,92 @@ def test_operator_algebra_recognises_hubbard_form():
     assert op._hubbard() is None          # spin-dependent one-body terms: averages only
     assert str(c_dagger_c((0, "u"), (1, "u"))) == "1.0*c^\\dagger_{0,u}c_{1,u}"
 
+
+
+@pytest.mark.parametrize("no,ne", [(10, 5), (12, 6), (16, 8), (32, 16)])
+def test_unrank_inverts_rank(no, ne):
+    rng = np.random.default_rng(no)
+    n = O.binom(no, ne)
+    for r in rng.integers(0, n, 300):
+        s = O.unrank(no, ne, int(r))
+        assert bin(s).count("1") == ne and O.rank(no, ne, s) == int(r)
+    if no <= 16:
+        b = O.hilbert(no, ne)
+        assert all(O.unrank(no, ne, i) == int(b[i]) for i in range(0, n, max(1, n // 500)))
+
+
+def test_hashvec_matches_c():
+    L = O.lib()
+    idx = [0, 1, 7, 12345, 601080389, 2 ** 31 + 5]
+    for kind in (0, 1):
+        v = O.hashvec(idx, 3, kind)
+        assert all(L.orc_hashval(i, 3, kind) == v[q] for q, i in enumerate(idx))
+    assert set(np.unique(O.hashvec(np.arange(1000), 1, 1))) <= set(range(-3, 4))
+
+
+@pytest.mark.parametrize("norb,lattice", [(10, (5, 2)), (12, (4, 3))])
+def test_heis_rows_equal_full_restatement(norb, lattice):
+    """The output-side row form of the Heisenberg HPROD equals the scatter
+    restatement bit for bit on every row (real and integer inputs, with
+    diagonal J terms present)."""
+    J = np.abs(O.square_pbc(*lattice, 1.0))
+    J[0, 0], J[3, 3] = 0.7, -0.2
+    J[1, 5] = 0.3   # an asymmetric extra term
+    n = O.binom(norb, norb // 2)
+    for kind in (0, 1):
+        x = O.hashvec(np.arange(n), 5, kind)
+        y = O.hprod_heis(norb, J, x)
+        yr, ab = O.hprod_heis_rows(norb, J, np.arange(n), 5, kind)
+        assert np.array_equal(yr, y)
+        assert np.all(ab >= np.abs(y) - 1e-12)
+
+
+def test_j_spin_heis_rows_equal_masked_restatement():
+    """J_SPIN with the bra restricted to sampled rows equals the full
+    restatement with a bra that is zero off those rows."""
+    norb = 12
+    n = O.binom(norb, norb // 2)
+    rows = np.sort(np.random.default_rng(3).choice(n, 150, replace=False))
+    for kind in (0, 1):
+        bra = np.zeros(n)
+        bra[rows] = O.hashvec(rows, 11, kind)
+        ket = O.hashvec(np.arange(n), 12, kind)
+        full = O.j_spin_heis(norb, bra, ket)           # Python view: SMATRIX transposed
+        pairs = [(J, K) for J in range(1, norb + 1) for K in range(1, norb + 1)]
+        got, ab = O.j_spin_heis_rows(norb, rows, 11, 12, kind, pairs)
+        ref = np.array([full[K - 1, J - 1] for (J, K) in pairs])
+        assert np.allclose(got, ref, rtol=0, atol=1e-13 * max(1.0, ab.max()))
+        if kind == 1:
+            assert np.array_equal(got, ref)
+
+
+def test_threaded_full_hubbard_loop_is_bit_identical():
+    sec = O.Sector(8, 4, 3)
+    rng = np.random.default_rng(4)
+    t = rng.standard_normal((8, 8))
+    U = rng.uniform(0, 5, 8)
+    x = rng.standard_normal(sec.dim)
+    assert np.array_equal(O.hprod_hubbard_mt(sec, t, U, x, nthreads=3), O.hprod_hubbard(sec, t, U, x))
+    sec = O.Sector(8, 4, 4)
+    x = rng.standard_normal(sec.dim)
+    assert np.array_equal(O.hprod_hubbard_mt(sec, t, U, x, nthreads=2), O.hprod_hubbard(sec, t, U, x))
+
+
+def test_self_energy_restatement_vanishes_without_interaction():
+    """U = 0: the SPGF_ED poles give G = G0 exactly, so the restated
+    self_energy is zero; with U > 0 it is not."""
+    norb = 5
+    t = O.ring(norb)
+    t[0, 2] = t[2, 0] = -0.4
+    ek, Vk = np.linalg.eigh(t)
+    for U, zero in ((0.0, True), (2.5, False)):
+        sec = O.Sector(norb, 2, 2)
+        H = O.dense_h(lambda v: O.hprod_hubbard(sec, t, U, v), sec.dim)
+        e, v = np.linalg.eigh(H)
+        sp = O.spgf_ed(sec, t, U, [v[:, 0]], norb)
+        diag = O.lehmann_gf_diag(sec, t, U, v[:, 0], e[0], norb)
+        pos, Q = diag["up"]["greater"]
+        assert np.allclose(sp["Q_greater_up"][:, :, 0], Q) and np.allclose(sp["positions_greater_up"] - e[0], pos)
+        S = O.self_energy_ref(Vk, ek, e[:1], [1.0], sp, 0.37, 0.1, True)
+        mag = np.abs(S["up"]).max()
+        assert (mag < 1e-9) if zero else (mag > 1e-3), (U, mag)

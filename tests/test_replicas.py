@@ -65,3 +65,53 @@ def test_single_rank_is_local():
     assert RP.world()[0] == 1
     assert RP.shard([1, 2, 3], 0, 1) == [1, 2, 3]
     assert RP.aggregate_rate(6.0, 2.0) == (3.0, 6.0, 2.0)
+
+
+def _cpu_sweep(specs, nw=64):
+    """Host stand-in for the batched sweep (same result structure): the
+    non-interacting G_ii(w) of each cluster's hopping matrix, shifted by U/2."""
+    import numpy as np
+    w = np.linspace(-10.0, 10.0, nw)
+    out = {}
+    for k, spec in enumerate(specs):
+        ek, V = np.linalg.eigh(spec["t"])
+        g = ((V ** 2)[None, :, :] / (w[:, None, None] - ek[None, None, :] - 0.5 * spec["U"] + 0.05j)).sum(axis=2)
+        out[k] = {"e0": float(ek[: spec["N"]].sum()), "G": np.stack([g.T, g.T])}
+    return out
+
+
+def _gather_main(rank, ws, port, out_dir):
+    os.environ.update({"WORLD_SIZE": str(ws), "RANK": str(rank), "LOCAL_RANK": str(rank),
+                       "MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port)})
+    import pickle
+    from pyhub_gb300 import replicas as RP
+    from pyhub_gb300.core import greens_batched as GB
+    RP.init("gloo")
+    clusters = GB.c4_clusters(9, seed=1)
+    merged = GB.sharded_sweep(clusters, rank, ws, sweep_fn=_cpu_sweep)
+    RP.barrier(sync_cuda=False)
+    RP.finish()
+    with open(os.path.join(out_dir, f"gather{rank}.pkl"), "wb") as f:
+        pickle.dump(merged, f)
+
+
+def test_sharded_sweep_gathers_every_cluster_on_rank0(tmp_path):
+    """Two gloo ranks sweep disjoint halves of 9 clusters; rank 0 ends with
+    every cluster's G(w), equal to a single-rank sweep of the same clusters."""
+    import pickle
+    import numpy as np
+    import torch.multiprocessing as mp
+    from pyhub_gb300.core import greens_batched as GB
+    ws = 2
+    port = _free_port()
+    ctx = mp.start_processes(_gather_main, args=(ws, port, str(tmp_path)), nprocs=ws, join=False,
+                             start_method="spawn")
+    while not ctx.join(timeout=120):
+        pass
+    got = pickle.load(open(tmp_path / "gather0.pkl", "rb"))
+    assert pickle.load(open(tmp_path / "gather1.pkl", "rb")) is None
+    ref = _cpu_sweep(GB.c4_clusters(9, seed=1))
+    assert sorted(got) == list(range(9))
+    for c in range(9):
+        assert got[c]["e0"] == ref[c]["e0"]
+        assert np.array_equal(got[c]["G"], ref[c]["G"])
