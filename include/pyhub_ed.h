@@ -169,6 +169,28 @@ int64_t ed_rdm_scratch_bytes(int npairs);
 int ed_rdm(ed_sector *s, void *stream, int dtype, int64_t ld, const void *bra, const void *ket,
            int npairs, const int32_t *pairs, int flags, double *out, void *scratch, int64_t scratch_bytes);
 
+/* The general two-body interaction of a Hubbard sector, the reference's
+ * IS_ULOC=3 path (hprod_hubbard.f90:37,62-86): ul (host, norb^4 FP64) is the
+ * tensor U exactly as the reference's FermiHubbard takes it (C order
+ * U[a][b][c][d]), read as the reference reads it, UL(J,K,M,N) =
+ * U[N-1][M-1][K-1][J-1], each (J,K) kept only when UPARTIAL(J,K) =
+ * sum_cd U[K-1][J-1][c][d]^2 >= 1e-14 (core_solver.py:143-147,
+ * compute_solver.f90:129-138).  After this call ed_hv adds
+ * sum UL(J,K,M,N) c+_{K up} c_{J up} c+_{N down} c_{M down} (terms with
+ * |UL| >= 1e-14) and the sector's on-site U is dropped (no ULDIAG term on
+ * that path).  The work per element is the number of terms: meant for the
+ * small clusters this interaction is used on. */
+int ed_sector_set_uijkl(ed_sector *s, const double *ul);
+/* Device scratch bytes of ed_dbl_occ for nquads site quadruples. */
+int64_t ed_dbl_occ_scratch_bytes(const ed_sector *s, int nquads);
+/* The two-body density of TWO_RDM with DO_RQ_TB (static_rq.f90:256-306):
+ * out[q] (device FP64) = DBL_OCC(J,K,M,N) = <ket| c+_{K up} c_{J up}
+ * c+_{N down} c_{M down} |bra> for quads (host int32 [4*nquads], 1-based
+ * (J,K,M,N)), summed in FP64.  Synchronises the stream once (the quad list
+ * is copied from pageable host memory). */
+int ed_dbl_occ(ed_sector *s, void *stream, int dtype, int64_t ld, const void *bra, const void *ket,
+               int nquads, const int32_t *quads, double *out, void *scratch, int64_t scratch_bytes);
+
 /* Green's-function start vector out = c_{site,s}|psi> (kind 0: up, 1: down)
  * or c^+_{site,s}|psi> (kind 2: up, 3: down), site 1-based, psi in sector src
  * (row stride ld0), out in sector dst (row stride ld1, written entirely).

@@ -919,3 +919,133 @@ void orc_j_spin_heis_rows(int norb, int64_t nrows, const int64_t *rows, int64_t 
         if (absout) absout[q] = aab;
     }
 }
+
+/* ------------------------------------------ U_ijkl interaction (IS_ULOC=3) --- */
+
+/* The reference reads the Python tensor U (C order, U[a][b][c][d]) from HDF5
+ * into the Fortran array UL(NORB,NORB,NORB,NORB), so UL(J,K,M,N) =
+ * U[N-1][M-1][K-1][J-1]; 'Upartial' = einsum('ijkl,ijkl->ij', U, U) becomes
+ * UPARTIAL(J,K) = sum_cd U[K-1][J-1][c][d]^2 (core_solver.py:145-147,
+ * compute_solver.f90:129-138). */
+#define ULF(ul, n, J, K, M, N) \
+    ((ul)[((((int64_t)(N) - 1) * (n) + ((M) - 1)) * (n) + ((K) - 1)) * (n) + ((J) - 1)])
+
+static double upartial(const double *ul, int n, int J, int K)
+{
+    double s = 0.0;
+    const double *p = ul + (((int64_t)(K - 1) * n + (J - 1)) * n) * n;
+    for (int64_t q = 0; q < (int64_t)n * n; ++q) s += p[q] * p[q];
+    return s;
+}
+
+/* HPROD with IS_ULOC=3 (hprod_hubbard.f90:17-118): the hopping terms of
+ * every (J,K) with |T(J,K)| >= 1e-14 or UPARTIAL(J,K) >= 1e-14 (:37), and,
+ * for UPARTIAL(J,K) >= 1e-14, the up hop J->K times every down hop M->N with
+ * |UL(J,K,M,N)| >= 1e-14 (:62-86); no ULDIAG term.  Same loop nest and
+ * linear-search rank as orc_hprod_hubbard_ref. */
+void orc_hprod_hubbard_uijkl_ref(int norb, int nup, int ndn,
+                                 const uint32_t *bup, int64_t nsup,
+                                 const uint32_t *bdn, int64_t nsdn,
+                                 const double *t, const double *ul,
+                                 const double *x, double *y)
+{
+    int64_t nst = nsup * nsdn;
+    for (int64_t i = 0; i < nst; ++i) y[i] = 0.0;
+    for (int J = 1; J <= norb; ++J) {
+        for (int K = 1; K <= norb; ++K) {
+            double tjk = TF(t, norb, J, K);
+            double upjk = upartial(ul, norb, J, K);
+            if (!((fabs(tjk) >= TOL14) || (upjk >= TOL14))) continue;
+            for (int64_t u = 0; u < nsup; ++u) {
+                uint32_t nw = orc_kinop(norb, bup[u], J, K);
+                if (nw == 0) continue;
+                int64_t pos = lin_rank(nw, bup, nsup);
+                if (pos <= 0) continue;
+                double ac = orc_anticom(norb, J, bup[u]);
+                ac = ac * orc_anticom(norb, K, nw);
+                int64_t p = pos - 1;
+                if (nup == ndn) {
+                    for (int64_t d = 0; d < nsdn; ++d) {
+                        y[d * nsup + p] = y[d * nsup + p] + ac * x[d * nsup + u] * tjk;
+                        y[p * nsup + d] = y[p * nsup + d] + ac * x[u * nsup + d] * tjk;
+                    }
+                } else {
+                    for (int64_t d = 0; d < nsdn; ++d)
+                        y[d * nsup + p] = y[d * nsup + p] + ac * x[d * nsup + u] * tjk;
+                }
+                if (upjk >= TOL14) {
+                    for (int M = 1; M <= norb; ++M)
+                        for (int N = 1; N <= norb; ++N) {
+                            double uv = ULF(ul, norb, J, K, M, N);
+                            if (!(fabs(uv) >= TOL14)) continue;
+                            for (int64_t d = 0; d < nsdn; ++d) {
+                                uint32_t nw2 = orc_kinop(norb, bdn[d], M, N);
+                                if (nw2 == 0) continue;
+                                int64_t pos2 = lin_rank(nw2, bdn, nsdn);
+                                if (pos2 <= 0) continue;
+                                double ac2 = orc_anticom(norb, M, bdn[d]);
+                                ac2 = ac2 * orc_anticom(norb, N, nw2);
+                                y[(pos2 - 1) * nsup + p] = y[(pos2 - 1) * nsup + p] + ac * ac2 * x[d * nsup + u] * uv;
+                            }
+                        }
+                }
+            }
+            if (nup != ndn) {
+                for (int64_t d = 0; d < nsdn; ++d) {
+                    uint32_t nw = orc_kinop(norb, bdn[d], J, K);
+                    if (nw == 0) continue;
+                    int64_t pos = lin_rank(nw, bdn, nsdn);
+                    if (pos <= 0) continue;
+                    double ac = orc_anticom(norb, J, bdn[d]);
+                    ac = ac * orc_anticom(norb, K, nw);
+                    int64_t p = pos - 1;
+                    for (int64_t u = 0; u < nsup; ++u)
+                        y[p * nsup + u] = y[p * nsup + u] + ac * x[d * nsup + u] * tjk;
+                }
+            }
+        }
+    }
+}
+
+/* TWO_RDM with DO_RQ_TB (static_rq.f90:247-306): DBL_OCC(J,K,M,N) =
+ * sum over the up hop J->K (string I -> POS) and the down hop M->N
+ * (L1 -> POS2) of AC*AC2*BRA((L1-1)*NSUP+I)*KET((POS2-1)*NSUP+POS), formed
+ * for K <= J and N <= M and copied to (J,K,N,M), (K,J,M,N), (K,J,N,M);
+ * NI(J) = DBL_OCC(J,J,J,J).  dbl: Fortran order, DBL_OCC(J,K,M,N) at
+ * (J-1) + (K-1) n + (M-1) n^2 + (N-1) n^3. */
+void orc_two_rdm_dbl_occ(int norb, const uint32_t *bup, int64_t nsup,
+                         const uint32_t *bdn, int64_t nsdn,
+                         const double *bra, const double *ket, double *dbl, double *ni)
+{
+    const int64_t n = norb;
+#define DO(J, K, M, N) dbl[((J) - 1) + ((K) - 1) * n + ((M) - 1) * n * n + ((N) - 1) * n * n * n]
+    for (int J = 1; J <= norb; ++J)
+        for (int K = 1; K <= J; ++K)
+            for (int M = 1; M <= norb; ++M)
+                for (int N = 1; N <= M; ++N) {
+                    double acc = 0.0;
+                    for (int64_t i = 0; i < nsup; ++i) {
+                        uint32_t nw = orc_kinop(norb, bup[i], J, K);
+                        if (nw == 0) continue;
+                        int64_t pos = lin_rank(nw, bup, nsup);
+                        if (pos <= 0) continue;
+                        double ac = orc_anticom(norb, J, bup[i]);
+                        ac = ac * orc_anticom(norb, K, nw);
+                        for (int64_t l1 = 0; l1 < nsdn; ++l1) {
+                            uint32_t nw2 = orc_kinop(norb, bdn[l1], M, N);
+                            if (nw2 == 0) continue;
+                            int64_t pos2 = lin_rank(nw2, bdn, nsdn);
+                            if (pos2 <= 0) continue;
+                            double ac2 = orc_anticom(norb, M, bdn[l1]);
+                            ac2 = ac2 * orc_anticom(norb, N, nw2);
+                            acc = acc + ac * ac2 * bra[l1 * nsup + i] * ket[(pos2 - 1) * nsup + (pos - 1)];
+                        }
+                    }
+                    DO(J, K, M, N) = acc;
+                    DO(J, K, N, M) = acc;
+                    DO(K, J, M, N) = acc;
+                    DO(K, J, N, M) = acc;
+                    if (J == K && J == M && J == N) ni[J - 1] = acc;
+                }
+#undef DO
+}

@@ -84,6 +84,8 @@ def lib():
             L.orc_j_spin.argtypes = [i32, P, i64, P, i64, P, P, P]
             L.orc_j_spin_heis.argtypes = [i32, P, i64, P, P, P]
             L.orc_gf_start.argtypes = [i32, i32, i32, i32, P, i64, P, i64, P, i64, P, i64, P, P]
+            L.orc_hprod_hubbard_uijkl_ref.argtypes = [i32, i32, i32, P, i64, P, i64, P, P, P, P]
+            L.orc_two_rdm_dbl_occ.argtypes = [i32, P, i64, P, i64, P, P, P, P]
             L.orc_unrank.restype = ctypes.c_uint32
             L.orc_unrank.argtypes = [i32, i32, i64]
             L.orc_hashval.restype = ctypes.c_double
@@ -156,6 +158,34 @@ def hprod_hubbard(sec: Sector, t, U, x, fast: bool = False, nthreads: int = 0) -
         lib().orc_hprod_hubbard_ref(sec.norb, sec.nup, sec.ndn, _p(sec.bup), sec.nsup, _p(sec.bdn),
                                     sec.nsdn, _p(t), _p(U), _p(x), _p(y))
     return y
+
+
+def hprod_hubbard_uijkl(sec: Sector, t, Ul, x) -> np.ndarray:
+    """y = H x with the U_ijkl interaction (IS_ULOC=3, hprod_hubbard.f90:17-118):
+    Ul is the (norb,)*4 tensor as handed to FermiHubbard (C order), read by the
+    reference as UL(J,K,M,N) = Ul[N-1,M-1,K-1,J-1] and gated per (J,K) by
+    UPARTIAL(J,K) = sum_cd Ul[K-1,J-1,c,d]^2."""
+    t = _f64(t)
+    Ul = _f64(Ul)
+    x = _f64(x)
+    y = np.empty_like(x)
+    lib().orc_hprod_hubbard_uijkl_ref(sec.norb, sec.nup, sec.ndn, _p(sec.bup), sec.nsup, _p(sec.bdn), sec.nsdn,
+                                      _p(t), _p(Ul), _p(x), _p(y))
+    return y
+
+
+def two_rdm_dbl_occ(sec: Sector, bra, ket=None):
+    """TWO_RDM with the two-body density (static_rq.f90:247-306): returns
+    (dbl, ni) with dbl[J-1,K-1,M-1,N-1] = DBL_OCC(J,K,M,N) (the array the
+    reference's two_rdm property returns for one state) and NI(J) =
+    DBL_OCC(J,J,J,J)."""
+    ket = bra if ket is None else ket
+    n = sec.norb
+    dbl = np.zeros(n ** 4)
+    ni = np.zeros(n)
+    lib().orc_two_rdm_dbl_occ(n, _p(sec.bup), sec.nsup, _p(sec.bdn), sec.nsdn, _p(_f64(bra)), _p(_f64(ket)),
+                              _p(dbl), _p(ni))
+    return dbl.reshape((n, n, n, n), order="F").copy(), ni
 
 
 def hprod_hubbard_pairs(sec: Sector, t, pairs, x, y, nthreads: int = 1) -> None:
@@ -591,6 +621,46 @@ def jw_hubbard_sector(sec: Sector, t, U) -> np.ndarray:
         H = term if H is None else H + term
     idx = np.array([_fock_index(norb, int(u), int(d)) for d in sec.bdn for u in sec.bup], dtype=np.int64)
     return H[idx][:, idx].toarray()
+
+
+def jw_hubbard_uijkl_sector(sec: Sector, t, Ul) -> np.ndarray:
+    """Dense sector matrix of sum_{J,K,s} T(J,K) c^+_{K s} c_{J s} +
+    sum UL(J,K,M,N) c^+_{K up} c_{J up} c^+_{N down} c_{M down} over
+    UPARTIAL(J,K) >= 1e-14 and |UL(J,K,M,N)| >= 1e-14, in the Fock space
+    (UL, UPARTIAL from Ul as the reference reads them)."""
+    norb = sec.norb
+    t = np.asarray(t, dtype=np.float64)
+    Ul = np.asarray(Ul, dtype=np.float64)
+    c = _jw_ops(2 * norb)
+    dn = lambda pos: c[pos - 1]
+    up = lambda pos: c[norb + pos - 1]
+    H = None
+    for J in range(1, norb + 1):
+        for K in range(1, norb + 1):
+            tjk = t[K - 1, J - 1]
+            if abs(tjk) >= F32_TOL14:
+                term = tjk * (up(K).T @ up(J) + dn(K).T @ dn(J))
+                H = term if H is None else H + term
+            if float(np.sum(Ul[K - 1, J - 1] ** 2)) < F32_TOL14:
+                continue
+            for M in range(1, norb + 1):
+                for N in range(1, norb + 1):
+                    v = Ul[N - 1, M - 1, K - 1, J - 1]
+                    if abs(v) < F32_TOL14:
+                        continue
+                    term = v * (up(K).T @ up(J) @ dn(N).T @ dn(M))
+                    H = term if H is None else H + term
+    idx = np.array([_fock_index(norb, int(u), int(d)) for d in sec.bdn for u in sec.bup], dtype=np.int64)
+    return H[idx][:, idx].toarray()
+
+
+def jw_two_body(sec: Sector, bra, ket, J: int, K: int, M: int, N: int) -> float:
+    """<ket| c^+_{K up} c_{J up} c^+_{N down} c_{M down} |bra> in the Fock space."""
+    norb = sec.norb
+    c = _jw_ops(2 * norb)
+    op = c[norb + K - 1].T @ c[norb + J - 1] @ c[N - 1].T @ c[M - 1]
+    idx = np.array([_fock_index(norb, int(u), int(d)) for d in sec.bdn for u in sec.bup], dtype=np.int64)
+    return float(np.asarray(ket) @ (op[idx][:, idx] @ np.asarray(bra)))
 
 
 def jw_heis_sector(norb: int, J, physical: bool = False) -> np.ndarray:

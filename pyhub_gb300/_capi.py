@@ -44,6 +44,9 @@ _SIGS = {
     "ed_batch_scratch_bytes": (_I64, [_P]),
     "ed_batch_lanczos": (_I, [_P, _P, _I, _P, _P, _I, _P, _P, _P, _I64]),
     "ed_batch_hv": (_I, [_P, _P, _I, _P, _P, _P, _I64]),
+    "ed_sector_set_uijkl": (_I, [_P, _P]),
+    "ed_dbl_occ_scratch_bytes": (_I64, [_P, _I]),
+    "ed_dbl_occ": (_I, [_P, _P, _I, _I64, _P, _P, _I, _P, _P, _P, _I64]),
     "ed_batch_ritz": (_I, [_P, _P, _I, _P, _P, _I, _P, _P, _P, _P, _P, _I64]),
     "ed_batch_create_rows": (_I, [_I, _P, _I, ctypes.POINTER(_P)]),
     "ed_batch_rows": (_I, [_P]),
@@ -254,6 +257,31 @@ class Sector:
         else:
             raw = o.reshape(npairs, 2)
         return raw, pr
+
+    def set_uijkl(self, Ul):
+        """Add the U_ijkl interaction (the reference's is_Uloc=3 path): Ul is
+        the (norb,)*4 tensor as FermiHubbard takes it; the on-site U is dropped."""
+        u = np.ascontiguousarray(Ul, dtype=np.float64).reshape((self.norb,) * 4)
+        self._keep = self._keep + (u,)
+        check("ed_sector_set_uijkl", lib().ed_sector_set_uijkl(self._h, u.ctypes.data))
+
+    def dbl_occ(self, bra, ket=None, quads=None, ld: int | None = None, stream=None):
+        """DBL_OCC(J,K,M,N) = <ket|c+_{K up} c_{J up} c+_{N down} c_{M down}|bra>
+        for the given 1-based quads ([n][4]); returns (host FP64 [n], quads)."""
+        import torch
+        ket = bra if ket is None else ket
+        q = np.ascontiguousarray(np.asarray(quads, dtype=np.int32).reshape(-1, 4))
+        out = torch.zeros(len(q), dtype=torch.float64, device=bra.device)
+        nb = int(lib().ed_dbl_occ_scratch_bytes(self._h, len(q)))
+        scratch = torch.empty((nb + 7) // 8, dtype=torch.float64, device=bra.device)
+        ld = self.ld if ld is None else ld
+        need = self._need(ld)
+        if ket.dtype != bra.dtype:
+            raise TypeError("bra and ket must have the same dtype")
+        check("ed_dbl_occ", lib().ed_dbl_occ(self._h, _stream(stream), dtype_code(bra.dtype), int(ld),
+                                             _ptr(bra, need, "bra"), _ptr(ket, need, "ket"), len(q), q.ctypes.data,
+                                             _ptr(out), _ptr(scratch), nb))
+        return out.cpu().numpy(), q
 
     def hv(self, x, y, scale: float = 1.0, dots=None, scratch=None, ld: int | None = None, stream=None):
         """y = scale * H x (device tensors in the internal layout unless ld is given)."""

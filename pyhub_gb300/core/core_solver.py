@@ -72,17 +72,29 @@ class CoreSolver(Basis, GreenFunction, StaticQuantities):
         U = np.asarray(U, dtype=np.float64)
         if U.ndim == 1 and U.shape == (self.nb_sites,):
             return U
-        if U.ndim == 4:
-            raise NotImplementedError("the U_ijkl interaction (is_Uloc=3) is not built")
+        if U.ndim == 4 and U.shape == (self.nb_sites,) * 4:
+            # is_Uloc=3 (core_solver.py:141-147): the interaction replaces the on-site U
+            if not np.isclose(U, np.einsum('ijkl->jilk', U)).all():
+                raise ValueError('U tensor must be symmetric')
+            return np.zeros(self.nb_sites)
         raise ValueError(f'U must be a float or a np.ndarray of size (nb_sites,) or '
                          f'(nb_sites,nb_sites,nb_sites,nb_sites,), not {type(self.U)}')
+
+    @property
+    def _uijkl(self):
+        """The U tensor when the interaction is the general U_ijkl (is_Uloc=3), else None."""
+        U = self.U
+        return U if isinstance(U, np.ndarray) and U.ndim == 4 else None
 
     def sector(self, nup: int, ndn: int):
         key = (int(nup), int(ndn))
         if key not in self._sectors:
             if self._kind == _capi.ED_HUBBARD:
-                self._sectors[key] = _capi.Sector(self.nb_sites, nup, ndn, _capi.ED_HUBBARD,
-                                                  t=np.asarray(self.t_matrix, dtype=np.float64), U=self._u_vector())
+                sec = _capi.Sector(self.nb_sites, nup, ndn, _capi.ED_HUBBARD,
+                                   t=np.asarray(self.t_matrix, dtype=np.float64), U=self._u_vector())
+                if self._uijkl is not None:
+                    sec.set_uijkl(self._uijkl)
+                self._sectors[key] = sec
             else:
                 self._sectors[key] = _capi.Sector(self.nb_sites, nup, ndn, _capi.ED_HEISENBERG,
                                                   J=np.asarray(self.J_matrix, dtype=np.float64))
@@ -253,6 +265,11 @@ class CoreSolver(Basis, GreenFunction, StaticQuantities):
         dm_dn = np.zeros((nw, N, N))
         ni = np.zeros((nw, N))
         sisj = np.zeros((nw, N, N))
+        two_body = self._uijkl is not None and self._kind == _capi.ED_HUBBARD
+        dbl = np.zeros((nw, N, N, N, N)) if two_body else None
+        # DBL_OCC is formed for K <= J and N <= M and copied to the three other orders (static_rq.f90:256-303)
+        quads = [(J, K, M, Nn) for J in range(1, N + 1) for K in range(1, J + 1)
+                 for M in range(1, N + 1) for Nn in range(1, M + 1)] if two_body else None
         for b in range(nw):
             if self.wgt[b] == 0.0 and b > 0:
                 continue
@@ -262,10 +279,18 @@ class CoreSolver(Basis, GreenFunction, StaticQuantities):
                 raw, _ = sec.rdm_raw(psi, pairs=all_pairs(N), flags=flags)
                 gu, gd, n_, sm = assemble_hubbard(raw, N, self.nup[0], self.ndown[0])
                 dm_up[b], dm_dn[b], ni[b], sisj[b] = gu, gd, n_, sm
+                if two_body:
+                    vals, _ = sec.dbl_occ(psi, quads=quads)
+                    for (J, K, M, Nn), v in zip(quads, vals):
+                        for a, c in ((J, K), (K, J)):
+                            dbl[b, a - 1, c - 1, M - 1, Nn - 1] = v
+                            dbl[b, a - 1, c - 1, Nn - 1, M - 1] = v
+                    ni[b] = [dbl[b, j, j, j, j] for j in range(N)]   # NI(J) = DBL_OCC(J,J,J,J) on this path
             else:
                 raw, _ = sec.rdm_raw(psi, pairs=all_pairs(N))
                 sisj[b] = assemble_heisenberg(raw, N)
-        self._rq = {"density_matrix_up": dm_up, "density_matrix_down": dm_dn, "ni": ni, "sisj": sisj}
+        self._rq = {"density_matrix_up": dm_up, "density_matrix_down": dm_dn, "ni": ni, "sisj": sisj,
+                    "dbl_occ": dbl}
         self.is_reduced_quantities = True
         self.printv(f'end calculation | elapsed time {np.around(pc() - t0, 4)} s')
 

@@ -76,7 +76,13 @@ class StaticQuantities:
 
     @property
     def two_rdm(self):
-        raise NotImplementedError("the two-body density (dbl_occ, U_ijkl path is_Uloc=3) is not built")
+        """DBL_OCC(J,K,M,N) weighted over the states, as the reference's
+        two_rdm returns it (reduced_quantities.py:25-27): [J-1,K-1,M-1,N-1].
+        Stored only for the U_ijkl interaction (is_Uloc=3), as in the reference."""
+        dbl = self._rq.get("dbl_occ") if self._rq else None
+        if dbl is None:
+            raise KeyError("reduced_quantities/dbl_occ is formed only for the U_ijkl interaction (is_Uloc=3)")
+        return np.einsum("bijkl,b->ijkl", dbl, self._wnorm())
 
     @property
     def density(self):
@@ -124,8 +130,14 @@ class StaticQuantities:
 
     @property
     def e_two_body(self):
-        return (np.sum(self.ni * self.U_matrix)
-                + np.einsum("bij,ij,b", self._rq["sisj"], self.J_matrix, self._wnorm()))
+        """reduced_quantities.py:68-75: with the U_ijkl interaction the
+        reference contracts its dbl_occ dataset ('lkjib' of the file's
+        [N][M][K][J][b] = DBL_OCC(J,K,M,N)) with U[i,j,k,l]."""
+        sj = np.einsum("bij,ij,b", self._rq["sisj"], self.J_matrix, self._wnorm())
+        dbl = self._rq.get("dbl_occ") if self._rq else None
+        if dbl is not None:
+            return np.einsum("bijkl,ijkl,b", dbl, self.U_matrix, self._wnorm()) + sj
+        return np.sum(self.ni * self.U_matrix) + sj
 
 
 class GreenFunction:

@@ -72,6 +72,13 @@ struct HopTable {
     float *ell_cf32 = nullptr;
     double *ell_cf64 = nullptr;
     int2 *ell_pk32 = nullptr;      // [ell_slots*32] {src, FP32 coefficient bits}: one 8-byte load per slot
+    // When every hop coefficient has one magnitude (|t| the same on every
+    // bond, as on the usual lattice models) and n < 32767: the same slots as
+    // 2-byte entries, bit 15 the sign of the coefficient, bits 0..14 the
+    // source; padding slots read source n (a zero column the row kernel
+    // appends) with coefficient +ell_mag.  ell_mag = 0: no such table.
+    uint16_t *ell_s16 = nullptr;   // [ell_slots*32]
+    float ell_mag = 0.0f;
     bool owner = true;
 };
 
@@ -122,6 +129,21 @@ struct HeisStruct {
     double ab_fjk[kMaxAB] = {}, ab_fkj[kMaxAB] = {}, ab_zz[kMaxAB] = {};
 };
 
+// The U_ijkl interaction of a Hubbard sector (the reference's IS_ULOC=3):
+// terms UL(J,K,M,N) c+_{K up} c_{J up} c+_{N down} c_{M down}, grouped by the
+// down pair (M,N); one device allocation.
+struct UijklTables {
+    int ngroups = 0, nterms = 0;
+    int4 *groups = nullptr;    // {M, N, first term, count}
+    int2 *jk = nullptr;        // {J, K} per term
+    double *val = nullptr;     // UL(J,K,M,N) per term
+    float *val32 = nullptr;
+    void *pool = nullptr;
+};
+
+int uijkl_hv(ed_sector *s, cudaStream_t st, int dtype, int64_t ld, const void *x, void *y, double scale);
+void uijkl_free(UijklTables *u);
+
 int heis_struct_build(ed_sector *s);
 void heis_struct_free(HeisStruct *hs);
 int heis_struct_hv(ed_sector *s, cudaStream_t st, int dtype, const void *x, void *y, double scale, double *dots,
@@ -142,6 +164,7 @@ struct ed_sector {
     double u_value = 0.0;
     ed::HeisTables heis;
     ed::HeisStruct *hs = nullptr;  // Heisenberg row tables
+    ed::UijklTables *uijkl = nullptr;   // U_ijkl terms (ed_sector_set_uijkl), else NULL
     // colex rank of an empty-site pattern h (bit j: site j+1 empty) in byte
     // chunks, shared by every kernel that ranks strings on the fly:
     // rank = sum_b lut[b][popcount(h & (2^(8b)-1))][byte b of h]

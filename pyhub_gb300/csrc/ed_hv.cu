@@ -17,6 +17,7 @@
 #include "ed_common.cuh"
 
 #include <cstdlib>
+#include <cstring>
 
 namespace ed {
 
@@ -27,6 +28,8 @@ struct HubArgs {
     int64_t nslice;
     const int32_t *ell_off; const int32_t *ell_src;
     const int2 *ell_pk32;
+    const uint16_t *ell_s16;   // 2-byte slots (one coefficient magnitude), or NULL
+    uint32_t mag_bits;         // FP32 bits of that magnitude
     double u_site[kMaxSites];
     float u_site32[kMaxSites];
     int u_uniform;
@@ -237,6 +240,88 @@ __global__ void __launch_bounds__(1024) hub_row_col4_kernel(const float *__restr
     }
 }
 
+// The four-row column kernel with 2-byte hop-table slots (every coefficient
+// +-tau): a slot is the source string in bits 0..14 and the sign of the
+// coefficient in bit 15, so a warp reads one slot with one 64-byte load
+// instead of 256 bytes.  Padding slots read column nsup, which the kernel
+// stages as zeros.
+template <int G>
+__device__ __forceinline__ void col_group_s16(const uint16_t *__restrict__ s16, int64_t at, uint32_t mag_bits,
+                                              const float4 *xs4, float (&acc)[4])
+{
+    uint32_t v[G];
+#pragma unroll
+    for (int i = 0; i < G; ++i) v[i] = __ldg(s16 + at + i * 32);
+#pragma unroll
+    for (int i = 0; i < G; ++i) {
+        const float c = __uint_as_float(mag_bits | ((v[i] & 0x8000u) << 16));
+        const float4 x = xs4[v[i] & 0x7fffu];
+        acc[0] += c * x.x;
+        acc[1] += c * x.y;
+        acc[2] += c * x.z;
+        acc[3] += c * x.w;
+    }
+}
+
+__global__ void __launch_bounds__(1024) hub_row_col4_s16_kernel(const float *__restrict__ x, float *__restrict__ y,
+                                                                const HubArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float4 *xs4 = reinterpret_cast<float4 *>(smem_raw);   // [nsup + 1], column nsup = 0
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    const int64_t nsup = a.nsup, ld = a.ld;
+    const float uval = (float)a.u_value, sc = (float)a.scale;
+    const float *ued_t = static_cast<const float *>(a.uediag), *ded_t = static_cast<const float *>(a.dediag);
+    if (threadIdx.x == 0) xs4[nsup] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int64_t d0 = (int64_t)blockIdx.x * 4; d0 < a.nsdn; d0 += (int64_t)gridDim.x * 4) {
+        const int nr = (int)min((int64_t)4, a.nsdn - d0);
+        const float *x0 = x + d0 * ld;
+        for (int64_t c = threadIdx.x; c < nsup; c += blockDim.x) {
+            float4 v;
+            v.x = __ldg(x0 + c);
+            v.y = nr > 1 ? __ldg(x0 + ld + c) : 0.f;
+            v.z = nr > 2 ? __ldg(x0 + 2 * ld + c) : 0.f;
+            v.w = nr > 3 ? __ldg(x0 + 3 * ld + c) : 0.f;
+            xs4[c] = v;
+        }
+        __syncthreads();
+        uint32_t sd[4];
+        float ed[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            sd[r] = (r < nr) ? __ldg(a.dstr + d0 + r) : 0u;
+            ed[r] = (r < nr) ? __ldg(ded_t + d0 + r) : 0.f;
+        }
+        for (int64_t sl = warp; sl < a.nslice; sl += nwarps) {
+            const int64_t u = sl * 32 + lane;
+            const bool ok = u < nsup;
+            const int64_t uu = ok ? u : nsup - 1;
+            const uint32_t su = __ldg(a.ustr + uu);
+            const float eu = __ldg(ued_t + uu);
+            const float4 xv = xs4[uu];
+            const float xr[4] = {xv.x, xv.y, xv.z, xv.w};
+            float acc[4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r) acc[r] = (eu + ed[r] + u_energy<float>(a, su & sd[r], uval)) * xr[r];
+            const int s0 = __ldg(a.ell_off + sl), ns = __ldg(a.ell_off + sl + 1) - s0;
+            const int64_t at0 = (int64_t)s0 * 32 + lane;
+            int k = 0;
+            for (; k + 8 <= ns; k += 8) col_group_s16<8>(a.ell_s16, at0 + k * 32, a.mag_bits, xs4, acc);
+            if (k + 4 <= ns) {
+                col_group_s16<4>(a.ell_s16, at0 + k * 32, a.mag_bits, xs4, acc);
+                k += 4;
+            }
+            for (; k < ns; ++k) col_group_s16<1>(a.ell_s16, at0 + k * 32, a.mag_bits, xs4, acc);
+            if (ok) {
+#pragma unroll
+                for (int r = 0; r < 4; ++r)
+                    if (r < nr) y[(d0 + r) * ld + u] = acc[r] * sc;
+            }
+        }
+        __syncthreads();
+    }
+}
+
 constexpr int kSlabLoads = 4;   // neighbour-row loads in flight per warp in the slab pass (8 costs occupancy)
 
 // Pass 2: down hops, y[d][slab] += sum_e c_e x[src_e][slab]; optional dots.
@@ -414,6 +499,13 @@ static int hub_hv(ed_sector *s, cudaStream_t st, int64_t ld, const T *x, T *y, d
     a.ell_off = s->up.ell_off;
     a.ell_src = s->up.ell_src;
     a.ell_pk32 = s->up.ell_pk32;
+    a.ell_s16 = (s->up.ell_mag > 0.0f) ? s->up.ell_s16 : nullptr;
+    {
+        const float m = s->up.ell_mag;
+        uint32_t bits;
+        std::memcpy(&bits, &m, sizeof(bits));
+        a.mag_bits = bits;
+    }
     for (int b = 0; b < kMaxSites; ++b) {
         a.u_site[b] = s->u_site[b];
         a.u_site32[b] = (float)s->u_site[b];
@@ -444,7 +536,16 @@ static int hub_hv(ed_sector *s, cudaStream_t st, int64_t ld, const T *x, T *y, d
     constexpr int R2 = 2;
     const bool two = (size_t)R2 * row_bytes * 2 <= (size_t)maxsm;
     const int threads = 512;
-    if (sizeof(T) == 4 && (size_t)s->nsup * 16 <= (size_t)maxsm) {
+    if (sizeof(T) == 4 && a.ell_s16 != nullptr && (size_t)(s->nsup + 1) * 16 <= (size_t)maxsm) {
+        // four rows per 1024-thread CTA, 2-byte hop-table slots
+        const size_t smem = (size_t)(s->nsup + 1) * 16;
+        int64_t blocks = (s->nsdn + 3) / 4;
+        if (blocks > nsm) blocks = nsm;
+        ED_CHECK_CUDA(cudaFuncSetAttribute(hub_row_col4_s16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem));
+        hub_row_col4_s16_kernel<<<(unsigned)blocks, 1024, smem, st>>>(reinterpret_cast<const float *>(x),
+                                                                      reinterpret_cast<float *>(y), a);
+    } else if (sizeof(T) == 4 && (size_t)s->nsup * 16 <= (size_t)maxsm) {
         // four rows per 1024-thread CTA, staged as 16-byte columns
         const size_t smem = (size_t)s->nsup * 16;
         int64_t blocks = (s->nsdn + 3) / 4;
@@ -469,6 +570,11 @@ static int hub_hv(ed_sector *s, cudaStream_t st, int64_t ld, const T *x, T *y, d
         hub_row_kernel<T, 1><<<(unsigned)blocks, threads, smem, st>>>(x, y, a, sld, vec_ok ? 1 : 0);
     }
     ED_CHECK_LAUNCH();
+    // ---- the U_ijkl terms, if any (before pass 2, whose fused dots need the whole product)
+    if (s->uijkl) {
+        const int rc = uijkl_hv(s, st, sizeof(T) == 4 ? ED_F32 : ED_F64, ld, x, y, scale);
+        if (rc != ED_OK) return rc;
+    }
     // ---- pass 2
     // slab width: the x slab (nsdn rows x width) should take at most slab_l2_bytes() of L2
     int64_t slab_w = (int64_t)(slab_l2_bytes() / ((double)s->nsdn * sizeof(T)));
@@ -478,7 +584,16 @@ static int hub_hv(ed_sector *s, cudaStream_t st, int64_t ld, const T *x, T *y, d
     const int64_t ngroups = (s->nsdn + 7) / 8;
     const int64_t nslab = (s->nsup + slab_w - 1) / slab_w;
     const int64_t nitems = ngroups * nslab;
-    int64_t blocks2 = (int64_t)nsm * 8;
+    // one wave of resident CTAs: each walks its share of the items, so a grid past the
+    // resident count would leave a second, partial wave running whole shares
+    const bool vec2pre = (ld % VWS == 0);
+    int per_sm = 0;
+    if (vec2pre)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hub_slab_kernel<T, VWS>, 256, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hub_slab_kernel<T, 1>, 256, 0);
+    if (per_sm < 1) per_sm = 1;
+    int64_t blocks2 = (int64_t)nsm * per_sm;
     if (blocks2 > kMaxPartialBlocks) blocks2 = kMaxPartialBlocks;
     if (blocks2 > nitems) blocks2 = nitems;
     if (blocks2 < 1) blocks2 = 1;

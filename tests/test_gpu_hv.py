@@ -103,6 +103,33 @@ def test_hubbard_f32_within_bound(edlib, case):
         assert np.all(np.abs(y - yref) <= bound + 1e-30)
 
 
+@pytest.mark.parametrize("case", [(4, 2, 2), (8, 4, 4), (9, 4, 5), (12, 6, 6), (12, 5, 7)])
+def test_hubbard_f32_single_magnitude_hopping(edlib, case):
+    """Hopping of one magnitude with both signs (the 2-byte-slot row pass):
+    FP32 within 64 eps32 (|H||x|)_i of the oracle (exact enumeration for the
+    larger sectors: the FP64 product of the FP32-rounded x), bit-exact for
+    integer x, with per-site U and on-site energies."""
+    import torch
+    norb, nu, nd = case
+    rng = np.random.default_rng(3 * norb + nu)
+    mask = rng.random((norb, norb)) < 0.45
+    t = np.where(mask, np.where(rng.random((norb, norb)) < 0.5, -1.0, 1.0), 0.0)
+    t = np.triu(t, 1) + np.triu(t, 1).T
+    t[np.diag_indices(norb)] = rng.integers(-2, 3, norb)
+    U = rng.integers(0, 9, norb).astype(np.float64)
+    osec = O.Sector(norb, nu, nd)
+    sec = edlib.Sector(norb, nu, nd, edlib.ED_HUBBARD, t=t, U=U)
+    xi = rng.integers(-8, 9, size=osec.dim).astype(np.float64)
+    yi = O.hprod_hubbard(osec, t, U, xi, fast=True)
+    for layout in (None, sec.ld):
+        assert np.array_equal(_run(edlib, sec, xi, torch.float32, layout), yi)
+    x = rng.standard_normal(osec.dim).astype(np.float32).astype(np.float64)
+    yref = O.hprod_hubbard(osec, t, U, x, fast=True)
+    babs = O.hprod_hubbard(osec, np.abs(t), np.abs(U), np.abs(x), fast=True)   # (|H||x|)_i
+    y = _run(edlib, sec, x, torch.float32, sec.ld)
+    assert np.all(np.abs(y - yref) <= 64 * EPS32 * babs + 1e-30)
+
+
 def test_hubbard_fused_dots(edlib):
     import torch
     norb, nu, nd = 10, 5, 4

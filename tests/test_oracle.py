@@ -326,3 +326,36 @@ def test_self_energy_restatement_vanishes_without_interaction():
         S = O.self_energy_ref(Vk, ek, e[:1], [1.0], sp, 0.37, 0.1, True)
         mag = np.abs(S["up"]).max()
         assert (mag < 1e-9) if zero else (mag > 1e-3), (U, mag)
+
+
+def _uijkl(rng, n, density=0.4):
+    Ul = rng.standard_normal((n,) * 4) * (rng.random((n,) * 4) < density)
+    Ul = 0.5 * (Ul + np.einsum("ijkl->jilk", Ul))   # the symmetry the reference requires (core_solver.py:143)
+    Ul[1, 0] = 0.0                                  # a (J,K) pair gated off by UPARTIAL
+    return Ul
+
+
+@pytest.mark.parametrize("case", [(4, 2, 2), (4, 2, 1), (5, 2, 3), (5, 3, 3)])
+def test_uijkl_restatement_equals_jordan_wigner(case):
+    """IS_ULOC=3: the HPROD restatement (index order UL(J,K,M,N) =
+    U[N-1,M-1,K-1,J-1], UPARTIAL gate) equals the Fock-space construction,
+    and DBL_OCC of TWO_RDM equals <ket|c+_K c_J c+_N c_M|bra> for K<=J, N<=M."""
+    n, nu, nd = case
+    rng = np.random.default_rng(n * 10 + nu)
+    sec = O.Sector(n, nu, nd)
+    t = rng.standard_normal((n, n))
+    t = t + t.T
+    Ul = _uijkl(rng, n)
+    H = O.jw_hubbard_uijkl_sector(sec, t, Ul)
+    Hd = O.dense_h(lambda v: O.hprod_hubbard_uijkl(sec, t, Ul, v), sec.dim)
+    assert np.abs(H - Hd).max() <= 1e-13 * max(1.0, np.abs(H).max())
+    bra, ket = rng.standard_normal(sec.dim), rng.standard_normal(sec.dim)
+    dbl, ni = O.two_rdm_dbl_occ(sec, bra, ket)
+    for J in range(1, n + 1):
+        for K in range(1, J + 1):
+            for M in range(1, n + 1):
+                for N in range(1, M + 1):
+                    v = O.jw_two_body(sec, bra, ket, J, K, M, N)
+                    assert abs(dbl[J - 1, K - 1, M - 1, N - 1] - v) <= 1e-12, (J, K, M, N)
+                    assert dbl[K - 1, J - 1, N - 1, M - 1] == dbl[J - 1, K - 1, M - 1, N - 1]
+    assert np.array_equal(ni, [dbl[j, j, j, j] for j in range(n)])
