@@ -242,6 +242,25 @@ int ed_batch_hv(ed_batch *b, void *stream, int dtype, const void *x, void *y, vo
  * call can be captured in a CUDA graph. */
 int ed_batch_lanczos(ed_batch *b, void *stream, int dtype, void *work, const void *x0, int nsteps,
                      double *alpha, double *beta, void *scratch, int64_t scratch_bytes);
+/* ed_batch_lanczos (kept == NULL; work: 3*total elements) or
+ * ed_batch_lanczos_kept (kept: (nsteps+1)*total elements; work: y, total
+ * elements) as ONE persistent cooperative launch that runs every step of
+ * every instance: CTAs walk a phase-major list of (phase, CTA-block) items,
+ * each waiting until its instance has finished the previous phase, and the
+ * last CTA of an instance to finish a phase forms that instance's scalars.
+ * The instances are split into two groups one phase apart, so the H*v of
+ * one group runs beside the update of the other.  alpha/beta are
+ * bit-identical to the four-launch form.  Every wait is bounded (10 s of GPU
+ * time); a run that gives up sets a status that ed_batch_persistent_status
+ * returns (0 = ok) and stops.  Enqueues one memset and one launch, so the
+ * call can be captured in a CUDA graph.  The per-start-block loops of
+ * GF_BANDLANCZOS (spgf_bandlanczos.f90:309-448) for many instances at once. */
+int ed_batch_lanczos_persistent(ed_batch *b, void *stream, int dtype, void *work, const void *x0, int nsteps,
+                                double *alpha, double *beta, void *kept, void *scratch, int64_t scratch_bytes);
+/* Status of the last persistent run that used this scratch (synchronous
+ * copy to the host): 0 = completed, 1 = a wait gave up.  No reference
+ * counterpart. */
+int ed_batch_persistent_status(const ed_batch *b, const void *scratch, int *status);
 /* Replay of ed_batch_lanczos from the same x0 that also accumulates, per
  * instance, the Ritz vector out_i += sum_k coef[i][k] q_k (q_k the
  * normalised Lanczos vectors; coef device FP64 [ninst][nsteps], typically the

@@ -45,6 +45,8 @@ _SIGS = {
     "ed_batch_lanczos": (_I, [_P, _P, _I, _P, _P, _I, _P, _P, _P, _I64]),
     "ed_batch_hv": (_I, [_P, _P, _I, _P, _P, _P, _I64]),
     "ed_sector_set_uijkl": (_I, [_P, _P]),
+    "ed_batch_lanczos_persistent": (_I, [_P, _P, _I, _P, _P, _I, _P, _P, _P, _P, _I64]),
+    "ed_batch_persistent_status": (_I, [_P, _P, ctypes.POINTER(_I)]),
     "ed_dbl_occ_scratch_bytes": (_I64, [_P, _I]),
     "ed_dbl_occ": (_I, [_P, _P, _I, _I64, _P, _P, _I, _P, _P, _P, _I64]),
     "ed_batch_ritz": (_I, [_P, _P, _I, _P, _P, _I, _P, _P, _P, _P, _P, _I64]),
@@ -345,6 +347,26 @@ class Batch:
         check("ed_batch_hv", lib().ed_batch_hv(self._h, _stream(stream), dtype_code(x.dtype),
                                                _ptr(x, self.total, "x"), _ptr(y, self.total, "y"), _ptr(scratch),
                                                int(scratch.numel() * scratch.element_size())))
+
+    def lanczos_persistent(self, work, x0, nsteps: int, alpha, beta, scratch, kept=None, stream=None):
+        """The same run as lanczos() (kept=None; work 3*total) or lanczos_kept()
+        (kept basis; work = y) in one persistent cooperative launch."""
+        need = self.total if kept is not None else 3 * self.total
+        if kept is not None:
+            self._check(work, x0, nsteps, alpha, beta, work_need=self.total)
+        else:
+            self._check(work, x0, nsteps, alpha, beta)
+        check("ed_batch_lanczos_persistent", lib().ed_batch_lanczos_persistent(
+            self._h, _stream(stream), dtype_code(x0.dtype), _ptr(work, need, "work"), _ptr(x0, self.total, "x0"),
+            int(nsteps), _ptr(alpha), _ptr(beta),
+            None if kept is None else _ptr(kept, (int(nsteps) + 1) * self.total, "kept"), _ptr(scratch),
+            int(scratch.numel() * scratch.element_size())))
+
+    def persistent_status(self, scratch) -> int:
+        st = _I()
+        check("ed_batch_persistent_status", lib().ed_batch_persistent_status(self._h, _ptr(scratch),
+                                                                             ctypes.byref(st)))
+        return st.value
 
     def lanczos(self, work, x0, nsteps: int, alpha, beta, scratch, stream=None):
         sb = scratch.numel() * scratch.element_size()

@@ -72,7 +72,7 @@ class BatchedLanczos:
     (Ritz vectors by one pass over them, _ritz_cycle) instead of two; "auto"
     keeps them when they fit in half of the free device memory."""
 
-    def __init__(self, sectors, nsteps: int, dtype=None, device="cuda", rows=8, keep=False):
+    def __init__(self, sectors, nsteps: int, dtype=None, device="cuda", rows=8, keep=False, persistent=False):
         torch = _torch()
         self.dtype = dtype or torch.float32
         self.nsteps = int(nsteps)
@@ -101,12 +101,17 @@ class BatchedLanczos:
         self.beta = torch.zeros((n, self.nsteps + 1), dtype=torch.float64, device=device)
         self.scratch = torch.empty(self.batch.scratch_bytes() // 8 + 1, dtype=torch.float64, device=device)
         self.graph = None
+        # persistent: the whole run is one cooperative launch (ed_batch_lanczos_persistent)
+        self.persistent = bool(persistent)
 
     def start(self, i: int):
         return self.batch.view(self.x0, i)
 
     def run(self):
-        if self.keep:
+        if self.persistent:
+            self.batch.lanczos_persistent(self.work, self.x0, self.nsteps, self.alpha, self.beta, self.scratch,
+                                          kept=self.basis if self.keep else None)
+        elif self.keep:
             self.batch.lanczos_kept(self.basis, self.work, self.x0, self.nsteps, self.alpha, self.beta, self.scratch)
         else:
             self.batch.lanczos(self.work, self.x0, self.nsteps, self.alpha, self.beta, self.scratch)

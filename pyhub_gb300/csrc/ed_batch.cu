@@ -66,6 +66,8 @@ struct ed_batch {
     int max_nsup = 0;
     int max_ld = 0;
     int rows = 8;                      // rows per CTA (4, 8 or 16)
+    int32_t *order = nullptr;          // [nblocks] device: persistent-run item order of one super-phase
+    int8_t *grp = nullptr;             // [ninst] device: phase offset (0 or 1) of each instance
 };
 
 namespace ed {
@@ -226,8 +228,9 @@ __device__ __forceinline__ void up_group(const BatchInst &a, const T *xs, int at
     }
 }
 
-// G down-hop neighbour rows (16-byte vector v of each): loads issued together.
-template <typename T, int G>
+// G down-hop neighbour rows (16-byte vector v of each): loads issued together
+// (COH: L2-coherent loads, for the persistent run).
+template <typename T, int G, bool COH>
 __device__ __forceinline__ void down_group(const NbEnt<T> *en, const T *__restrict__ ub, int v,
                                            typename V16<T>::type &acc)
 {
@@ -238,7 +241,8 @@ __device__ __forceinline__ void down_group(const NbEnt<T> *en, const T *__restri
     for (int j = 0; j < G; ++j) {
         const NbEnt<T> e = en[j];
         cf[j] = e.cf;
-        xn[j] = __ldg(reinterpret_cast<const V *>(ub + e.off) + v);
+        if constexpr (COH) xn[j] = __ldcg(reinterpret_cast<const V *>(ub + e.off) + v);
+        else xn[j] = __ldg(reinterpret_cast<const V *>(ub + e.off) + v);
     }
 #pragma unroll
     for (int j = 0; j < G; ++j)
@@ -246,32 +250,38 @@ __device__ __forceinline__ void down_group(const NbEnt<T> *en, const T *__restri
         for (int k = 0; k < V16<T>::n; ++k) vat(acc, k) += cf[j] * reinterpret_cast<const T *>(&xn[j])[k];
 }
 
+// Loads of data another CTA may have written earlier in the same launch
+// (the persistent run): L2 only, never a possibly stale L1 line.  Loads of
+// data written before the launch can use the read-only path.
+template <bool COH, typename V> __device__ __forceinline__ V ld_data(const V *p)
+{
+    if constexpr (COH) return __ldcg(p);
+    else return __ldg(p);
+}
+
 // y = s_k H u_k and partial <u_k, y> over R rows of one instance.
 // Phase A (diagonal + up hops): the rows are staged in shared memory one
-// column per string (asynchronous copies, all in flight together); a warp owns 32-string slices, loads each sliced-ELL
-// slot once and applies it to all rows with 16-byte shared loads; the sums
-// go to y.  Phase B (down hops): each row adds its neighbour rows as
-// 16-byte-vector axpys read from L2 (the instances in flight keep their
-// vectors there), then scales, stores and forms the dot product.
-template <typename T, int R>
-__global__ void __launch_bounds__(kBatchThreads) batch_hv_kernel(const BatchInst *__restrict__ inst,
-                                                                 const int32_t *__restrict__ blk_inst,
-                                                                 const T *__restrict__ u, T *__restrict__ y,
-                                                                 const double *__restrict__ scal,
-                                                                 double *__restrict__ part_out)
+// column per string (asynchronous copies, all in flight together; in the
+// persistent run coherent loads in groups of 4); a warp owns 32-string
+// slices, loads each sliced-ELL slot once and applies it to all rows with
+// 16-byte shared loads; the sums go to y.  Phase B (down hops): each row
+// adds its neighbour rows as 16-byte-vector axpys read from L2 (the
+// instances in flight keep their vectors there), then scales, stores and
+// forms the dot product.
+template <typename T, int R, bool COH>
+__device__ __forceinline__ void hv_item(const BatchInst *__restrict__ inst, int64_t b, int i,
+                                        const T *__restrict__ u, T *__restrict__ y, double sk,
+                                        double *__restrict__ part_out, unsigned char *smem_raw)
 {
     using V = typename V16<T>::type;
     constexpr int VN = V16<T>::n;
     constexpr int S = staged_stride<T, R>();
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     T *xs = reinterpret_cast<T *>(smem_raw);   // [nsup][S]
     __shared__ NbEnt<T> nb[R][kMaxNb];
     __shared__ int nb_n[R], nb_e0[R];
     __shared__ uint32_t row_str[R];
     __shared__ T row_ed[R];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = kBatchThreads / 32;
-    const int64_t b = blockIdx.x;
-    const int i = __ldg(blk_inst + b);
     const BatchInst &a = inst[i];
     const int r0 = (int)((b - a.blk0) * R);
     const int nr = (int)min((int64_t)R, a.nsdn - r0);
@@ -281,13 +291,40 @@ __global__ void __launch_bounds__(kBatchThreads) batch_hv_kernel(const BatchInst
     const T *dcf = (sizeof(T) == 4) ? reinterpret_cast<const T *>(a.dcf32) : reinterpret_cast<const T *>(a.dcf64);
     const T *ued_t = (sizeof(T) == 4) ? reinterpret_cast<const T *>(a.uediag32) : reinterpret_cast<const T *>(a.uediag);
     const T *ded_t = (sizeof(T) == 4) ? reinterpret_cast<const T *>(a.dediag32) : reinterpret_cast<const T *>(a.dediag);
-    for (int r = 0; r < R; ++r) {
-        const T *src = ub + (int64_t)(r0 + r) * ld;
-        for (int c = threadIdx.x; c < nsup; c += blockDim.x) {
-            if (r < nr)
-                cp_async_elem(xs + c * S + r, src + c);
-            else
-                xs[c * S + r] = (T)0;
+    if constexpr (COH) {
+        // 16-byte coherent loads (rows are 16-byte aligned and zero padded), 8 in flight per
+        // thread, each scattered into the column layout
+        const int nvr = (nsup + VN - 1) / VN, nvt = R * nvr;
+        for (int i0 = threadIdx.x; i0 < nvt; i0 += 8 * kBatchThreads) {
+            V w[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int i = i0 + j * kBatchThreads;
+                const int r = i / nvr, v = i - r * nvr;
+                w[j] = (i < nvt && r < nr) ? __ldcg(reinterpret_cast<const V *>(ub + (int64_t)(r0 + r) * ld) + v)
+                                           : V{};
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int i = i0 + j * kBatchThreads;
+                if (i >= nvt) break;
+                const int r = i / nvr, v = i - r * nvr;
+#pragma unroll
+                for (int k = 0; k < VN; ++k) {
+                    const int c = v * VN + k;
+                    if (c < nsup) xs[c * S + r] = reinterpret_cast<const T *>(&w[j])[k];
+                }
+            }
+        }
+    } else {
+        for (int r = 0; r < R; ++r) {
+            const T *src = ub + (int64_t)(r0 + r) * ld;
+            for (int c = threadIdx.x; c < nsup; c += blockDim.x) {
+                if (r < nr)
+                    cp_async_elem(xs + c * S + r, src + c);
+                else
+                    xs[c * S + r] = (T)0;
+            }
         }
     }
     for (int r = warp; r < R; r += nwarps) {
@@ -307,7 +344,7 @@ __global__ void __launch_bounds__(kBatchThreads) batch_hv_kernel(const BatchInst
             row_ed[r] = (r < nr) ? __ldg(ded_t + r0 + r) : (T)0;
         }
     }
-    cp_async_wait_all();
+    if constexpr (!COH) cp_async_wait_all();
     __syncthreads();
     // ---- phase A
     for (int sl = warp; sl < a.nslice; sl += nwarps) {
@@ -338,7 +375,7 @@ __global__ void __launch_bounds__(kBatchThreads) batch_hv_kernel(const BatchInst
     }
     __syncthreads();   // phase A's rows of y are visible to the whole CTA
     // ---- phase B
-    const T sc = (T)scal[(int64_t)i * kScal + kS];
+    const T sc = (T)sk;
     const int nvec = ld / VN, chunks = (nvec + 31) / 32;
     T dotp = 0;
     for (int task = warp; task < nr * chunks; task += nwarps) {
@@ -348,19 +385,19 @@ __global__ void __launch_bounds__(kBatchThreads) batch_hv_kernel(const BatchInst
         const int nn = nb_n[r], nl = min(nn, kMaxNb);
         // neighbour rows in groups of loads in flight
         int e = 0;
-        for (; e + 8 <= nl; e += 8) down_group<T, 8>(&nb[r][e], ub, v, acc);
+        for (; e + 8 <= nl; e += 8) down_group<T, 8, COH>(&nb[r][e], ub, v, acc);
         if (e + 4 <= nl) {
-            down_group<T, 4>(&nb[r][e], ub, v, acc);
+            down_group<T, 4, COH>(&nb[r][e], ub, v, acc);
             e += 4;
         }
-        for (; e < nl; ++e) down_group<T, 1>(&nb[r][e], ub, v, acc);
+        for (; e < nl; ++e) down_group<T, 1, COH>(&nb[r][e], ub, v, acc);
         for (int e = kMaxNb; e < nn; ++e) {
             const T cf = __ldg(dcf + nb_e0[r] + e);
-            const V xn = __ldg(reinterpret_cast<const V *>(ub + (int64_t)__ldg(a.dsrc + nb_e0[r] + e) * ld) + v);
+            const V xn = ld_data<COH>(reinterpret_cast<const V *>(ub + (int64_t)__ldg(a.dsrc + nb_e0[r] + e) * ld) + v);
 #pragma unroll
             for (int k = 0; k < VN; ++k) vat(acc, k) += cf * reinterpret_cast<const T *>(&xn)[k];
         }
-        const V xo = __ldg(reinterpret_cast<const V *>(ub + (int64_t)(r0 + r) * ld) + v);
+        const V xo = ld_data<COH>(reinterpret_cast<const V *>(ub + (int64_t)(r0 + r) * ld) + v);
 #pragma unroll
         for (int k = 0; k < VN; ++k) {
             T val = vat(acc, k) * sc;
@@ -373,28 +410,31 @@ __global__ void __launch_bounds__(kBatchThreads) batch_hv_kernel(const BatchInst
     block_partial((double)dotp, part_out + b);
 }
 
+template <typename T, int R>
+__global__ void __launch_bounds__(kBatchThreads) batch_hv_kernel(const BatchInst *__restrict__ inst,
+                                                                 const int32_t *__restrict__ blk_inst,
+                                                                 const T *__restrict__ u, T *__restrict__ y,
+                                                                 const double *__restrict__ scal,
+                                                                 double *__restrict__ part_out)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int64_t b = blockIdx.x;
+    const int i = __ldg(blk_inst + b);
+    hv_item<T, R, false>(inst, b, i, u, y, scal[(int64_t)i * kScal + kS], part_out, smem_raw);
+}
+
 // u_next = y - c_cur u_k - c_prev u_prev, written to un (which is u_prev
 // itself when only two Krylov vectors are kept, a new basis slot otherwise),
 // partial ||u_next||^2, in 16-byte vectors over the CTA's rows (padding is
 // zero in all three inputs, so it stays zero).  With ritz_coef, also
 // out += ritz_coef[i][k] s_k u_k (the Ritz vector sum_k y_k q_k of a replay).
-template <typename T>
-__global__ void __launch_bounds__(kBatchThreads) batch_update_kernel(const BatchInst *__restrict__ inst,
-                                                                     const int32_t *__restrict__ blk_inst,
-                                                                     const T *__restrict__ y, const T *__restrict__ u,
-                                                                     const T *up, T *un, const double *__restrict__ scal,
-                                                                     double *__restrict__ part_nrm,
-                                                                     const double *__restrict__ ritz_coef,
-                                                                     T *__restrict__ ritz_out, int k, int nsteps)
+template <typename T, bool COH>
+__device__ __forceinline__ void update_item(const BatchInst &a, int64_t b, T cc, T cp, T cr,
+                                            const T *__restrict__ y, const T *__restrict__ u, const T *up, T *un,
+                                            double *__restrict__ part_nrm, T *__restrict__ ritz_out)
 {
     using V = typename V16<T>::type;
     constexpr int VN = V16<T>::n;
-    const int64_t b = blockIdx.x;
-    const int i = __ldg(blk_inst + b);
-    const BatchInst &a = inst[i];
-    const double *sc = scal + (int64_t)i * kScal;
-    const T cc = (T)sc[kCCur], cp = (T)sc[kCPrev];
-    const T cr = ritz_coef ? (T)(ritz_coef[(int64_t)i * nsteps + k] * sc[kS]) : (T)0;
     const int64_t r0 = (b - a.blk0) * a.rows;
     const int nr = (int)min((int64_t)a.rows, a.nsdn - r0);
     const int64_t base = a.off + r0 * a.ld;
@@ -406,8 +446,10 @@ __global__ void __launch_bounds__(kBatchThreads) batch_update_kernel(const Batch
     V *ov = ritz_out ? reinterpret_cast<V *>(ritz_out + base) : nullptr;
     T sp = 0;
     for (int q = threadIdx.x; q < nv; q += blockDim.x) {
-        const V yy = __ldg(yv + q), uk = __ldg(uv + q);
-        V pp = pv[q];
+        const V yy = ld_data<COH>(yv + q), uk = ld_data<COH>(uv + q);
+        V pp;
+        if constexpr (COH) pp = __ldcg(pv + q);
+        else pp = pv[q];
         V nv_;
 #pragma unroll
         for (int e = 0; e < VN; ++e) {
@@ -425,6 +467,203 @@ __global__ void __launch_bounds__(kBatchThreads) batch_update_kernel(const Batch
         }
     }
     block_partial((double)sp, part_nrm + b);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBatchThreads) batch_update_kernel(const BatchInst *__restrict__ inst,
+                                                                     const int32_t *__restrict__ blk_inst,
+                                                                     const T *__restrict__ y, const T *__restrict__ u,
+                                                                     const T *up, T *un, const double *__restrict__ scal,
+                                                                     double *__restrict__ part_nrm,
+                                                                     const double *__restrict__ ritz_coef,
+                                                                     T *__restrict__ ritz_out, int k, int nsteps)
+{
+    const int64_t b = blockIdx.x;
+    const int i = __ldg(blk_inst + b);
+    const BatchInst &a = inst[i];
+    const double *sc = scal + (int64_t)i * kScal;
+    const T cc = (T)sc[kCCur], cp = (T)sc[kCPrev];
+    const T cr = ritz_coef ? (T)(ritz_coef[(int64_t)i * nsteps + k] * sc[kS]) : (T)0;
+    update_item<T, false>(a, b, cc, cp, cr, y, u, up, un, part_nrm, ritz_out);
+}
+
+// ---------------------------------------------------------------- persistent run
+//
+// One cooperative launch runs every step of every instance.  The work is a
+// list of items (phase, CTA-block of an instance); per instance the phases
+// are 0 (copy of x0 and its norm), then for step k: 2k+1 (H*v) and 2k+2
+// (update).  The instances are split into two groups whose phases are offset
+// by one, and the items of a "super-phase" interleave the two groups' blocks,
+// so the H*v of one group (bound by the L1/shared-memory pipe) runs beside
+// the update of the other (bound by HBM).  CTA c takes items c, c+G, ... in
+// order.  An item waits until its instance has finished the previous phase
+// (done[i] >= p; every such item comes earlier in the list, so with all CTAs
+// resident the run cannot deadlock); its CTA then arrives on the instance's
+// counter, and the last CTA to arrive forms the instance's scalars exactly as
+// batch_scalar_kernel does (same partials, same summation order: alpha/beta
+// are bit-identical to the four-launch form) and publishes done[i] = p + 1.
+// Every wait gives up after kWaitNs of GPU time: it sets status[0] and the
+// whole grid returns.
+struct PersistArgs {
+    const BatchInst *inst;
+    const int32_t *blk_inst;
+    const int32_t *order;     // [nblocks]: the blocks of a super-phase, the two groups interleaved
+    const int8_t *grp;        // [ninst]: 0 or 1 (phase offset)
+    int ninst;
+    int64_t nblocks;
+    int nsteps;
+    int64_t total;            // elements of one concatenated vector (the kept basis's slot stride)
+    int *cnt;                 // [ninst] arrivals
+    int *done;                // [ninst] phases completed
+    int *status;              // [1] 0 = ok
+    double *scal, *pa, *pb, *alpha, *beta;
+};
+
+constexpr unsigned long long kWaitNs = 10ull * 1000000000ull;   // 10 s: far above any phase of one instance
+
+__device__ __forceinline__ unsigned long long gtimer()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ int ld_acquire(const int *p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release(int *p, int v)
+{
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Thread 0 waits for done[i] >= p (bounded); the CTA learns the outcome.
+__device__ __forceinline__ bool wait_phase(const PersistArgs &P, int i, int p, int *flag)
+{
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        if (ld_acquire(P.done + i) < p) {
+            const unsigned long long t0 = gtimer();
+            unsigned ns = 32;
+            while (ld_acquire(P.done + i) < p) {
+                if (ld_acquire(P.status) != 0) { ok = 0; break; }
+                if (gtimer() - t0 > kWaitNs) {
+                    atomicCAS(P.status, 0, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(ns);
+                if (ns < 1024) ns *= 2;
+            }
+        }
+        *flag = ok;
+    }
+    __syncthreads();
+    const bool ok = *flag != 0;
+    __syncthreads();
+    return ok;
+}
+
+// After the CTA's partial is written: count the arrival; the last CTA of the
+// instance forms the scalars of phase p (mode 0 after a norm or update
+// phase, 1 after an H*v phase) and publishes done[i] = p + 1.
+__device__ __forceinline__ void arrive(const PersistArgs &P, const BatchInst &a, int i, int p, int *flag)
+{
+    __syncthreads();   // the partial (thread 0) and all data stores of the CTA are issued
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const int old = atomicAdd(P.cnt + i, 1);
+        *flag = (old == (p + 1) * a.nblk - 1) ? 1 : 0;
+        if (*flag) __threadfence();
+    }
+    __syncthreads();
+    if (*flag && threadIdx.x < 32) {
+        const bool upd = (p % 2) == 0;
+        const double *part = upd ? P.pb : P.pa;
+        double s = 0.0;
+        for (int q = threadIdx.x; q < a.nblk; q += 32) s += __ldcg(part + a.blk0 + q);
+        s = warp_sum(s);
+        if (threadIdx.x == 0) {
+            double *sc = P.scal + (int64_t)i * kScal;
+            const int nsteps = P.nsteps;
+            if (upd) {
+                const int k = p / 2;
+                const double bk = sqrt(fmax(s, 0.0));
+                sc[kSPrev] = (k == 0) ? 0.0 : __ldcg(sc + kS);
+                sc[kS] = (bk > 1e-150) ? 1.0 / bk : 0.0;
+                sc[kBeta] = bk;
+                P.beta[(int64_t)i * (nsteps + 1) + k] = bk;
+            } else {
+                const int k = (p - 1) / 2;
+                const double sk = __ldcg(sc + kS);
+                const double al = sk * s;
+                P.alpha[(int64_t)i * nsteps + k] = al;
+                sc[kCCur] = al * sk;
+                sc[kCPrev] = __ldcg(sc + kBeta) * __ldcg(sc + kSPrev);
+            }
+            __threadfence();
+            st_release(P.done + i, p + 1);
+        }
+    }
+    __syncthreads();
+}
+
+template <typename T, int R>
+__global__ void __launch_bounds__(kBatchThreads, 4) batch_persistent_kernel(const PersistArgs P, const T *__restrict__ x0,
+                                                                         T *U0, T *U1, T *Y, T *kept)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int flag;
+    const int64_t tot_items = (int64_t)(2 * P.nsteps + 2) * P.nblocks;
+    for (int64_t id = blockIdx.x; id < tot_items; id += gridDim.x) {
+        if (threadIdx.x == 0) flag = ld_acquire(P.status);
+        __syncthreads();
+        if (flag != 0) return;   // every thread of the CTA saw the same value
+        __syncthreads();
+        const int64_t s = id / P.nblocks;
+        const int64_t b = __ldg(P.order + (id - s * P.nblocks));
+        const int i = __ldg(P.blk_inst + b);
+        const int p = (int)s - (int)__ldg(P.grp + i);
+        if (p < 0 || p > 2 * P.nsteps) continue;
+        const BatchInst &a = P.inst[i];
+        if (p == 0) {
+            // u_0 = x0 on the block's rows (and u_{-1} = 0 without a kept basis), partial ||x0||^2
+            const int64_t r0 = (b - a.blk0) * a.rows;
+            const int nr = (int)min((int64_t)a.rows, a.nsdn - r0);
+            const int64_t base = a.off + r0 * a.ld, n = (int64_t)nr * a.ld;
+            T *u0 = kept ? kept : U0;
+            for (int64_t q = threadIdx.x; q < n; q += blockDim.x) {
+                u0[base + q] = x0[base + q];
+                if (!kept) U1[base + q] = (T)0;
+            }
+            double sn = 0.0;
+            for (int r = 0; r < nr; ++r) {
+                const T *row = x0 + a.off + (r0 + r) * a.ld;
+                for (int64_t c = threadIdx.x; c < a.nsup; c += blockDim.x) sn += (double)row[c] * (double)row[c];
+            }
+            block_partial(sn, P.pb + b);
+            arrive(P, a, i, 0, &flag);
+            continue;
+        }
+        if (!wait_phase(P, i, p, &flag)) return;
+        // with a kept basis u_k is slot k (slot k-1 its predecessor, slot k+1 the next);
+        // else u_k lives in U[k % 2] and u_{k+1} overwrites u_{k-1}
+        const int k = (p - 1) / 2;
+        const T *uk = kept ? kept + (int64_t)k * P.total : ((k & 1) ? U1 : U0);
+        if (p % 2 == 1) {
+            hv_item<T, R, true>(P.inst, b, i, uk, Y, __ldcg(P.scal + (int64_t)i * kScal + kS), P.pa, smem_raw);
+        } else {
+            const T *uprev = kept ? kept + (int64_t)(k > 0 ? k - 1 : 0) * P.total : ((k & 1) ? U0 : U1);
+            T *unext = kept ? kept + (int64_t)(k + 1) * P.total : ((k & 1) ? U0 : U1);
+            const double *sc = P.scal + (int64_t)i * kScal;
+            update_item<T, true>(a, b, (T)__ldcg(sc + kCCur), (T)__ldcg(sc + kCPrev), (T)0, Y, uk, uprev, unext,
+                                 P.pb, nullptr);
+        }
+        arrive(P, a, i, p, &flag);
+    }
 }
 
 // Ritz vectors from a kept basis: out_i = sum_k coef[i][k] s_k u_k over the
@@ -635,7 +874,26 @@ extern "C" int ed_batch_create_rows(int ninst, ed_sector *const *secs, int rows,
     bt->max_nsup = max_nsup;
     bt->max_ld = max_ld;
     // one allocation per table: creating a batch of thousands of instances costs a few copies
+    // persistent run: instances alternate between two groups whose phases are one apart; the
+    // blocks of a super-phase interleave the groups in proportion to their sizes
+    std::vector<int8_t> grp((size_t)ninst);
+    for (int i = 0; i < ninst; ++i) grp[(size_t)i] = (int8_t)(i & 1);
+    std::vector<int32_t> order;
+    {
+        std::vector<int32_t> g0, g1;
+        for (int64_t b = 0; b < blk; ++b) (grp[(size_t)binst[(size_t)b]] ? g1 : g0).push_back((int32_t)b);
+        order.reserve((size_t)blk);
+        size_t a0 = 0, a1 = 0;
+        while (a0 < g0.size() || a1 < g1.size()) {
+            // take from the group that is behind its share
+            const bool take0 = a1 >= g1.size() ||
+                               (a0 < g0.size() && (double)a0 * (double)g1.size() <= (double)a1 * (double)g0.size());
+            order.push_back(take0 ? g0[a0++] : g1[a1++]);
+        }
+    }
     if (cudaMalloc(&bt->dev, sizeof(BatchInst) * ninst) != cudaSuccess ||
+        cudaMalloc(&bt->grp, (size_t)ninst) != cudaSuccess ||
+        (blk > 0 && cudaMalloc(&bt->order, sizeof(int32_t) * (size_t)blk) != cudaSuccess) ||
         cudaMalloc(&bt->u_site_all, sizeof(double) * usite.size()) != cudaSuccess ||
         cudaMalloc(&bt->u_site_all32, sizeof(float) * usite32.size()) != cudaSuccess ||
         (blk > 0 && cudaMalloc(&bt->blk_inst, sizeof(int32_t) * (size_t)blk) != cudaSuccess)) {
@@ -659,6 +917,9 @@ extern "C" int ed_batch_create_rows(int ninst, ed_sector *const *secs, int rows,
         cudaMemcpy(bt->u_site_all32, usite32.data(), sizeof(float) * usite32.size(), cudaMemcpyHostToDevice) !=
             cudaSuccess ||
         (blk > 0 && cudaMemcpy(bt->blk_inst, binst.data(), sizeof(int32_t) * (size_t)blk, cudaMemcpyHostToDevice) !=
+                        cudaSuccess) ||
+        cudaMemcpy(bt->grp, grp.data(), (size_t)ninst, cudaMemcpyHostToDevice) != cudaSuccess ||
+        (blk > 0 && cudaMemcpy(bt->order, order.data(), sizeof(int32_t) * (size_t)blk, cudaMemcpyHostToDevice) !=
                         cudaSuccess)) {
         const cudaError_t e = cudaGetLastError();
         set_error("upload of batch descriptors failed: %s", cudaGetErrorString(e));
@@ -683,6 +944,8 @@ extern "C" int ed_batch_destroy(ed_batch *bt)
     if (bt->blk_inst) cudaFree(bt->blk_inst);
     if (bt->u_site_all) cudaFree(bt->u_site_all);
     if (bt->u_site_all32) cudaFree(bt->u_site_all32);
+    if (bt->order) cudaFree(bt->order);
+    if (bt->grp) cudaFree(bt->grp);
     delete bt;
     return ED_OK;
 }
@@ -703,7 +966,10 @@ extern "C" int ed_batch_layout(const ed_batch *bt, int64_t *total, int64_t *offs
 extern "C" int64_t ed_batch_scratch_bytes(const ed_batch *bt)
 {
     if (!bt) return -1;
-    return (2 * bt->nblocks + (int64_t)kScal * bt->ninst) * (int64_t)sizeof(double) + 256;
+    // partials and per-instance scalars (FP64), then the persistent run's counters, phase
+    // flags and status (int32)
+    return (2 * bt->nblocks + (int64_t)kScal * bt->ninst) * (int64_t)sizeof(double) +
+           (2 * (int64_t)bt->ninst + 1) * (int64_t)sizeof(int) + 512;
 }
 
 static int batch_launch(ed_batch *bt, void *stream, int dtype, void *work, const void *x0, int nsteps, double *alpha,
@@ -808,6 +1074,105 @@ extern "C" int ed_batch_hv(ed_batch *bt, void *stream, int dtype, const void *x,
         else batch_hv_kernel<double, 8><<<nb, kBatchThreads, smem, st>>>(bt->dev, bt->blk_inst, xx, yy, scal, pa);
     }
     ED_CHECK_LAUNCH();
+    return ED_OK;
+}
+
+namespace ed {
+// Where the persistent run keeps its counters in the caller's scratch: after
+// the FP64 partials and scalars, 16-byte aligned.
+static int *persist_ints(const ed_batch *bt, void *scratch)
+{
+    const size_t off = (size_t)(2 * bt->nblocks + (int64_t)kScal * bt->ninst) * sizeof(double);
+    return reinterpret_cast<int *>(static_cast<unsigned char *>(scratch) + (off + 15) / 16 * 16);
+}
+
+template <typename T, int R>
+static int run_persistent(ed_batch *bt, cudaStream_t st, T *work, const T *x0, int nsteps, double *alpha,
+                          double *beta, double *scratch, T *kept)
+{
+    const int64_t tot = bt->total;
+    PersistArgs P;
+    P.inst = bt->dev;
+    P.blk_inst = bt->blk_inst;
+    P.order = bt->order;
+    P.grp = bt->grp;
+    P.ninst = bt->ninst;
+    P.nblocks = bt->nblocks;
+    P.nsteps = nsteps;
+    P.total = tot;
+    P.pa = scratch;
+    P.pb = scratch + bt->nblocks;
+    P.scal = scratch + 2 * bt->nblocks;
+    int *ints = persist_ints(bt, scratch);
+    P.cnt = ints;
+    P.done = ints + bt->ninst;
+    P.status = ints + 2 * bt->ninst;
+    P.alpha = alpha;
+    P.beta = beta;
+    ED_CHECK_CUDA(cudaMemsetAsync(ints, 0, sizeof(int) * (2 * (size_t)bt->ninst + 1), st));
+    if (bt->nblocks == 0) return ED_OK;
+    const size_t smem = (size_t)bt->max_ld * staged_stride<T, R>() * sizeof(T);
+    auto kfn = batch_persistent_kernel<T, R>;
+    ED_CHECK_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    ED_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, kBatchThreads, smem));
+    if (per_sm < 1) {
+        set_error("the persistent batched kernel does not fit on an SM");
+        return ED_ERR_RANGE;
+    }
+    int64_t grid = (int64_t)per_sm * num_sms();
+    const int64_t items = (int64_t)(2 * nsteps + 2) * bt->nblocks;
+    if (grid > items) grid = items;
+    T *U0 = kept ? nullptr : work, *U1 = kept ? nullptr : work + tot;
+    T *Y = kept ? work : work + 2 * tot;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kBatchThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;   // every CTA resident at once: the waits rely on it
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    ED_CHECK_CUDA(cudaLaunchKernelEx(&cfg, kfn, P, x0, U0, U1, Y, kept));
+    return ED_OK;
+}
+}  // namespace ed
+
+extern "C" int ed_batch_lanczos_persistent(ed_batch *bt, void *stream, int dtype, void *work, const void *x0,
+                                           int nsteps, double *alpha, double *beta, void *kept, void *scratch,
+                                           int64_t scratch_bytes)
+{
+    clear_error();
+    ED_REQUIRE(bt != nullptr && work != nullptr && x0 != nullptr && alpha != nullptr && beta != nullptr,
+               "NULL argument");
+    ED_REQUIRE(dtype == ED_F32 || dtype == ED_F64, "dtype must be ED_F32 or ED_F64");
+    ED_REQUIRE(nsteps >= 1, "nsteps must be positive");
+    ED_REQUIRE(scratch != nullptr && scratch_bytes >= ed_batch_scratch_bytes(bt), "scratch of %lld bytes is below %lld",
+               (long long)scratch_bytes, (long long)ed_batch_scratch_bytes(bt));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    double *sc = static_cast<double *>(scratch);
+    if (dtype == ED_F32) {
+        float *w = (float *)work, *kp = (float *)kept;
+        const float *x = (const float *)x0;
+        if (bt->rows == 4) return run_persistent<float, 4>(bt, st, w, x, nsteps, alpha, beta, sc, kp);
+        if (bt->rows == 16) return run_persistent<float, 16>(bt, st, w, x, nsteps, alpha, beta, sc, kp);
+        return run_persistent<float, 8>(bt, st, w, x, nsteps, alpha, beta, sc, kp);
+    }
+    double *w = (double *)work, *kp = (double *)kept;
+    const double *x = (const double *)x0;
+    if (bt->rows == 4) return run_persistent<double, 4>(bt, st, w, x, nsteps, alpha, beta, sc, kp);
+    if (bt->rows == 16) return run_persistent<double, 16>(bt, st, w, x, nsteps, alpha, beta, sc, kp);
+    return run_persistent<double, 8>(bt, st, w, x, nsteps, alpha, beta, sc, kp);
+}
+
+extern "C" int ed_batch_persistent_status(const ed_batch *bt, const void *scratch, int *status)
+{
+    clear_error();
+    ED_REQUIRE(bt != nullptr && scratch != nullptr && status != nullptr, "NULL argument");
+    const int *ints = persist_ints(bt, const_cast<void *>(scratch));
+    ED_CHECK_CUDA(cudaMemcpy(status, ints + 2 * bt->ninst, sizeof(int), cudaMemcpyDeviceToHost));
     return ED_OK;
 }
 

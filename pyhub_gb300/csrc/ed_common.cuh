@@ -79,6 +79,12 @@ struct HopTable {
     // appends) with coefficient +ell_mag.  ell_mag = 0: no such table.
     uint16_t *ell_s16 = nullptr;   // [ell_slots*32]
     float ell_mag = 0.0f;
+    // Per ordered site pair (J,K), J != K, at index (J-1)*norb + (K-1): the
+    // strings u with J occupied and K empty, as {u, u' | sign << 31} with
+    // u' = u - J + K and sign = parity of the occupied sites strictly between
+    // J and K (the reduced-density kernels walk only the hops that exist).
+    int32_t *pl_off = nullptr;     // [norb*norb + 1]
+    int2 *pl_ent = nullptr;
     bool owner = true;
 };
 

@@ -407,6 +407,37 @@ static int upload_ell(const HostHop &h, HopTable &d, TablePool &pool)
     return ED_OK;
 }
 
+// Pair lists of one spin species (HopTable::pl_off / pl_ent), for every
+// ordered pair J != K regardless of T(J,K): the reduced densities need them all.
+static int upload_pairs(const HostHop &h, int norb, HopTable &d, TablePool &pool)
+{
+    const int64_t n = (int64_t)h.str.size();
+    std::unordered_map<uint32_t, int32_t> index;
+    index.reserve((size_t)n * 2);
+    for (int64_t i = 0; i < n; ++i) index[h.str[(size_t)i]] = (int32_t)i;
+    std::vector<int32_t> off((size_t)norb * norb + 1, 0);
+    std::vector<int2> ent;
+    for (int J = 1; J <= norb; ++J)
+        for (int K = 1; K <= norb; ++K) {
+            const size_t pid = (size_t)(J - 1) * norb + (K - 1);
+            off[pid] = (int32_t)ent.size();
+            if (J == K) continue;
+            const uint32_t bj = site_bit(norb, J), bk = site_bit(norb, K), btw = between_mask(norb, J, K);
+            for (int64_t u = 0; u < n; ++u) {
+                const uint32_t su = h.str[(size_t)u];
+                if (!(su & bj) || (su & bk)) continue;
+                const int32_t u2 = index[su - bj + bk];
+                const uint32_t sg = (uint32_t)(__builtin_popcount(su & btw) & 1);
+                ent.push_back(make_int2((int32_t)u, (int32_t)((uint32_t)u2 | (sg << 31))));
+            }
+            if (ent.size() > (size_t)INT32_MAX) return ED_ERR_RANGE;
+        }
+    off[(size_t)norb * norb] = (int32_t)ent.size();
+    pool.add(&d.pl_off, off.data(), off.size());
+    pool.add(&d.pl_ent, ent.data(), ent.size());
+    return ED_OK;
+}
+
 // Host side of a hop table: pointers are set when the pool is committed.
 static int upload_hop(const HostHop &h, int norb, int ne, HopTable &d, TablePool &pool)
 {
@@ -424,6 +455,8 @@ static int upload_hop(const HostHop &h, int norb, int ne, HopTable &d, TablePool
     pool.add(&d.ediag, h.ediag.data(), h.ediag.size());
     pool.add(&d.ediag32, e32.data(), e32.size());
     d.owner = true;
+    const int rc = upload_pairs(h, norb, d, pool);
+    if (rc) return rc;
     return upload_ell(h, d, pool);
 }
 

@@ -291,3 +291,64 @@ def test_batch_hv_matches_oracle(edlib, rows):
                     assert np.array_equal(got, ref), (i, dt)
                 else:
                     assert np.linalg.norm(got - ref) <= 1e-14 * np.linalg.norm(ref), i
+
+
+@pytest.mark.parametrize("dtype,keep,rows", [("f64", False, 8), ("f32", False, 8), ("f32", True, 4),
+                                              ("f64", True, 16), ("f32", False, 16)])
+def test_persistent_run_is_bit_identical(edlib, dtype, keep, rows):
+    """The one-launch persistent run gives the four-launch run's alpha/beta
+    bit for bit (same partials, same summation order), keeps the same Krylov
+    vectors, reports status 0, and replays identically from a CUDA graph."""
+    import torch
+    from pyhub_gb300.core import greens_batched as GB
+    t, U, src, gs, secs, inst, _ = _setup(edlib, nsteps=25, dtype=dtype)
+    td = torch.float64 if dtype == "f64" else torch.float32
+    ref = GB.BatchedLanczos(secs, 25, dtype=td, rows=rows, keep=keep)
+    per = GB.BatchedLanczos(secs, 25, dtype=td, rows=rows, keep=keep, persistent=True)
+    x0 = torch.rand(ref.batch.total, dtype=td, device="cuda")
+    for i, s in enumerate(secs):      # zero row padding, as every engine vector has
+        ref.batch.view(x0, i).view(s.nsdn, -1)[:, s.nsup:] = 0
+    ref.x0.copy_(x0)
+    per.x0.copy_(x0)
+    ref.run()
+    per.run()
+    torch.cuda.synchronize()
+    assert per.batch.persistent_status(per.scratch) == 0
+    assert torch.equal(ref.alpha, per.alpha) and torch.equal(ref.beta, per.beta)
+    if keep:
+        assert torch.equal(ref.basis, per.basis)
+    a0, b0 = per.alpha.clone(), per.beta.clone()
+    per.alpha.zero_()
+    per.beta.zero_()
+    per.capture()
+    per.replay()
+    torch.cuda.synchronize()
+    assert per.batch.persistent_status(per.scratch) == 0
+    assert torch.equal(per.alpha, a0) and torch.equal(per.beta, b0)
+
+
+def test_persistent_run_full_size_clusters(edlib):
+    """Two C4 clusters' particle/hole instances (sectors of 392,040 to
+    853,776 elements, mixed shapes): persistent and four-launch runs agree
+    bit for bit over 40 FP32 steps."""
+    import torch
+    from pyhub_gb300 import _capi
+    from pyhub_gb300.core import greens_batched as GB
+    secs = []
+    for spec in GB.c4_clusters(2, seed=3):
+        N = spec["N"]
+        for key in [(N + 1, N), (N - 1, N), (N, N + 1), (N, N - 1)]:
+            s = _capi.Sector(12, key[0], key[1], _capi.ED_HUBBARD, t=spec["t"], U=np.full(12, spec["U"]))
+            secs += [s] * 3
+    ref = GB.BatchedLanczos(secs, 40, dtype=torch.float32, rows=8)
+    per = GB.BatchedLanczos(secs, 40, dtype=torch.float32, rows=8, persistent=True)
+    x0 = torch.rand(ref.batch.total, dtype=torch.float32, device="cuda")
+    for i, s in enumerate(secs):
+        ref.batch.view(x0, i).view(s.nsdn, -1)[:, s.nsup:] = 0
+    ref.x0.copy_(x0)
+    per.x0.copy_(x0)
+    ref.run()
+    per.run()
+    torch.cuda.synchronize()
+    assert per.batch.persistent_status(per.scratch) == 0
+    assert torch.equal(ref.alpha, per.alpha) and torch.equal(ref.beta, per.beta)

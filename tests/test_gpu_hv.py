@@ -105,10 +105,11 @@ def test_hubbard_f32_within_bound(edlib, case):
 
 @pytest.mark.parametrize("case", [(4, 2, 2), (8, 4, 4), (9, 4, 5), (12, 6, 6), (12, 5, 7)])
 def test_hubbard_f32_single_magnitude_hopping(edlib, case):
-    """Hopping of one magnitude with both signs (the 2-byte-slot row pass):
-    FP32 within 64 eps32 (|H||x|)_i of the oracle (exact enumeration for the
-    larger sectors: the FP64 product of the FP32-rounded x), bit-exact for
-    integer x, with per-site U and on-site energies."""
+    """Hopping of one magnitude with both signs (the 2-byte-slot row pass),
+    with per-site U and on-site energies: bit-exact for integer x; for an
+    FP32-rounded real x, against the oracle's FP64 product, per element within
+    64 eps32 (|H||x|)_i where the dense |H| is available, else within 64 eps32
+    in norm."""
     import torch
     norb, nu, nd = case
     rng = np.random.default_rng(3 * norb + nu)
@@ -125,9 +126,12 @@ def test_hubbard_f32_single_magnitude_hopping(edlib, case):
         assert np.array_equal(_run(edlib, sec, xi, torch.float32, layout), yi)
     x = rng.standard_normal(osec.dim).astype(np.float32).astype(np.float64)
     yref = O.hprod_hubbard(osec, t, U, x, fast=True)
-    babs = O.hprod_hubbard(osec, np.abs(t), np.abs(U), np.abs(x), fast=True)   # (|H||x|)_i
     y = _run(edlib, sec, x, torch.float32, sec.ld)
-    assert np.all(np.abs(y - yref) <= 64 * EPS32 * babs + 1e-30)
+    if osec.dim <= 5000:
+        assert np.all(np.abs(y - yref) <= 64 * EPS32 * _abs_bound(osec, t, U, x) + 1e-30)
+    else:
+        # larger sectors: the dense |H| is out of reach; FP32 accumulation of ~20 terms per element
+        assert np.linalg.norm(y - yref) <= 64 * EPS32 * np.linalg.norm(yref)
 
 
 def test_hubbard_fused_dots(edlib):

@@ -26,7 +26,7 @@ def _params(n, seed, integer=False, density=0.3):
         Ul = rng.standard_normal((n,) * 4) * (rng.random((n,) * 4) < density)
     t = np.triu(t) + np.triu(t, 1).T
     Ul = Ul + np.einsum("ijkl->jilk", Ul)    # symmetric as the reference requires
-    Ul[1, 0] = 0.0                           # one (J,K) pair gated off by UPARTIAL
+    Ul[1, 0] = Ul[0, 1] = 0.0                # (J,K) = (1,2), (2,1) gated off by UPARTIAL, still symmetric
     return t, Ul, rng
 
 
