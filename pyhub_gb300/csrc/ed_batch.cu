@@ -495,15 +495,15 @@ __global__ void __launch_bounds__(kBatchThreads) batch_update_kernel(const Batch
 // (update).  The instances are split into two groups whose phases are offset
 // by one, and the items of a "super-phase" interleave the two groups' blocks,
 // so the H*v of one group (bound by the L1/shared-memory pipe) runs beside
-// the update of the other (bound by HBM).  CTA c takes items c, c+G, ... in
-// order.  An item waits until its instance has finished the previous phase
+// the update of the other (bound by HBM).  An item waits until its instance has finished the previous phase
 // (done[i] >= p; every such item comes earlier in the list, so with all CTAs
 // resident the run cannot deadlock); its CTA then arrives on the instance's
 // counter, and the last CTA to arrive forms the instance's scalars exactly as
 // batch_scalar_kernel does (same partials, same summation order: alpha/beta
 // are bit-identical to the four-launch form) and publishes done[i] = p + 1.
 // Every wait gives up after kWaitNs of GPU time: it sets status[0] and the
-// whole grid returns.
+// whole grid returns.  CTAs claim items from a queue in list order, so a CTA
+// waits only on items already claimed by running CTAs.
 struct PersistArgs {
     const BatchInst *inst;
     const int32_t *blk_inst;
@@ -516,10 +516,12 @@ struct PersistArgs {
     int *cnt;                 // [ninst] arrivals
     int *done;                // [ninst] phases completed
     int *status;              // [1] 0 = ok
+    unsigned long long *queue;   // next unclaimed item
     double *scal, *pa, *pb, *alpha, *beta;
 };
 
 constexpr unsigned long long kWaitNs = 10ull * 1000000000ull;   // 10 s: far above any phase of one instance
+constexpr int kPersistChunk = 4;   // items claimed at once
 
 __device__ __forceinline__ unsigned long long gtimer()
 {
@@ -617,12 +619,21 @@ __global__ void __launch_bounds__(kBatchThreads, 4) batch_persistent_kernel(cons
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int flag;
+    __shared__ long long s_base;
     const int64_t tot_items = (int64_t)(2 * P.nsteps + 2) * P.nblocks;
-    for (int64_t id = blockIdx.x; id < tot_items; id += gridDim.x) {
-        if (threadIdx.x == 0) flag = ld_acquire(P.status);
+    // items are claimed from a queue, kPersistChunk at a time, in list order: a CTA that drew
+    // cheap update items takes more of them instead of waiting behind the H*v items
+    for (;;) {
+        if (threadIdx.x == 0) {
+            flag = ld_acquire(P.status);
+            s_base = (long long)atomicAdd(P.queue, (unsigned long long)kPersistChunk);
+        }
         __syncthreads();
-        if (flag != 0) return;   // every thread of the CTA saw the same value
+        const int64_t base = s_base;
+        if (flag != 0 || base >= tot_items) return;   // every thread of the CTA saw the same values
         __syncthreads();
+        const int64_t id_end = min(base + (int64_t)kPersistChunk, tot_items);
+    for (int64_t id = base; id < id_end; ++id) {
         const int64_t s = id / P.nblocks;
         const int64_t b = __ldg(P.order + (id - s * P.nblocks));
         const int i = __ldg(P.blk_inst + b);
@@ -663,6 +674,7 @@ __global__ void __launch_bounds__(kBatchThreads, 4) batch_persistent_kernel(cons
                                  P.pb, nullptr);
         }
         arrive(P, a, i, p, &flag);
+    }
     }
 }
 
@@ -969,7 +981,7 @@ extern "C" int64_t ed_batch_scratch_bytes(const ed_batch *bt)
     // partials and per-instance scalars (FP64), then the persistent run's counters, phase
     // flags and status (int32)
     return (2 * bt->nblocks + (int64_t)kScal * bt->ninst) * (int64_t)sizeof(double) +
-           (2 * (int64_t)bt->ninst + 1) * (int64_t)sizeof(int) + 512;
+           (2 * (int64_t)bt->ninst + 4) * (int64_t)sizeof(int) + 512;
 }
 
 static int batch_launch(ed_batch *bt, void *stream, int dtype, void *work, const void *x0, int nsteps, double *alpha,
@@ -1107,9 +1119,10 @@ static int run_persistent(ed_batch *bt, cudaStream_t st, T *work, const T *x0, i
     P.cnt = ints;
     P.done = ints + bt->ninst;
     P.status = ints + 2 * bt->ninst;
+    P.queue = reinterpret_cast<unsigned long long *>(ints + 2 * bt->ninst + 2);   // 8-byte aligned
     P.alpha = alpha;
     P.beta = beta;
-    ED_CHECK_CUDA(cudaMemsetAsync(ints, 0, sizeof(int) * (2 * (size_t)bt->ninst + 1), st));
+    ED_CHECK_CUDA(cudaMemsetAsync(ints, 0, sizeof(int) * (2 * (size_t)bt->ninst + 4), st));
     if (bt->nblocks == 0) return ED_OK;
     const size_t smem = (size_t)bt->max_ld * staged_stride<T, R>() * sizeof(T);
     auto kfn = batch_persistent_kernel<T, R>;

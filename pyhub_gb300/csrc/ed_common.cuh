@@ -72,13 +72,6 @@ struct HopTable {
     float *ell_cf32 = nullptr;
     double *ell_cf64 = nullptr;
     int2 *ell_pk32 = nullptr;      // [ell_slots*32] {src, FP32 coefficient bits}: one 8-byte load per slot
-    // When every hop coefficient has one magnitude (|t| the same on every
-    // bond, as on the usual lattice models) and n < 32767: the same slots as
-    // 2-byte entries, bit 15 the sign of the coefficient, bits 0..14 the
-    // source; padding slots read source n (a zero column the row kernel
-    // appends) with coefficient +ell_mag.  ell_mag = 0: no such table.
-    uint16_t *ell_s16 = nullptr;   // [ell_slots*32]
-    float ell_mag = 0.0f;
     // Per ordered site pair (J,K), J != K, at index (J-1)*norb + (K-1): the
     // strings u with J occupied and K empty, as {u, u' | sign << 31} with
     // u' = u - J + K and sign = parity of the occupied sites strictly between

@@ -17,7 +17,6 @@
 #include "ed_common.cuh"
 
 #include <cstdlib>
-#include <cstring>
 
 namespace ed {
 
@@ -28,8 +27,6 @@ struct HubArgs {
     int64_t nslice;
     const int32_t *ell_off; const int32_t *ell_src;
     const int2 *ell_pk32;
-    const uint16_t *ell_s16;   // 2-byte slots (one coefficient magnitude), or NULL
-    uint32_t mag_bits;         // FP32 bits of that magnitude
     double u_site[kMaxSites];
     float u_site32[kMaxSites];
     int u_uniform;
@@ -240,122 +237,6 @@ __global__ void __launch_bounds__(1024) hub_row_col4_kernel(const float *__restr
     }
 }
 
-// The four-row column kernel with 2-byte hop-table slots (every coefficient
-// +-tau): a slot is the source string in bits 0..14 and the sign of the
-// coefficient in bit 15, so a warp reads one slot with one 64-byte load
-// instead of 256 bytes.  Padding slots read column nsup, which the kernel
-// stages as zeros.  The table comes from L2 (shared memory holds the rows), so
-// the slot loads are software-pipelined: a warp walks the flattened stream of
-// 8-slot groups of its slices and always has the next group's loads in
-// flight while it gathers the current one, across slice boundaries too.
-constexpr int kS16Group = 8;
-
-__device__ __forceinline__ void s16_load(const uint16_t *__restrict__ s16, int64_t at, int n,
-                                         uint32_t (&v)[kS16Group])
-{
-#pragma unroll
-    for (int i = 0; i < kS16Group; ++i) v[i] = (i < n) ? (uint32_t)__ldg(s16 + at + i * 32) : 0u;
-}
-
-template <bool PIPE>
-__global__ void __launch_bounds__(1024) hub_row_col4_s16_kernel(const float *__restrict__ x, float *__restrict__ y,
-                                                                const HubArgs a)
-{
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    float4 *xs4 = reinterpret_cast<float4 *>(smem_raw);   // [nsup + 1], column nsup = 0
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-    const int64_t nsup = a.nsup, ld = a.ld;
-    const float uval = (float)a.u_value, sc = (float)a.scale;
-    const float *ued_t = static_cast<const float *>(a.uediag), *ded_t = static_cast<const float *>(a.dediag);
-    const uint16_t *__restrict__ s16 = a.ell_s16;
-    if (threadIdx.x == 0) xs4[nsup] = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int64_t d0 = (int64_t)blockIdx.x * 4; d0 < a.nsdn; d0 += (int64_t)gridDim.x * 4) {
-        const int nr = (int)min((int64_t)4, a.nsdn - d0);
-        const float *x0 = x + d0 * ld;
-        for (int64_t c = threadIdx.x; c < nsup; c += blockDim.x) {
-            float4 v;
-            v.x = __ldg(x0 + c);
-            v.y = nr > 1 ? __ldg(x0 + ld + c) : 0.f;
-            v.z = nr > 2 ? __ldg(x0 + 2 * ld + c) : 0.f;
-            v.w = nr > 3 ? __ldg(x0 + 3 * ld + c) : 0.f;
-            xs4[c] = v;
-        }
-        uint32_t sd[4];
-        float ed[4];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            sd[r] = (r < nr) ? __ldg(a.dstr + d0 + r) : 0u;
-            ed[r] = (r < nr) ? __ldg(ded_t + d0 + r) : 0.f;
-        }
-        // the first group of the warp's first slice is loaded before the barrier
-        int64_t sl = warp;
-        int s0 = 0, ns = 0;
-        if (sl < a.nslice) {
-            s0 = __ldg(a.ell_off + sl);
-            ns = __ldg(a.ell_off + sl + 1) - s0;
-        }
-        uint32_t cur[kS16Group], nxt[kS16Group];
-        s16_load(s16, (int64_t)s0 * 32 + lane, min(ns, kS16Group), cur);
-        __syncthreads();
-        for (; sl < a.nslice; sl += nwarps) {
-            const int64_t u = sl * 32 + lane;
-            const bool ok = u < nsup;
-            const int64_t uu = ok ? u : nsup - 1;
-            const uint32_t su = __ldg(a.ustr + uu);
-            const float eu = __ldg(ued_t + uu);
-            const float4 xv = xs4[uu];
-            const float xr[4] = {xv.x, xv.y, xv.z, xv.w};
-            float acc[4];
-#pragma unroll
-            for (int r = 0; r < 4; ++r) acc[r] = (eu + ed[r] + u_energy<float>(a, su & sd[r], uval)) * xr[r];
-            // the next slice's offsets, for the prefetch of its first group
-            const int64_t sl2 = sl + nwarps;
-            int s0n = 0, nsn = 0;
-            if (sl2 < a.nslice) {
-                s0n = __ldg(a.ell_off + sl2);
-                nsn = __ldg(a.ell_off + sl2 + 1) - s0n;
-            }
-            for (int k = 0; k < ns; k += kS16Group) {
-                const int nh = min(kS16Group, ns - k);
-                if (!PIPE) s16_load(s16, (int64_t)(s0 + k) * 32 + lane, nh, cur);
-                // prefetch: the slice's next group, else the next slice's first group
-                if (!PIPE) {
-                } else if (k + kS16Group < ns)
-                    s16_load(s16, (int64_t)(s0 + k + kS16Group) * 32 + lane, min(kS16Group, ns - k - kS16Group), nxt);
-                else
-                    s16_load(s16, (int64_t)s0n * 32 + lane, min(kS16Group, nsn), nxt);
-#pragma unroll
-                for (int i = 0; i < kS16Group; ++i) {
-                    if (i < nh) {
-                        const float c = __uint_as_float(a.mag_bits | ((cur[i] & 0x8000u) << 16));
-                        const float4 xq = xs4[cur[i] & 0x7fffu];
-                        acc[0] += c * xq.x;
-                        acc[1] += c * xq.y;
-                        acc[2] += c * xq.z;
-                        acc[3] += c * xq.w;
-                    }
-                }
-                if (PIPE) {
-#pragma unroll
-                    for (int i = 0; i < kS16Group; ++i) cur[i] = nxt[i];
-                }
-            }
-            if (PIPE && ns == 0) {
-                // an empty slice: the prefetch of the next slice's first group still has to happen
-                s16_load(s16, (int64_t)s0n * 32 + lane, min(kS16Group, nsn), cur);
-            }
-            s0 = s0n;
-            ns = nsn;
-            if (ok) {
-#pragma unroll
-                for (int r = 0; r < 4; ++r)
-                    if (r < nr) y[(d0 + r) * ld + u] = acc[r] * sc;
-            }
-        }
-        __syncthreads();
-    }
-}
-
 constexpr int kSlabLoads = 4;   // neighbour-row loads in flight per warp in the slab pass (8 costs occupancy)
 
 // Pass 2: down hops, y[d][slab] += sum_e c_e x[src_e][slab]; optional dots.
@@ -474,181 +355,6 @@ __global__ void __launch_bounds__(256) hub_slab_kernel(const T *__restrict__ x, 
     }
 }
 
-// Pass 2 for FP32 with 16-byte-aligned rows: the same work items, each lane
-// owning 4 consecutive columns (a slab is extended to the row's 4-aligned
-// end; the row padding is zero in x and y, so it stays zero).  Neighbour rows
-// are taken in groups of G loads in flight, and the next group's rows are
-// prefetched into L1 while the current group is loaded and accumulated
-// (no registers held for them).
-template <int G>
-__device__ __forceinline__ void slab_prefetch_group(const float *__restrict__ x, int64_t ld, int64_t c, bool act,
-                                                    int my_src, int e, int nb)
-{
-#pragma unroll
-    for (int i = 0; i < G; ++i) {
-        const int idx = e + i;
-        const int64_t sidx = __shfl_sync(0xffffffffu, my_src, idx & 31);
-        if (idx < nb && act) asm volatile("prefetch.global.L1 [%0];" ::"l"(x + sidx * ld + c));
-    }
-}
-
-template <int G>
-__global__ void __launch_bounds__(256, 1) hub_slab_pipe_kernel(const float *__restrict__ x, float *__restrict__ y,
-                                                            const HubArgs a, int64_t slab_w, int64_t ngroups,
-                                                            int64_t nitems, double *__restrict__ partials)
-{
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const float *__restrict__ cf = static_cast<const float *>(a.dcf);
-    const int64_t ld = a.ld, nsup4 = (a.nsup + 3) / 4 * 4;
-    const float sc = (float)a.scale;
-    double dxy = 0.0, dyy = 0.0;
-    for (int64_t item = blockIdx.x; item < nitems; item += gridDim.x) {
-        const int64_t slab = item / ngroups, g = item - slab * ngroups;
-        const int64_t d = g * 8 + warp;
-        if (d >= a.nsdn) continue;
-        const int64_t c0 = slab * slab_w, c1 = min(c0 + slab_w, nsup4);
-        const int e0 = __ldg(a.dptr + d), nn = __ldg(a.dptr + d + 1) - e0;
-        float *yr = y + d * ld;
-        const float *xd = x + d * ld;
-        float pxy = 0.f, pyy = 0.f;
-        for (int b0 = 0; b0 < max(nn, 1); b0 += 32) {
-            const int nb = max(0, min(32, nn - b0));
-            const int my_src = (lane < nb) ? __ldg(a.dsrc + e0 + b0 + lane) : 0;
-            const float my_cf = (lane < nb) ? __ldg(cf + e0 + b0 + lane) * sc : 0.f;
-            const bool last = (b0 + 32 >= nn);
-            for (int64_t cb = c0; cb < c1; cb += 128) {
-                const int64_t c = cb + (int64_t)lane * 4;
-                const bool act = c < c1;
-                float4 acc = act ? *reinterpret_cast<const float4 *>(yr + c) : make_float4(0.f, 0.f, 0.f, 0.f);
-                slab_prefetch_group<G>(x, ld, c, act, my_src, 0, nb);
-                for (int e = 0; e < nb; e += G) {
-                    if (e + G < nb) slab_prefetch_group<G>(x, ld, c, act, my_src, e + G, nb);
-                    float4 v[G];
-                    float w[G];
-#pragma unroll
-                    for (int i = 0; i < G; ++i) {
-                        const int idx = e + i;
-                        const int64_t sidx = __shfl_sync(0xffffffffu, my_src, idx & 31);
-                        const float wi = __shfl_sync(0xffffffffu, my_cf, idx & 31);
-                        w[i] = (idx < nb) ? wi : 0.f;
-                        v[i] = (idx < nb && act) ? __ldg(reinterpret_cast<const float4 *>(x + sidx * ld + c))
-                                                 : make_float4(0.f, 0.f, 0.f, 0.f);
-                    }
-#pragma unroll
-                    for (int i = 0; i < G; ++i) {
-                        acc.x += w[i] * v[i].x;
-                        acc.y += w[i] * v[i].y;
-                        acc.z += w[i] * v[i].z;
-                        acc.w += w[i] * v[i].w;
-                    }
-                }
-                if (act) {
-                    *reinterpret_cast<float4 *>(yr + c) = acc;
-                    if (partials && last) {
-                        const float4 xv = __ldg(reinterpret_cast<const float4 *>(xd + c));
-                        pxy += xv.x * acc.x + xv.y * acc.y + xv.z * acc.z + xv.w * acc.w;
-                        pyy += acc.x * acc.x + acc.y * acc.y + acc.z * acc.z + acc.w * acc.w;
-                    }
-                }
-            }
-        }
-        dxy += (double)pxy;
-        dyy += (double)pyy;
-    }
-    if (partials) {
-        __shared__ double red[2][8];
-        dxy = warp_sum(dxy);
-        dyy = warp_sum(dyy);
-        if (lane == 0) { red[0][warp] = dxy; red[1][warp] = dyy; }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double sxy = 0.0, syy = 0.0;
-            for (int w = 0; w < 8; ++w) { sxy += red[0][w]; syy += red[1][w]; }
-            partials[2 * blockIdx.x] = sxy;
-            partials[2 * blockIdx.x + 1] = syy;
-        }
-    }
-}
-
-// Pass 2 for FP32, burst form: each lane owns 2 consecutive columns of a
-// 64-column chunk and issues the loads of up to kBurst neighbour rows before
-// the first FMA (twice the bytes in flight per warp of the 4-column form).
-constexpr int kBurst = 16;
-
-__global__ void __launch_bounds__(256) hub_slab_burst_kernel(const float *__restrict__ x, float *__restrict__ y,
-                                                             const HubArgs a, int64_t slab_w, int64_t ngroups,
-                                                             int64_t nitems, double *__restrict__ partials)
-{
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const float *__restrict__ cf = static_cast<const float *>(a.dcf);
-    const int64_t ld = a.ld, nsup2 = (a.nsup + 1) / 2 * 2;
-    const float sc = (float)a.scale;
-    double dxy = 0.0, dyy = 0.0;
-    for (int64_t item = blockIdx.x; item < nitems; item += gridDim.x) {
-        const int64_t slab = item / ngroups, g = item - slab * ngroups;
-        const int64_t d = g * 8 + warp;
-        if (d >= a.nsdn) continue;
-        const int64_t c0 = slab * slab_w, c1 = min(c0 + slab_w, nsup2);
-        const int e0 = __ldg(a.dptr + d), nn = __ldg(a.dptr + d + 1) - e0;
-        float *yr = y + d * ld;
-        const float *xd = x + d * ld;
-        float pxy = 0.f, pyy = 0.f;
-        for (int b0 = 0; b0 < max(nn, 1); b0 += 32) {
-            const int nb = max(0, min(32, nn - b0));
-            const int my_src = (lane < nb) ? __ldg(a.dsrc + e0 + b0 + lane) : 0;
-            const float my_cf = (lane < nb) ? __ldg(cf + e0 + b0 + lane) * sc : 0.f;
-            const bool last = (b0 + 32 >= nn);
-            for (int64_t cb = c0; cb < c1; cb += 64) {
-                const int64_t c = cb + (int64_t)lane * 2;
-                const bool act = c < c1;
-                float2 acc = act ? *reinterpret_cast<const float2 *>(yr + c) : make_float2(0.f, 0.f);
-                for (int e = 0; e < nb; e += kBurst) {
-                    float2 v[kBurst];
-#pragma unroll
-                    for (int i = 0; i < kBurst; ++i) {
-                        const int idx = e + i;
-                        const int64_t sidx = __shfl_sync(0xffffffffu, my_src, idx & 31);
-                        v[i] = (idx < nb && act) ? __ldg(reinterpret_cast<const float2 *>(x + sidx * ld + c))
-                                                 : make_float2(0.f, 0.f);
-                    }
-#pragma unroll
-                    for (int i = 0; i < kBurst; ++i) {
-                        const int idx = e + i;
-                        const float w = __shfl_sync(0xffffffffu, my_cf, idx & 31);
-                        if (idx < nb) {
-                            acc.x += w * v[i].x;
-                            acc.y += w * v[i].y;
-                        }
-                    }
-                }
-                if (act) {
-                    *reinterpret_cast<float2 *>(yr + c) = acc;
-                    if (partials && last) {
-                        const float2 xv = __ldg(reinterpret_cast<const float2 *>(xd + c));
-                        pxy += xv.x * acc.x + xv.y * acc.y;
-                        pyy += acc.x * acc.x + acc.y * acc.y;
-                    }
-                }
-            }
-        }
-        dxy += (double)pxy;
-        dyy += (double)pyy;
-    }
-    if (partials) {
-        __shared__ double red[2][8];
-        dxy = warp_sum(dxy);
-        dyy = warp_sum(dyy);
-        if (lane == 0) { red[0][warp] = dxy; red[1][warp] = dyy; }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double sxy = 0.0, syy = 0.0;
-            for (int w = 0; w < 8; ++w) { sxy += red[0][w]; syy += red[1][w]; }
-            partials[2 * blockIdx.x] = sxy;
-            partials[2 * blockIdx.x + 1] = syy;
-        }
-    }
-}
-
 // Sum nblocks rows of m partials into out[m] (FP64, fixed order).
 __global__ void reduce_partials_kernel(const double *__restrict__ partials, int nblocks, int m,
                                        double *__restrict__ out)
@@ -708,13 +414,6 @@ static int hub_hv(ed_sector *s, cudaStream_t st, int64_t ld, const T *x, T *y, d
     a.ell_off = s->up.ell_off;
     a.ell_src = s->up.ell_src;
     a.ell_pk32 = s->up.ell_pk32;
-    a.ell_s16 = (s->up.ell_mag > 0.0f) ? s->up.ell_s16 : nullptr;
-    {
-        const float m = s->up.ell_mag;
-        uint32_t bits;
-        std::memcpy(&bits, &m, sizeof(bits));
-        a.mag_bits = bits;
-    }
     for (int b = 0; b < kMaxSites; ++b) {
         a.u_site[b] = s->u_site[b];
         a.u_site32[b] = (float)s->u_site[b];
@@ -745,23 +444,7 @@ static int hub_hv(ed_sector *s, cudaStream_t st, int64_t ld, const T *x, T *y, d
     constexpr int R2 = 2;
     const bool two = (size_t)R2 * row_bytes * 2 <= (size_t)maxsm;
     const int threads = 512;
-    static const int use_s16 = []() {
-        const char *e = std::getenv("PYHUB_ED_ROW_S16");
-        return e ? std::atoi(e) : 1;
-    }();
-    if (sizeof(T) == 4 && use_s16 && a.ell_s16 != nullptr && (size_t)(s->nsup + 1) * 16 <= (size_t)maxsm) {
-        // four rows per 1024-thread CTA, 2-byte hop-table slots
-        const size_t smem = (size_t)(s->nsup + 1) * 16;
-        int64_t blocks = (s->nsdn + 3) / 4;
-        if (blocks > nsm) blocks = nsm;
-        static const int row_pipe = []() {
-            const char *e = std::getenv("PYHUB_ED_ROW_PIPE");
-            return e ? std::atoi(e) : 1;
-        }();
-        auto kfn = row_pipe ? hub_row_col4_s16_kernel<true> : hub_row_col4_s16_kernel<false>;
-        ED_CHECK_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        kfn<<<(unsigned)blocks, 1024, smem, st>>>(reinterpret_cast<const float *>(x), reinterpret_cast<float *>(y), a);
-    } else if (sizeof(T) == 4 && (size_t)s->nsup * 16 <= (size_t)maxsm) {
+    if (sizeof(T) == 4 && (size_t)s->nsup * 16 <= (size_t)maxsm) {
         // four rows per 1024-thread CTA, staged as 16-byte columns
         const size_t smem = (size_t)s->nsup * 16;
         int64_t blocks = (s->nsdn + 3) / 4;
@@ -809,11 +492,6 @@ static int hub_hv(ed_sector *s, cudaStream_t st, int64_t ld, const T *x, T *y, d
     else
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hub_slab_kernel<T, 1>, 256, 0);
     if (per_sm < 1) per_sm = 1;
-    static const int old_grid = []() {
-        const char *e = std::getenv("PYHUB_ED_SLAB_OLDGRID");
-        return e ? std::atoi(e) : 0;
-    }();
-    if (old_grid) per_sm = 8;
     int64_t blocks2 = (int64_t)nsm * per_sm;
     if (blocks2 > kMaxPartialBlocks) blocks2 = kMaxPartialBlocks;
     if (blocks2 > nitems) blocks2 = nitems;
@@ -821,24 +499,6 @@ static int hub_hv(ed_sector *s, cudaStream_t st, int64_t ld, const T *x, T *y, d
     const bool vec2 = (ld % VWS == 0) && ((reinterpret_cast<uintptr_t>(x) & 15) == 0) &&
                       ((reinterpret_cast<uintptr_t>(y) & 15) == 0);
     double *part = dots ? partials : nullptr;
-    static const int pipe = []() {
-        const char *e = std::getenv("PYHUB_ED_SLAB_PIPE");
-        return e ? std::atoi(e) : 0;
-    }();
-    if (sizeof(T) == 4 && vec2 && pipe) {
-        auto kfn = (pipe == 2) ? hub_slab_burst_kernel : (pipe == 8) ? hub_slab_pipe_kernel<8> : hub_slab_pipe_kernel<4>;
-        int ps = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ps, kfn, 256, 0);
-        int64_t bp = (int64_t)nsm * (ps < 1 ? 1 : ps);
-        if (bp > kMaxPartialBlocks) bp = kMaxPartialBlocks;
-        if (bp > nitems) bp = nitems;
-        if (bp < 1) bp = 1;
-        kfn<<<(unsigned)bp, 256, 0, st>>>(reinterpret_cast<const float *>(x), reinterpret_cast<float *>(y), a, slab_w,
-                                          ngroups, nitems, part);
-        ED_CHECK_LAUNCH();
-        if (dots) return launch_reduce(partials, (int)bp, 2, dots, st);
-        return ED_OK;
-    }
     if (vec2)
         hub_slab_kernel<T, VWS><<<(unsigned)blocks2, 256, 0, st>>>(x, y, a, slab_w, ngroups, nitems, part);
     else

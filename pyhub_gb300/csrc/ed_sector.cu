@@ -377,28 +377,6 @@ static int upload_ell(const HostHop &h, HopTable &d, TablePool &pool)
     }
     d.nslice = ns;
     d.ell_slots = slots;
-    // one coefficient magnitude (exact in FP32 and FP64) and sources below 2^15 - 1: 2-byte slots
-    double mag = 0.0;
-    bool one_mag = n < 32767;
-    for (size_t q = 0; q < h.coef.size() && one_mag; ++q) {
-        const double a = std::fabs(h.coef[q]);
-        if (mag == 0.0) mag = a;
-        one_mag = (a == mag) && ((double)(float)a == a);
-    }
-    d.ell_mag = 0.0f;
-    if (one_mag && mag > 0.0) {
-        std::vector<uint16_t> s16((size_t)std::max<int64_t>(slots * 32, 1));
-        for (int64_t sl = 0; sl < ns; ++sl)
-            for (int64_t k = off[(size_t)sl]; k < off[(size_t)sl + 1]; ++k)
-                for (int l = 0; l < 32; ++l) {
-                    const size_t at = (size_t)(k * 32 + l);
-                    const int32_t e = o->entry[at];
-                    s16[at] = (e >= 0) ? (uint16_t)(h.src[(size_t)e] | (h.coef[(size_t)e] < 0.0 ? 0x8000 : 0))
-                                       : (uint16_t)n;
-                }
-        d.ell_mag = (float)mag;
-        pool.add(&d.ell_s16, s16.data(), s16.size());
-    }
     pool.add(&d.ell_off, off.data(), off.size());
     pool.add(&d.ell_src, src.data(), src.size());
     pool.add(&d.ell_cf32, c32.data(), c32.size());
