@@ -569,16 +569,16 @@ __device__ __forceinline__ bool wait_phase(const PersistArgs &P, int i, int p, i
     return ok;
 }
 
-// After the CTA's partial is written: count the arrival; the last CTA of the
-// instance forms the scalars of phase p (mode 0 after a norm or update
+// After the CTA's partials are written: count its n arrivals (consecutive
+// items of one instance and phase); the last CTA of the instance forms the scalars of phase p (mode 0 after a norm or update
 // phase, 1 after an H*v phase) and publishes done[i] = p + 1.
-__device__ __forceinline__ void arrive(const PersistArgs &P, const BatchInst &a, int i, int p, int *flag)
+__device__ __forceinline__ void arrive(const PersistArgs &P, const BatchInst &a, int i, int p, int n, int *flag)
 {
-    __syncthreads();   // the partial (thread 0) and all data stores of the CTA are issued
+    __syncthreads();   // the partials (thread 0) and all data stores of the CTA are issued
     if (threadIdx.x == 0) {
         __threadfence();
-        const int old = atomicAdd(P.cnt + i, 1);
-        *flag = (old == (p + 1) * a.nblk - 1) ? 1 : 0;
+        const int old = atomicAdd(P.cnt + i, n);
+        *flag = (old + n == (p + 1) * a.nblk) ? 1 : 0;
         if (*flag) __threadfence();
     }
     __syncthreads();
@@ -633,6 +633,8 @@ __global__ void __launch_bounds__(kBatchThreads, 4) batch_persistent_kernel(cons
         if (flag != 0 || base >= tot_items) return;   // every thread of the CTA saw the same values
         __syncthreads();
         const int64_t id_end = min(base + (int64_t)kPersistChunk, tot_items);
+    // consecutive items of one instance and phase are counted with one arrival
+    int run_i = -1, run_p = -1, run_n = 0;
     for (int64_t id = base; id < id_end; ++id) {
         const int64_t s = id / P.nblocks;
         const int64_t b = __ldg(P.order + (id - s * P.nblocks));
@@ -640,15 +642,19 @@ __global__ void __launch_bounds__(kBatchThreads, 4) batch_persistent_kernel(cons
         const int p = (int)s - (int)__ldg(P.grp + i);
         if (p < 0 || p > 2 * P.nsteps) continue;
         const BatchInst &a = P.inst[i];
+        if (run_n > 0 && (i != run_i || p != run_p)) {
+            arrive(P, P.inst[run_i], run_i, run_p, run_n, &flag);
+            run_n = 0;
+        }
         if (p == 0) {
             // u_0 = x0 on the block's rows (and u_{-1} = 0 without a kept basis), partial ||x0||^2
             const int64_t r0 = (b - a.blk0) * a.rows;
             const int nr = (int)min((int64_t)a.rows, a.nsdn - r0);
-            const int64_t base = a.off + r0 * a.ld, n = (int64_t)nr * a.ld;
+            const int64_t base_e = a.off + r0 * a.ld, n = (int64_t)nr * a.ld;
             T *u0 = kept ? kept : U0;
             for (int64_t q = threadIdx.x; q < n; q += blockDim.x) {
-                u0[base + q] = x0[base + q];
-                if (!kept) U1[base + q] = (T)0;
+                u0[base_e + q] = x0[base_e + q];
+                if (!kept) U1[base_e + q] = (T)0;
             }
             double sn = 0.0;
             for (int r = 0; r < nr; ++r) {
@@ -656,25 +662,28 @@ __global__ void __launch_bounds__(kBatchThreads, 4) batch_persistent_kernel(cons
                 for (int64_t c = threadIdx.x; c < a.nsup; c += blockDim.x) sn += (double)row[c] * (double)row[c];
             }
             block_partial(sn, P.pb + b);
-            arrive(P, a, i, 0, &flag);
-            continue;
-        }
-        if (!wait_phase(P, i, p, &flag)) return;
-        // with a kept basis u_k is slot k (slot k-1 its predecessor, slot k+1 the next);
-        // else u_k lives in U[k % 2] and u_{k+1} overwrites u_{k-1}
-        const int k = (p - 1) / 2;
-        const T *uk = kept ? kept + (int64_t)k * P.total : ((k & 1) ? U1 : U0);
-        if (p % 2 == 1) {
-            hv_item<T, R, true>(P.inst, b, i, uk, Y, __ldcg(P.scal + (int64_t)i * kScal + kS), P.pa, smem_raw);
         } else {
-            const T *uprev = kept ? kept + (int64_t)(k > 0 ? k - 1 : 0) * P.total : ((k & 1) ? U0 : U1);
-            T *unext = kept ? kept + (int64_t)(k + 1) * P.total : ((k & 1) ? U0 : U1);
-            const double *sc = P.scal + (int64_t)i * kScal;
-            update_item<T, true>(a, b, (T)__ldcg(sc + kCCur), (T)__ldcg(sc + kCPrev), (T)0, Y, uk, uprev, unext,
-                                 P.pb, nullptr);
+            if (run_n == 0 && !wait_phase(P, i, p, &flag)) return;
+            // with a kept basis u_k is slot k (slot k-1 its predecessor, slot k+1 the next);
+            // else u_k lives in U[k % 2] and u_{k+1} overwrites u_{k-1}
+            const int k = (p - 1) / 2;
+            const T *uk = kept ? kept + (int64_t)k * P.total : ((k & 1) ? U1 : U0);
+            if (p % 2 == 1) {
+                hv_item<T, R, true>(P.inst, b, i, uk, Y, __ldcg(P.scal + (int64_t)i * kScal + kS), P.pa,
+                                    smem_raw);
+            } else {
+                const T *uprev = kept ? kept + (int64_t)(k > 0 ? k - 1 : 0) * P.total : ((k & 1) ? U0 : U1);
+                T *unext = kept ? kept + (int64_t)(k + 1) * P.total : ((k & 1) ? U0 : U1);
+                const double *sc = P.scal + (int64_t)i * kScal;
+                update_item<T, true>(a, b, (T)__ldcg(sc + kCCur), (T)__ldcg(sc + kCPrev), (T)0, Y, uk, uprev,
+                                     unext, P.pb, nullptr);
+            }
         }
-        arrive(P, a, i, p, &flag);
+        run_i = i;
+        run_p = p;
+        ++run_n;
     }
+    if (run_n > 0) arrive(P, P.inst[run_i], run_i, run_p, run_n, &flag);
     }
 }
 
@@ -897,10 +906,14 @@ extern "C" int ed_batch_create_rows(int ninst, ed_sector *const *secs, int rows,
         order.reserve((size_t)blk);
         size_t a0 = 0, a1 = 0;
         while (a0 < g0.size() || a1 < g1.size()) {
-            // take from the group that is behind its share
+            // take a run of kPersistChunk blocks from the group that is behind its share (consecutive
+            // blocks of one instance, whose arrivals a CTA then counts at once)
             const bool take0 = a1 >= g1.size() ||
                                (a0 < g0.size() && (double)a0 * (double)g1.size() <= (double)a1 * (double)g0.size());
-            order.push_back(take0 ? g0[a0++] : g1[a1++]);
+            for (int r = 0; r < kPersistChunk; ++r) {
+                if (take0 && a0 < g0.size()) order.push_back(g0[a0++]);
+                else if (!take0 && a1 < g1.size()) order.push_back(g1[a1++]);
+            }
         }
     }
     if (cudaMalloc(&bt->dev, sizeof(BatchInst) * ninst) != cudaSuccess ||
