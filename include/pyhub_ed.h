@@ -305,11 +305,13 @@ int ed_cf_eval(void *stream, int n, int m, const double *alpha, const double *be
  * reference (its dot products run on the CPU, lanczos.f90:53-55).
  * Same arguments and results as ed_multidot.  The partial sums live in a fixed
  * 1 MiB device array inside the library: nvec is limited to 64 (ED_ERR_RANGE
- * beyond), every GPU that loads the library holds the array until the
- * process exits, and calls that overlap on the GPU race because they share
- * it.  The first call on each device looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.
- * No call allocates or frees device memory. */
+ * beyond), the array is resident on a device from the library module's first
+ * use there until the process exits, and calls that overlap on the GPU race
+ * because they share it.  Outside a stream capture every call looks up the
+ * array's device address (cudaGetSymbolAddress); inside a capture the
+ * address found by an earlier call on that device is used, so make one call
+ * before any stream capture (a capture without one is refused with
+ * ED_ERR_ARG).  No call allocates or frees device memory. */
 int ed_multidot_noalloc(void *stream, int dtype, int64_t n, const void *V, int64_t ldv, int nvec,
                         const void *w, const void *z, double *out);
 

@@ -514,9 +514,16 @@ __global__ void __launch_bounds__(256) heis_slab_kernel(const T *__restrict__ x,
 //   q[p][0] = J!=K: sum over states I with J up, K down of (-1)^(J+K) bra[I'] ket[I]
 //             (I' = I with J and K swapped);  J==K: 0.5 sum bra ket
 //   q[p][1] = sum bra ket Sz_J Sz_K
+// The per-pair kernel forms only the transverse (flip) sums q0 of J != K:
 // CTAs are (row range, chunk of kRdmP pairs); each thread keeps the chunk's
 // sums in registers over all its rows, so one pass over the vector serves
-// kRdmP pairs.
+// kRdmP pairs.  The diagonal sums (q1 of every pair, q0 of J == K) come from
+// heis_rdm_diag_kernel, factorised: with s_j = +1 / -1 for site j+1 up /
+// down and b = bra*ket, sum b s_J s_K is sum_col C(col) s_J s_K for two A
+// sites, sum_row W(row) s_J s_K for two B sites and sum_col s_J T_K(col) for
+// an A site J and a B site K, where per class m of rows C(col) = sum_row b,
+// T_K(col) = sum_row b s_K(row) and W(row) = sum_col b: ~nB FP64 operations
+// per element for every pair at once.
 
 constexpr int kRdmP = 8;
 constexpr int kRdmThreads = 256;
@@ -529,6 +536,10 @@ struct HsRdmArgs {
     const int32_t *rankA, *row_m, *rowidx;
     const int64_t *row_off;
     int16_t pj[kMaxSites * kMaxSites], pk[kMaxSites * kMaxSites];   // hole-bit positions (site-1)
+    // the diagonal pass: rows grouped by m, and its tiles per m (columns x row ranges)
+    const int32_t *rows_of_m;
+    int64_t row_base[kMaxHalf + 2];
+    int tile_base[kMaxHalf + 2], nry[kMaxHalf + 1];
 };
 
 template <typename T>
@@ -582,13 +593,7 @@ __global__ void __launch_bounds__(kRdmThreads) heis_rdm_row_kernel(const T *__re
                 if (q >= np) break;
                 const int J = a.pj[p0 + q], K = a.pk[p0 + q];
                 const int dJ = (int)((h >> J) & 1u), dK = (int)((h >> K) & 1u);
-                if (J == K) {
-                    r0[q] += (T)0.5 * bk;
-                    r1[q] += (T)0.25 * bk;
-                    continue;
-                }
-                r1[q] += (dJ == dK) ? (T)0.25 * bk : (T)-0.25 * bk;
-                if (dJ || !dK || soff[q] < 0) continue;   // needs J up, K down
+                if (J == K || dJ || !dK || soff[q] < 0) continue;   // a flip needs J up, K down
                 // the swapped state: A part and B part of h ^ (bit J | bit K)
                 uint32_t ma = 0;
                 if (J < nA) ma |= 1u << J;
@@ -624,6 +629,92 @@ __global__ void __launch_bounds__(kRdmThreads) heis_rdm_row_kernel(const T *__re
     }
 }
 
+constexpr int kHdThreads = 256;
+
+template <typename T>
+__global__ void __launch_bounds__(kHdThreads) heis_rdm_diag_kernel(const T *__restrict__ bra, const T *__restrict__ ket,
+                                                                   const HsRdmArgs a, int mlo, int mhi,
+                                                                   double *__restrict__ partials)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double *Ts = reinterpret_cast<double *>(smem_raw);   // [kMaxHalf][kHdThreads]
+    double *Cs = Ts + kMaxHalf * kHdThreads;              // [kHdThreads]
+    double *accW = Cs + kHdThreads;                       // [npairs]
+    __shared__ double red[kHdThreads / 32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int m = mlo;
+    while (m < mhi && blockIdx.x >= a.tile_base[m + 1]) ++m;
+    const int ncx = (int)((a.ncol[m] + kHdThreads - 1) / kHdThreads);
+    const int local = blockIdx.x - a.tile_base[m];
+    const int cx = local % ncx, ry = local / ncx, nry = a.nry[m];
+    const int64_t col = (int64_t)cx * kHdThreads + threadIdx.x;
+    const bool act = col < a.ncol[m];
+    const int64_t nr_m = a.row_base[m + 1] - a.row_base[m];
+    const int64_t q0r = nr_m * ry / nry, q1r = nr_m * (ry + 1) / nry;
+    const int nA = a.nA;
+    for (int q = threadIdx.x; q < a.npairs; q += blockDim.x) accW[q] = 0.0;
+    double C = 0.0, Tk[kMaxHalf];
+#pragma unroll
+    for (int k = 0; k < kMaxHalf; ++k) Tk[k] = 0.0;
+    for (int64_t rr = q0r; rr < q1r; ++rr) {
+        const int32_t row = __ldg(a.rows_of_m + a.row_base[m] + rr);
+        const uint32_t hb = __ldg(a.row_pat + row);
+        const int64_t off = __ldg(a.row_off + row);
+        const double b = act ? (double)__ldg(bra + off + col) * (double)__ldg(ket + off + col) : 0.0;
+        C += b;
+#pragma unroll
+        for (int k = 0; k < kMaxHalf; ++k) Tk[k] += ((hb >> k) & 1u) ? -b : b;
+        double w = warp_sum(b);
+        __syncthreads();
+        if (lane == 0) red[warp] = w;
+        __syncthreads();
+        w = 0.0;
+#pragma unroll
+        for (int q = 0; q < kHdThreads / 32; ++q) w += red[q];
+        for (int q = threadIdx.x; q < a.npairs; q += blockDim.x) {
+            const int J = a.pj[q], K = a.pk[q];
+            if (J >= nA && K >= nA && J != K) {
+                const int sJ = ((hb >> (J - nA)) & 1u) ? -1 : 1, sK = ((hb >> (K - nA)) & 1u) ? -1 : 1;
+                accW[q] += (sJ * sK > 0) ? w : -w;
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < kMaxHalf; ++k) Ts[k * kHdThreads + threadIdx.x] = Tk[k];
+    Cs[threadIdx.x] = C;
+    __syncthreads();
+    for (int q = warp; q < a.npairs; q += kHdThreads / 32) {
+        const int J = a.pj[q], K = a.pk[q];
+        double s1 = 0.0;
+        for (int t = lane; t < kHdThreads; t += 32) {
+            const int64_t cc = (int64_t)cx * kHdThreads + t;
+            if (cc >= a.ncol[m]) continue;
+            const uint32_t ha = __ldg(a.col_pat + a.col_base[m] + cc);
+            if (J == K) {
+                s1 += Cs[t];
+            } else if (J < nA && K < nA) {
+                const bool neg = (((ha >> J) ^ (ha >> K)) & 1u) != 0;
+                s1 += neg ? -Cs[t] : Cs[t];
+            } else if (J < nA || K < nA) {
+                const int ja = J < nA ? J : K, kb = (J < nA ? K : J) - nA;
+                const double tv = Ts[kb * kHdThreads + t];
+                s1 += ((ha >> ja) & 1u) ? -tv : tv;
+            }
+        }
+        s1 = warp_sum(s1);
+        if (lane == 0) {
+            double *o = partials + ((int64_t)blockIdx.x * a.npairs + q) * 2;
+            if (J == K) {
+                o[0] = 0.5 * s1;
+                o[1] = 0.25 * s1;
+            } else {
+                o[0] = 0.0;
+                o[1] = 0.25 * ((J >= nA && K >= nA) ? accW[q] : s1);
+            }
+        }
+    }
+}
+
 template <typename T>
 static int heis_struct_rdm_run(ed_sector *s, cudaStream_t st, const T *bra, const T *ket, int npairs,
                                const int32_t *pairs, double *out, double *scratch, int max_blocks)
@@ -643,13 +734,45 @@ static int heis_struct_rdm_run(ed_sector *s, cudaStream_t st, const T *bra, cons
         a.pj[p] = (int16_t)(pairs[2 * p] - 1);
         a.pk[p] = (int16_t)(pairs[2 * p + 1] - 1);
     }
+    if (h.nB > kMaxHalf) {
+        set_error("B half of %d sites (at most %d)", h.nB, kMaxHalf);
+        return ED_ERR_RANGE;
+    }
+    a.rows_of_m = h.rows_of_m;
+    for (int m = 0; m <= kMaxHalf + 1; ++m) a.row_base[m] = h.row_base[m];
+    // diagonal tiles: per class m, 256-column tiles times row ranges, about max_blocks in all
+    const int64_t dim = s->dim;
+    int ntiles = 0;
+    for (int m = 0; m <= kMaxHalf + 1; ++m) a.tile_base[m] = 0;
+    for (int m = h.mlo; m <= h.mhi; ++m) {
+        a.tile_base[m] = ntiles;
+        const int64_t nr_m = h.row_base[m + 1] - h.row_base[m];
+        const int ncx = (int)((h.ncol[m] + kHdThreads - 1) / kHdThreads);
+        const double share = dim > 0 ? (double)(h.ncol[m] * nr_m) / (double)dim : 0.0;
+        int nry = (int)std::max<double>(1.0, std::floor(share * max_blocks / std::max(ncx, 1)));
+        nry = (int)std::min<int64_t>(std::max<int64_t>(nr_m, 1), nry);
+        a.nry[m] = nry;
+        ntiles += ncx * nry;
+    }
+    a.tile_base[h.mhi + 1] = ntiles;
+    const int gx = (int)std::max<int64_t>(1, std::min<int64_t>(h.nrows, max_blocks));
+    if (gx + ntiles > 3 * max_blocks) {
+        set_error("spin-correlation pass needs %d partial rows (scratch holds %d)", gx + ntiles, 3 * max_blocks);
+        return ED_ERR_RANGE;
+    }
+    // flips (q0 of J != K) into partial rows [0, gx), diagonal sums into [gx, gx + ntiles)
     const size_t smem = (size_t)std::max<int64_t>(h.max_len, 1) * sizeof(T);
     ED_CHECK_CUDA(cudaFuncSetAttribute(heis_rdm_row_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int gx = (int)std::max<int64_t>(1, std::min<int64_t>(h.nrows, max_blocks));
     const dim3 grid((unsigned)gx, (unsigned)((npairs + kRdmP - 1) / kRdmP));
     heis_rdm_row_kernel<T><<<grid, kRdmThreads, smem, st>>>(bra, ket, a, scratch);
     ED_CHECK_LAUNCH();
-    return launch_reduce(scratch, gx, 2 * npairs, out, st);
+    const size_t smemd = (size_t)(kMaxHalf + 1) * kHdThreads * sizeof(double) + (size_t)npairs * sizeof(double);
+    ED_CHECK_CUDA(cudaFuncSetAttribute(heis_rdm_diag_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smemd));
+    heis_rdm_diag_kernel<T><<<ntiles, kHdThreads, smemd, st>>>(bra, ket, a, h.mlo, h.mhi,
+                                                                scratch + (int64_t)gx * 2 * npairs);
+    ED_CHECK_LAUNCH();
+    return launch_reduce(scratch, gx + ntiles, 2 * npairs, out, st);
 }
 
 int heis_struct_rdm(ed_sector *s, cudaStream_t st, int dtype, const void *bra, const void *ket, int npairs,

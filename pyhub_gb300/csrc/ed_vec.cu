@@ -309,8 +309,12 @@ static std::mutex g_noalloc_mu;
 
 // Device address of g_noalloc_partials on the current device.  In host code
 // the array's name is only a host-side stand-in, so the address is looked up
-// once per device (with that device current) and cached.
-static int noalloc_partials(double **out)
+// with the device current.  Outside a stream capture it is looked up on every
+// call (cheap), so a context that was torn down and rebuilt, where the module
+// may have loaded at another address, never gets a stale pointer; inside a
+// capture the address cached by an earlier call on this device is used, and a
+// capture with no earlier call is refused.
+static int noalloc_partials(cudaStream_t st, double **out)
 {
     int dev = 0;
     ED_CHECK_CUDA(cudaGetDevice(&dev));
@@ -318,8 +322,10 @@ static int noalloc_partials(double **out)
         set_error("device %d is beyond the %d devices ed_multidot_noalloc tracks", dev, kNoAllocMaxDevices);
         return ED_ERR_RANGE;
     }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    ED_CHECK_CUDA(cudaStreamIsCapturing(st, &cs));
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (g_noalloc_addr[dev] == nullptr) {
+    if (cs == cudaStreamCaptureStatusNone) {
         void *p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
         if (e != cudaSuccess) {
@@ -327,6 +333,9 @@ static int noalloc_partials(double **out)
             return ED_ERR_CUDA;
         }
         g_noalloc_addr[dev] = static_cast<double *>(p);
+    } else if (g_noalloc_addr[dev] == nullptr) {
+        set_error("ed_multidot_noalloc: call it once on this device outside a stream capture first");
+        return ED_ERR_ARG;
     }
     *out = g_noalloc_addr[dev];
     return ED_OK;
@@ -363,10 +372,10 @@ extern "C" int ed_multidot_noalloc(void *stream, int dtype, int64_t n, const voi
         set_error("%d blocks x %d sums exceed the fixed scratch of %lld doubles", grid, m, (long long)kNoAllocDoubles);
         return ED_ERR_RANGE;
     }
-    double *part = nullptr;
-    const int rc = noalloc_partials(&part);
-    if (rc) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    double *part = nullptr;
+    const int rc = noalloc_partials(st, &part);
+    if (rc) return rc;
     const size_t smem = sizeof(double) * 8 * (size_t)m;  // at most 8 KiB: no opt-in needed
     if (dtype == ED_F32)
         multidot_kernel<float><<<grid, kVecThreads, smem, st>>>(n, static_cast<const float *>(V), ldv, nvec,
