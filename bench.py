@@ -404,6 +404,34 @@ def c4_batched(args, ws: int, rank: int, local: int, warmup: int = 1) -> dict:
     for _ in range(reps):
         hb.batch.hv(x, y, hb.scratch)
     t_hv = clock.stop() / reps
+    # the whole batched run as one persistent launch against the four-launch graph, on the 64-cluster
+    # chunk's particle/hole instances (3,072 instances, FP32, 40 steps), graph replays timed
+    pl = {}
+    res_ab = {}
+    xs = None
+    for pers in (False, True):
+        blp = GB.BatchedLanczos(_c4_gf_instances(clusters[:64]), 40, dtype=torch.float32, rows=rows,
+                                persistent=pers)
+        if xs is None:
+            xs = torch.rand(blp.batch.total, dtype=torch.float32, device="cuda")
+            for i, sct in enumerate(blp.sectors):
+                blp.batch.view(xs, i).view(sct.nsdn, -1)[:, sct.nsup:] = 0
+        blp.x0.copy_(xs)
+        blp.capture()
+        blp.replay()
+        torch.cuda.synchronize()
+        clock = StreamClock().start()
+        for _ in range(3):
+            blp.replay()
+        pl["persistent_ms_per_step" if pers else "four_launch_ms_per_step"] = clock.stop() / 3 / 40 * 1e3
+        res_ab[pers] = (blp.alpha.clone(), blp.beta.clone())
+        if pers:
+            pl["persistent_status"] = blp.batch.persistent_status(blp.scratch)
+        del blp
+        torch.cuda.empty_cache()
+    pl["alpha_beta_bit_identical"] = bool(torch.equal(res_ab[False][0], res_ab[True][0]) and
+                                          torch.equal(res_ab[False][1], res_ab[True][1]))
+    del xs, res_ab
     peak, src_kind = peaks()
     alg = sum(s.dim for s in hb.sectors) * 8.0
     n_gf = tim["instances"]
@@ -423,7 +451,8 @@ def c4_batched(args, ws: int, rank: int, local: int, warmup: int = 1) -> dict:
                                  "frac": alg / t_hv / 1e9 / peak, "peak_kind": f"of {src_kind}",
                                  "alg_bytes_per_launch": alg, "ms": t_hv * 1e3,
                                  "instances": len(hb.sectors), "traffic": None},
-           "lanczos_step_bytes_per_instance": per_step_bytes}
+           "lanczos_step_bytes_per_instance": per_step_bytes,
+           "persistent_vs_four_launch": pl}
     del singles, blb, hb, x, y
     torch.cuda.empty_cache()
     return out
@@ -440,6 +469,20 @@ def _c4_hv_sample(clusters):
         U = np.full(norb, spec["U"])
         for key in [(N + 1, N), (N - 1, N), (N, N + 1), (N, N - 1)]:
             out.append(_capi.Sector(norb, key[0], key[1], _capi.ED_HUBBARD, t=spec["t"], U=U))
+    return out
+
+
+def _c4_gf_instances(clusters):
+    """The sectors of the 48 particle/hole start vectors of each cluster (12
+    instances per N+-1 sector), in the sweep's order."""
+    import numpy as np
+    from pyhub_gb300 import _capi
+    out = []
+    for spec in clusters:
+        norb, N = spec["t"].shape[0], spec["N"]
+        U = np.full(norb, spec["U"])
+        for key in [(N + 1, N), (N - 1, N), (N, N + 1), (N, N - 1)]:
+            out += [_capi.Sector(norb, key[0], key[1], _capi.ED_HUBBARD, t=spec["t"], U=U)] * norb
     return out
 
 
