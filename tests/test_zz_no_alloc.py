@@ -36,9 +36,8 @@ def test_multidot_noalloc_matches_multidot(edlib, dt, with_z, pad):
     n, nvec = 1_048_576 + 96, 9
     g = torch.Generator(device="cuda")
     g.manual_seed(7)
-    store = torch.randn((nvec, n + pad), generator=g, dtype=td, device="cuda")
-    V = store[:, :n]
-    z = V[4] if with_z else None
+    V = torch.randn((nvec, n + pad), generator=g, dtype=td, device="cuda")   # row stride n + pad
+    z = V[4, :n] if with_z else None
     m = 2 * nvec if with_z else nvec
     scratch = torch.empty(edlib.scratch_bytes(n, nvec) // 8 + 1, dtype=torch.float64, device="cuda")
     stream = torch.cuda.current_stream().cuda_stream
