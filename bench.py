@@ -69,7 +69,9 @@ def parse():
     p.add_argument("--probe", action="store_true",
                    help="for profilers: c2, a few launches of each solve kernel on 4x4-sized vectors (about "
                         "4 GB); c4, two 3-step batched FP32 Lanczos runs (8 rows per CTA) over the particle/hole "
-                        "instances of --clusters clusters")
+                        "instances of --clusters clusters, then one 3-step persistent run (--persistent); c5, two "
+                        "all-pairs RDM passes on an FP64 vector of the 14-site sector")
+    p.add_argument("--persistent", action="store_true", help="c4 --probe: add a persistent batched run")
     return p.parse_args()
 
 
@@ -315,6 +317,10 @@ def probe_c4(args):
     bl.x0.copy_(torch.rand(bl.batch.total, dtype=torch.float32, device="cuda"))
     for _ in range(2):
         bl.run()
+    if args.persistent:
+        bp = GB.BatchedLanczos(secs, 3, dtype=torch.float32, rows=8, persistent=True)
+        bp.x0.copy_(bl.x0)
+        bp.run()
     torch.cuda.synchronize()
     print(json.dumps({"probe": "ok", "instances": len(secs), "elements": int(bl.batch.total)}))
 
@@ -509,6 +515,25 @@ def run_c4(args):
                 "batched_gf": r, "roofline": r["batch_hv_roofline"], "clocks": clk}
         print(json.dumps(line), flush=True)
     RP.finish()
+
+
+def probe_c5(args):
+    """Two all-pairs RDM passes (ed_rdm, every pair of the 14 sites, down hops
+    and transverse term) on an FP64 start vector of the 14-site random-bond
+    sector: the launches profiled under ncu."""
+    import torch
+    from pyhub_gb300 import _build, _capi
+    from pyhub_gb300.core import lanczos as LZ
+    from pyhub_gb300.core.reduced_quantities import all_pairs
+    from pyhub_gb300.tools import lattices as LT
+    _build.build()
+    t, U, _ = LT.random_bond_cluster(14, 7, seed=0)
+    sec = _capi.Sector(14, 7, 7, _capi.ED_HUBBARD, t=t, U=U)
+    psi = LZ.start_vector(sec, 0, dtype=torch.float64)
+    for _ in range(2):
+        raw, _ = sec.rdm_raw(psi, pairs=all_pairs(14), flags=3)
+    torch.cuda.synchronize()
+    print(json.dumps({"probe": "ok", "dim": sec.dim, "q0_11": float(raw[0, 0])}))
 
 
 def run_c3(args):
@@ -708,7 +733,10 @@ def main():
         run_c3(args)
         return
     if args.config == "c5":
-        run_c5(args)
+        if args.probe:
+            probe_c5(args)
+        else:
+            run_c5(args)
         return
     import numpy as np
     import torch

@@ -19,6 +19,7 @@ pass instead of being read back from stored vectors).
 from __future__ import annotations
 
 import math
+import os
 from copy import deepcopy as dc
 from time import perf_counter as pc
 
@@ -26,6 +27,7 @@ import numpy as np
 
 from .. import _capi
 from . import lanczos as LZ
+from . import store
 from .basis import Basis
 from .reduced_quantities import (GreenFunction, StaticQuantities, all_pairs, assemble_heisenberg,
                                  assemble_hubbard)
@@ -321,6 +323,186 @@ class CoreSolver(Basis, GreenFunction, StaticQuantities):
     def printv(self, *args):
         if self.verbose:
             print(*args)
+
+    # ----------------------------------------------------------- persistence
+    @property
+    def archive(self):
+        """Default archive of save()/restore(): the solver.h5 tree as solver.npz."""
+        return os.path.splitext(self.filename)[0] + ".npz"
+
+    def write_in(self):
+        """The input group of solver.h5 (core_solver.py:118-163): parameters and flags."""
+        grp = {"@nb_sites": self.nb_sites, "@n_up": self.nup[0], "@n_down": self.ndown[0],
+               "@do_solution": True, "@do_rq": bool(self.is_reduced_quantities), "@do_spgf": bool(self.is_spgf),
+               "@do_tprf": False, "@store_H": bool(getattr(self, "store_H", False)),
+               "@nb_sites_comp": int(getattr(self, "nb_sites_comp", self.nb_sites)), "@exec_name": self.exec_name}
+        U = self._uijkl
+        if U is not None:
+            grp.update({"@is_Uloc": 3, "U": np.asarray(U, dtype=np.float64),
+                        "Upartial": np.einsum('ijkl,ijkl->ij', U, U), "@do_rq_two_body": True})
+        elif self._kind == _capi.ED_HUBBARD:
+            grp.update({"@is_Uloc": 2, "U": self._u_vector(), "@do_rq_two_body": False})
+        grp["t_matrix"] = np.asarray(self.t_matrix, dtype=np.float64)
+        grp["J"] = np.asarray(self.J_matrix, dtype=np.float64)
+        grp["@T"] = float(self.T)
+        grp["@nb_comp_states"] = int(getattr(self, "nb_comp_states_", 1))
+        grp["@excited_state"] = int(self.excited_state) + 1   # 0: Boltzmann average (core_solver.py:75)
+        grp["lanczos"] = {"@max_lcz": int(getattr(self, "max_lcz", 600)),
+                          "@acc_lcz": float(getattr(self, "acc_lcz", 1.e-8)), "@renorm": False}
+        return grp
+
+    def _solve_group(self):
+        """The solve group (solve.f90:26-120, lanczos.f90:37-126).  A dense solve keeps
+        eigenvectors[b] = state b; a Lanczos solve keeps its Ritz states as psi_<b>
+        (reference basis order) in place of the Krylov vectors it does not store."""
+        s = self._sol
+        grp = {"@nstates": int(s["nstates"]), "eigenvalues": np.asarray(s["eigenvalues"], dtype=np.float64),
+               "boltzmann": np.asarray(s["boltzmann"], dtype=np.float64), "@nw": len(s["boltzmann"]),
+               "@deg": int(s["deg"]), "@is_lanczos": int(bool(s["is_lanczos"]))}
+        if s.get("H") is not None:
+            grp["H"] = np.asarray(s["H"]).T   # read back transposed, as core_solver.py:185 does
+        if not s["is_lanczos"]:
+            grp["eigenvectors"] = np.asarray(s["eigenvectors_ref"]).T
+            return grp
+        sec = self.sector(self.nup[0], self.ndown[0])
+        for b, v in enumerate(s["psis"]):
+            if v is not None:
+                grp[f"psi_{b}"] = sec.to_ref(v).cpu().numpy()
+        grp["lanczos"] = {"alpha": np.asarray(s["alpha"], dtype=np.float64),
+                          "beta": np.asarray(s["beta"], dtype=np.float64),
+                          "@lcz_conv": float(s["conv"]), "@nb_lcz": int(s["nb_lcz"]),
+                          "@max_lcz": int(getattr(self, "max_lcz", 600)), "@converged": bool(s["converged"]),
+                          "@precision": str(s.get("precision", "f64")), "@reorth": str(s.get("reorth", "full"))}
+        return grp
+
+    def _rq_group(self):
+        """reduced_quantities (static_rq.f90:16-45) in the layout the reference reads
+        (reduced_quantities.py:14-48): the state index last, dbl_occ as [i,j,k,l,b]."""
+        rq = self._rq
+        grp = {"density_matrix_up": np.transpose(rq["density_matrix_up"], (1, 2, 0)),
+               "density_matrix_down": np.transpose(rq["density_matrix_down"], (1, 2, 0)),
+               "ni": np.transpose(rq["ni"]), "sisj": np.transpose(rq["sisj"], (1, 2, 0))}
+        if rq.get("dbl_occ") is not None:
+            grp["dbl_occ"] = np.transpose(rq["dbl_occ"], (4, 3, 2, 1, 0))
+        return grp
+
+    def _spgf_group(self):
+        """Pole blocks of every state: continued-fraction poles of each start vector
+        c_i|psi_b> (diag_<i>) and (c_i + c_j)|psi_b> (pair_<i>_<j>) as [2, m] arrays
+        (eigenvalues, weights), with the start-vector norms."""
+        grp = {"@nstates": len(self._spgf), "@nb_sites_comp": int(self.nb_sites_comp)}
+        for b, st in enumerate(self._spgf):
+            if st is None:
+                continue
+            sg = {"@down_is_up": bool(st["down"] is st["up"])}
+            for spin in (("up",) if st["down"] is st["up"] else ("up", "down")):
+                for part, blk in st[spin].items():
+                    g = {"@n": blk.n, "@sign": blk.sign, "@e0": blk.e0,
+                         "norm2": np.array([blk.norm2.get(i, np.nan) for i in range(blk.n)])}
+                    for i, (e, w) in blk.diag.items():
+                        g[f"diag_{i}"] = np.stack([np.asarray(e, dtype=np.float64), np.asarray(w, dtype=np.float64)])
+                    for (i, j), (e, w) in blk.pair.items():
+                        g[f"pair_{i}_{j}"] = np.stack([np.asarray(e, dtype=np.float64), np.asarray(w, dtype=np.float64)])
+                        g[f"norm2_pair_{i}_{j}"] = np.float64(blk.norm2_pair[(i, j)])
+                    sg[f"{spin}_{part}"] = g
+            grp[f"state_{b}"] = sg
+        return grp
+
+    def save(self, path: str = None) -> str:
+        """Write the solve's inputs and results (the solver.h5 tree: input, solve,
+        reduced_quantities, spgf) to one archive; returns its path."""
+        if self._sol is None:
+            raise RuntimeError("nothing to save: call kernel() first")
+        tree = {"input": self.write_in(), "solve": self._solve_group()}
+        if self._rq is not None:
+            tree["reduced_quantities"] = self._rq_group()
+        if self._spgf is not None:
+            tree["spgf"] = self._spgf_group()
+        return store.save(path or self.archive, tree)
+
+    def restore(self, path: str = None):
+        """Load an archive written by save() for the same Hamiltonian, so that the
+        properties (e, e0, psi0, rq, gf ...) answer without a new solve.  Raises
+        ValueError when the archive holds another model, sector or parameter set."""
+        from .greens import PoleBlock
+        tree = store.load(path or self.archive)
+        inp, mine = tree["input"], self.write_in()
+        for key in ("@nb_sites", "@n_up", "@n_down", "@exec_name", "@is_Uloc", "@T"):
+            if (key in inp) != (key in mine) or (key in inp and inp[key] != mine[key]):
+                raise ValueError(f"the archive holds another solve: input {key[1:]} differs")
+        for key in ("t_matrix", "J", "U"):
+            if (key in inp) != (key in mine) or (key in inp and not np.array_equal(inp[key], mine[key])):
+                raise ValueError(f"the archive holds another solve: input {key} differs")
+        lz = inp.get("lanczos", {})
+        self.max_lcz, self.acc_lcz = int(lz.get("@max_lcz", 600)), float(lz.get("@acc_lcz", 1.e-8))
+        self.nb_comp_states_ = int(inp["@nb_comp_states"])
+        self.store_H = bool(inp["@store_H"])
+        self.nb_sites_comp = int(inp["@nb_sites_comp"])
+        sg = tree["solve"]
+        sol = {"eigenvalues": np.asarray(sg["eigenvalues"]), "is_lanczos": bool(sg["@is_lanczos"]),
+               "deg": int(sg["@deg"]), "nstates": int(sg["@nstates"]),
+               "H": None if "H" not in sg else np.ascontiguousarray(np.asarray(sg["H"]).T),
+               "boltzmann": np.asarray(sg["boltzmann"])}
+        if sol["is_lanczos"]:
+            torch = _torch()
+            sec = self.sector(self.nup[0], self.ndown[0])
+            nps = 1 + max([int(k[4:]) for k in sg if k.startswith("psi_")], default=-1)
+            sol["psis"] = [None] * nps
+            for b in range(nps):
+                if f"psi_{b}" in sg:
+                    sol["psis"][b] = sec.from_ref(torch.from_numpy(np.ascontiguousarray(sg[f"psi_{b}"])).cuda())
+            g = sg["lanczos"]
+            sol.update({"alpha": np.asarray(g["alpha"]), "beta": np.asarray(g["beta"]),
+                        "conv": float(g["@lcz_conv"]), "nb_lcz": int(g["@nb_lcz"]),
+                        "converged": bool(g["@converged"]), "precision": str(g["@precision"]),
+                        "reorth": str(g["@reorth"])})
+        else:
+            sol["eigenvectors_ref"] = np.ascontiguousarray(np.asarray(sg["eigenvectors"]).T)
+        self._sol = sol
+        self.is_solve = True
+        self.set_state(int(inp["@excited_state"]) - 1)
+        self._rq, self._spgf = None, None
+        self.is_reduced_quantities = self.is_spgf = False
+        if "reduced_quantities" in tree:
+            r = tree["reduced_quantities"]
+            back = lambda a, ax: np.ascontiguousarray(np.transpose(a, ax))   # noqa: E731
+            self._rq = {"density_matrix_up": back(r["density_matrix_up"], (2, 0, 1)),
+                        "density_matrix_down": back(r["density_matrix_down"], (2, 0, 1)),
+                        "ni": back(r["ni"], (1, 0)), "sisj": back(r["sisj"], (2, 0, 1)),
+                        "dbl_occ": back(r["dbl_occ"], (4, 3, 2, 1, 0)) if "dbl_occ" in r else None}
+            self.is_reduced_quantities = True
+        if "spgf" in tree:
+            sp = tree["spgf"]
+            out = []
+            for b in range(int(sp["@nstates"])):
+                st = sp.get(f"state_{b}")
+                if st is None:
+                    out.append(None)
+                    continue
+                blocks = {}
+                for spin in (("up",) if st["@down_is_up"] else ("up", "down")):
+                    blocks[spin] = {}
+                    for part in ("greater", "lesser"):
+                        g = st[f"{spin}_{part}"]
+                        blk = PoleBlock(int(g["@n"]), float(g["@sign"]), float(g["@e0"]))
+                        for i, v in enumerate(np.asarray(g["norm2"])):
+                            if not np.isnan(v):
+                                blk.norm2[i] = float(v)
+                        for k, v in g.items():
+                            if k.startswith("diag_"):
+                                blk.diag[int(k[5:])] = (v[0], v[1])
+                            elif k.startswith("pair_"):
+                                i, j = (int(x) for x in k[5:].split("_"))
+                                blk.pair[(i, j)] = (v[0], v[1])
+                                blk.norm2_pair[(i, j)] = float(g[f"norm2_pair_{i}_{j}"])
+                        blocks[spin][part] = blk
+                if st["@down_is_up"]:
+                    blocks["down"] = blocks["up"]
+                out.append(blocks)
+            self._spgf = out
+            self.is_spgf = True
+            self.gf = self.compute_gf()
+        return self
 
     # ----------------------------------------------------------- properties
     @property
