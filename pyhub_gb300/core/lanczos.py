@@ -318,6 +318,8 @@ def lanczos_full(sec, v0, max_steps: int, dtype=None, rule=None, check_every: in
             # the check posted after the previous step, read while this step runs
             kc, ev, hs, hab = pending
             pending = None
+            # step kc is already enqueued: its lanczos_coef part 1 rewrites beta[kc-1] and s[kc]
+            # from the same norm (idempotent), so stopping at check kc leaves the Ritz scales intact
             if ev is not None:
                 ev.synchronize()
             st_c, g_c = int(hs[0]), float(hs[1])

@@ -229,7 +229,7 @@ __device__ __forceinline__ void up_group(const BatchInst &a, const T *xs, int at
 }
 
 // G down-hop neighbour rows (16-byte vector v of each): loads issued together
-// (COH: L2-coherent loads, for the persistent run).
+// (COH: ordinary weak loads, for the persistent run).
 template <typename T, int G, bool COH>
 __device__ __forceinline__ void down_group(const NbEnt<T> *en, const T *__restrict__ ub, int v,
                                            typename V16<T>::type &acc)
@@ -241,7 +241,7 @@ __device__ __forceinline__ void down_group(const NbEnt<T> *en, const T *__restri
     for (int j = 0; j < G; ++j) {
         const NbEnt<T> e = en[j];
         cf[j] = e.cf;
-        if constexpr (COH) xn[j] = __ldcg(reinterpret_cast<const V *>(ub + e.off) + v);
+        if constexpr (COH) xn[j] = __ldca(reinterpret_cast<const V *>(ub + e.off) + v);
         else xn[j] = __ldg(reinterpret_cast<const V *>(ub + e.off) + v);
     }
 #pragma unroll
@@ -251,18 +251,21 @@ __device__ __forceinline__ void down_group(const NbEnt<T> *en, const T *__restri
 }
 
 // Loads of data another CTA may have written earlier in the same launch
-// (the persistent run): L2 only, never a possibly stale L1 line.  Loads of
-// data written before the launch can use the read-only path.
+// (the persistent run): ordinary weak loads (ld.global.ca, or cp.async for
+// the staged rows), each after the CTA's acquire load of the instance's phase
+// counter, which the writers published with fence + release.  The PTX memory
+// model makes those writes visible to weak loads ordered after the acquire;
+// it gives no such guarantee to the non-coherent read-only path (ld.global.nc),
+// which only loads of data written before the launch use.
 template <bool COH, typename V> __device__ __forceinline__ V ld_data(const V *p)
 {
-    if constexpr (COH) return __ldcg(p);
+    if constexpr (COH) return __ldca(p);
     else return __ldg(p);
 }
 
 // y = s_k H u_k and partial <u_k, y> over R rows of one instance.
 // Phase A (diagonal + up hops): the rows are staged in shared memory one
-// column per string (asynchronous copies, all in flight together; in the
-// persistent run coherent loads in groups of 4); a warp owns 32-string
+// column per string (asynchronous copies, all in flight together); a warp owns 32-string
 // slices, loads each sliced-ELL slot once and applies it to all rows with
 // 16-byte shared loads; the sums go to y.  Phase B (down hops): each row
 // adds its neighbour rows as 16-byte-vector axpys read from L2 (the
@@ -291,40 +294,13 @@ __device__ __forceinline__ void hv_item(const BatchInst *__restrict__ inst, int6
     const T *dcf = (sizeof(T) == 4) ? reinterpret_cast<const T *>(a.dcf32) : reinterpret_cast<const T *>(a.dcf64);
     const T *ued_t = (sizeof(T) == 4) ? reinterpret_cast<const T *>(a.uediag32) : reinterpret_cast<const T *>(a.uediag);
     const T *ded_t = (sizeof(T) == 4) ? reinterpret_cast<const T *>(a.dediag32) : reinterpret_cast<const T *>(a.dediag);
-    if constexpr (COH) {
-        // 16-byte coherent loads (rows are 16-byte aligned and zero padded), 8 in flight per
-        // thread, each scattered into the column layout
-        const int nvr = (nsup + VN - 1) / VN, nvt = R * nvr;
-        for (int i0 = threadIdx.x; i0 < nvt; i0 += 8 * kBatchThreads) {
-            V w[8];
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const int i = i0 + j * kBatchThreads;
-                const int r = i / nvr, v = i - r * nvr;
-                w[j] = (i < nvt && r < nr) ? __ldcg(reinterpret_cast<const V *>(ub + (int64_t)(r0 + r) * ld) + v)
-                                           : V{};
-            }
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const int i = i0 + j * kBatchThreads;
-                if (i >= nvt) break;
-                const int r = i / nvr, v = i - r * nvr;
-#pragma unroll
-                for (int k = 0; k < VN; ++k) {
-                    const int c = v * VN + k;
-                    if (c < nsup) xs[c * S + r] = reinterpret_cast<const T *>(&w[j])[k];
-                }
-            }
-        }
-    } else {
-        for (int r = 0; r < R; ++r) {
-            const T *src = ub + (int64_t)(r0 + r) * ld;
-            for (int c = threadIdx.x; c < nsup; c += blockDim.x) {
-                if (r < nr)
-                    cp_async_elem(xs + c * S + r, src + c);
-                else
-                    xs[c * S + r] = (T)0;
-            }
+    for (int r = 0; r < R; ++r) {
+        const T *src = ub + (int64_t)(r0 + r) * ld;
+        for (int c = threadIdx.x; c < nsup; c += blockDim.x) {
+            if (r < nr)
+                cp_async_elem(xs + c * S + r, src + c);
+            else
+                xs[c * S + r] = (T)0;
         }
     }
     for (int r = warp; r < R; r += nwarps) {
@@ -344,7 +320,7 @@ __device__ __forceinline__ void hv_item(const BatchInst *__restrict__ inst, int6
             row_ed[r] = (r < nr) ? __ldg(ded_t + r0 + r) : (T)0;
         }
     }
-    if constexpr (!COH) cp_async_wait_all();
+    cp_async_wait_all();
     __syncthreads();
     // ---- phase A
     for (int sl = warp; sl < a.nslice; sl += nwarps) {
@@ -448,7 +424,7 @@ __device__ __forceinline__ void update_item(const BatchInst &a, int64_t b, T cc,
     for (int q = threadIdx.x; q < nv; q += blockDim.x) {
         const V yy = ld_data<COH>(yv + q), uk = ld_data<COH>(uv + q);
         V pp;
-        if constexpr (COH) pp = __ldcg(pv + q);
+        if constexpr (COH) pp = __ldca(pv + q);
         else pp = pv[q];
         V nv_;
 #pragma unroll

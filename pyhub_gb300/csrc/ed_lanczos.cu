@@ -67,7 +67,11 @@ __device__ __forceinline__ double block_max_d(double v, double *red)
 }
 
 // One CTA.  Part 1 (every call, k >= 1): beta_{k-1} and s_k from nrm, with
-// the breakdown test of the host loop (beta <= 1e-13 max(1, |alpha|)).  Part 2
+// the breakdown test of the host loop (beta <= 1e-13 max(1, |alpha|)).
+// Part 1 is idempotent: a second call for the same k with the same nrm writes
+// the same beta_{k-1} and s_k.  The host's look-ahead relies on it (a run that
+// stops at a check has already enqueued the next step, whose part 1 rewrites
+// them before the Ritz vector is formed).  Part 2
 // (dots != NULL): G row k, Linv row k, coef and alpha_k; it also stops the run
 // when u_k is numerically dependent on the basis.  Once stopped, coef is
 // written as zeros (and s stays 0), so the vectors that follow are zero and
