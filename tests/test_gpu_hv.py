@@ -15,7 +15,7 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 
 HUB_CASES = [(2, 1, 1), (4, 2, 2), (5, 2, 3), (6, 3, 3), (6, 2, 4), (7, 3, 2), (8, 4, 4), (8, 1, 7),
-             (9, 4, 5), (10, 5, 5), (10, 0, 3), (12, 6, 6), (12, 5, 6)]
+             (9, 4, 5), (10, 5, 5), (10, 0, 3), (6, 3, 0), (4, 4, 4), (12, 6, 6), (12, 5, 6)]
 EPS64 = np.finfo(np.float64).eps
 EPS32 = float(np.finfo(np.float32).eps)
 
