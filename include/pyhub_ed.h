@@ -251,8 +251,9 @@ int ed_batch_lanczos(ed_batch *b, void *stream, int dtype, void *work, const voi
  * The instances are split into two groups one phase apart, so the H*v of
  * one group runs beside the update of the other.  alpha/beta are
  * bit-identical to the four-launch form.  Every wait is bounded (10 s of GPU
- * time); a run that gives up sets a status that ed_batch_persistent_status
- * returns (0 = ok) and stops.  Enqueues one memset and one launch, so the
+ * time unless ed_batch_persistent_watchdog sets another limit); a run that
+ * gives up sets a status that ed_batch_persistent_status returns (0 = ok)
+ * and stops.  Enqueues one memset and one launch, so the
  * call can be captured in a CUDA graph.  The per-start-block loops of
  * GF_BANDLANCZOS (spgf_bandlanczos.f90:309-448) for many instances at once. */
 int ed_batch_lanczos_persistent(ed_batch *b, void *stream, int dtype, void *work, const void *x0, int nsteps,
@@ -261,6 +262,13 @@ int ed_batch_lanczos_persistent(ed_batch *b, void *stream, int dtype, void *work
  * copy to the host): 0 = completed, 1 = a wait gave up.  No reference
  * counterpart. */
 int ed_batch_persistent_status(const ed_batch *b, const void *scratch, int *status);
+/* Settings of the batch's later persistent runs: the limit of every wait in
+ * seconds of GPU time (0 < wait_seconds <= 60; 10 when never set), and, to
+ * test that limit, an instance whose first H*v phase never completes
+ * (stall_instance; -1 = none): the CTAs that wait on it give up after the
+ * limit, status 1 is set and the whole grid returns.  Host-side only.  No
+ * reference counterpart. */
+int ed_batch_persistent_watchdog(ed_batch *b, double wait_seconds, int stall_instance);
 /* Replay of ed_batch_lanczos from the same x0 that also accumulates, per
  * instance, the Ritz vector out_i += sum_k coef[i][k] q_k (q_k the
  * normalised Lanczos vectors; coef device FP64 [ninst][nsteps], typically the

@@ -47,6 +47,7 @@ _SIGS = {
     "ed_sector_set_uijkl": (_I, [_P, _P]),
     "ed_batch_lanczos_persistent": (_I, [_P, _P, _I, _P, _P, _I, _P, _P, _P, _P, _I64]),
     "ed_batch_persistent_status": (_I, [_P, _P, ctypes.POINTER(_I)]),
+    "ed_batch_persistent_watchdog": (_I, [_P, ctypes.c_double, _I]),
     "ed_dbl_occ_scratch_bytes": (_I64, [_P, _I]),
     "ed_dbl_occ": (_I, [_P, _P, _I, _I64, _P, _P, _I, _P, _P, _P, _I64]),
     "ed_batch_ritz": (_I, [_P, _P, _I, _P, _P, _I, _P, _P, _P, _P, _P, _I64]),
@@ -367,6 +368,12 @@ class Batch:
         check("ed_batch_persistent_status", lib().ed_batch_persistent_status(self._h, _ptr(scratch),
                                                                              ctypes.byref(st)))
         return st.value
+
+    def persistent_watchdog(self, wait_seconds: float = 10.0, stall_instance: int = -1):
+        """Wait limit of later persistent runs, and (to test it) an instance
+        whose first H*v phase never completes."""
+        check("ed_batch_persistent_watchdog", lib().ed_batch_persistent_watchdog(self._h, float(wait_seconds),
+                                                                                 int(stall_instance)))
 
     def lanczos(self, work, x0, nsteps: int, alpha, beta, scratch, stream=None):
         sb = scratch.numel() * scratch.element_size()

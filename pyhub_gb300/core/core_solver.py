@@ -26,6 +26,7 @@ from time import perf_counter as pc
 import numpy as np
 
 from .. import _capi
+from ..trace import nvtx
 from . import lanczos as LZ
 from . import store
 from .basis import Basis
@@ -120,12 +121,14 @@ class CoreSolver(Basis, GreenFunction, StaticQuantities):
         self._sectors = {}
         self._rq = None
         self._spgf = None
-        sec = self.sector(self.nup[0], self.ndown[0])
+        with nvtx("pyhub.sector"):
+            sec = self.sector(self.nup[0], self.ndown[0])
         self.printv('start calculation')
-        if sec.dim < max_lcz:
-            self._sol = self._exact_diag(sec, store_H)
-        else:
-            self._sol = self._lanczos(sec, max_lcz, acc_lcz, nb_comp_states, dtype, reorth, seed, refine_steps)
+        with nvtx("pyhub.solve"):
+            if sec.dim < max_lcz:
+                self._sol = self._exact_diag(sec, store_H)
+            else:
+                self._sol = self._lanczos(sec, max_lcz, acc_lcz, nb_comp_states, dtype, reorth, seed, refine_steps)
         self._sol["boltzmann"] = self._boltzmann(self._sol["eigenvalues"], nb_comp_states)
         self.is_solve = True
         self.wgt = dc(self.boltzmann)
@@ -258,6 +261,10 @@ class CoreSolver(Basis, GreenFunction, StaticQuantities):
         return psis[k]
 
     def reduced_quantities(self):
+        with nvtx("pyhub.reduced_quantities"):
+            self._reduced_quantities()
+
+    def _reduced_quantities(self):
         t0 = pc()
         self.printv('start reduced quantities calculation')
         sec = self.sector(self.nup[0], self.ndown[0])
@@ -297,6 +304,10 @@ class CoreSolver(Basis, GreenFunction, StaticQuantities):
         self.printv(f'end calculation | elapsed time {np.around(pc() - t0, 4)} s')
 
     def spgf(self, nb_sites_comp=None, nsteps: int = None, offdiag: bool = True):
+        with nvtx("pyhub.spgf"):
+            self._spgf_run(nb_sites_comp, nsteps, offdiag)
+
+    def _spgf_run(self, nb_sites_comp, nsteps, offdiag):
         from . import greens as GR
         self.nb_sites_comp = self.nb_sites if nb_sites_comp is None else nb_sites_comp
         if self._kind != _capi.ED_HUBBARD:

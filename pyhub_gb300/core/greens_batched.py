@@ -20,6 +20,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from .. import _capi
+from ..trace import nvtx
 from . import lanczos as LZ
 
 
@@ -369,7 +370,8 @@ def sweep(clusters, nsteps: int = 150, chunk: int = 64, dtype=None, gs_steps: in
                     for site in range(1, norb + 1):
                         inst.append((ci, spin, part, site))
                         secs.append(own[key])
-        gsb = batched_ground_states(srcs, nsteps=gs_steps, tol=gs_tol, seed=c0)
+        with nvtx("pyhub.sweep.ground_states"):
+            gsb = batched_ground_states(srcs, nsteps=gs_steps, tol=gs_tol, seed=c0)
         restarts = max(restarts, gsb.restarts)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
@@ -389,18 +391,20 @@ def sweep(clusters, nsteps: int = 150, chunk: int = 64, dtype=None, gs_steps: in
                                      bl.x0[int(off[i]):], stride)
         torch.cuda.synchronize()
         t2 = time.perf_counter()
-        if graph:
-            bl.capture()
-            bl.replay()
-        else:
-            bl.run()
-        torch.cuda.synchronize()
+        with nvtx("pyhub.sweep.batched_lanczos"):
+            if graph:
+                bl.capture()
+                bl.replay()
+            else:
+                bl.run()
+            torch.cuda.synchronize()
         t3 = time.perf_counter()
         # greater: <phi|(w + E0 + i eta - H)^-1|phi>; lesser: <phi|(w - E0 + i eta + H)^-1|phi>
         sg = torch.tensor([1.0 if p == "greater" else -1.0 for (_, _, p, _) in inst], dtype=torch.float64,
                           device="cuda")
         e0s = torch.tensor([gsb.e0[ci] for (ci, _, _, _) in inst], dtype=torch.float64, device="cuda")
-        G = _capi.cf_eval(bl.alpha, bl.beta, omega.to(torch.complex128) + 1j * eta, shift=sg * e0s, sign=sg)
+        with nvtx("pyhub.sweep.continued_fractions"):
+            G = _capi.cf_eval(bl.alpha, bl.beta, omega.to(torch.complex128) + 1j * eta, shift=sg * e0s, sign=sg)
         for ci in range(len(cl)):
             norb = cl[ci]["t"].shape[0]
             g = G[base[ci]: base[ci] + 4 * norb].view(2, 2, norb, -1).sum(dim=1)

@@ -68,6 +68,8 @@ struct ed_batch {
     int rows = 8;                      // rows per CTA (4, 8 or 16)
     int32_t *order = nullptr;          // [nblocks] device: persistent-run item order of one super-phase
     int8_t *grp = nullptr;             // [ninst] device: phase offset (0 or 1) of each instance
+    double wait_s = 10.0;              // persistent run: limit of every wait, in seconds of GPU time
+    int stall_inst = -1;               // persistent run: instance whose first H*v phase never completes (-1: none)
 };
 
 namespace ed {
@@ -477,7 +479,7 @@ __global__ void __launch_bounds__(kBatchThreads) batch_update_kernel(const Batch
 // counter, and the last CTA to arrive forms the instance's scalars exactly as
 // batch_scalar_kernel does (same partials, same summation order: alpha/beta
 // are bit-identical to the four-launch form) and publishes done[i] = p + 1.
-// Every wait gives up after kWaitNs of GPU time: it sets status[0] and the
+// Every wait gives up after wait_ns of GPU time: it sets status[0] and the
 // whole grid returns.  CTAs claim items from a queue in list order, so a CTA
 // waits only on items already claimed by running CTAs.
 struct PersistArgs {
@@ -494,9 +496,10 @@ struct PersistArgs {
     int *status;              // [1] 0 = ok
     unsigned long long *queue;   // next unclaimed item
     double *scal, *pa, *pb, *alpha, *beta;
+    unsigned long long wait_ns;  // limit of every wait (default 10 s: far above any phase of one instance)
+    int stall_inst;              // watchdog test: this instance never completes phase 1 (-1: none)
 };
 
-constexpr unsigned long long kWaitNs = 10ull * 1000000000ull;   // 10 s: far above any phase of one instance
 constexpr int kPersistChunk = 4;   // items claimed at once
 
 __device__ __forceinline__ unsigned long long gtimer()
@@ -528,7 +531,7 @@ __device__ __forceinline__ bool wait_phase(const PersistArgs &P, int i, int p, i
             unsigned ns = 32;
             while (ld_acquire(P.done + i) < p) {
                 if (ld_acquire(P.status) != 0) { ok = 0; break; }
-                if (gtimer() - t0 > kWaitNs) {
+                if (gtimer() - t0 > P.wait_ns) {
                     atomicCAS(P.status, 0, 1);
                     ok = 0;
                     break;
@@ -552,10 +555,14 @@ __device__ __forceinline__ void arrive(const PersistArgs &P, const BatchInst &a,
 {
     __syncthreads();   // the partials (thread 0) and all data stores of the CTA are issued
     if (threadIdx.x == 0) {
-        __threadfence();
-        const int old = atomicAdd(P.cnt + i, n);
-        *flag = (old + n == (p + 1) * a.nblk) ? 1 : 0;
-        if (*flag) __threadfence();
+        int last = 0;
+        if (i != P.stall_inst || p != 1) {   // the watchdog test leaves one counter short: its waiters give up
+            __threadfence();
+            const int old = atomicAdd(P.cnt + i, n);
+            last = (old + n == (p + 1) * a.nblk) ? 1 : 0;
+            if (last) __threadfence();
+        }
+        *flag = last;
     }
     __syncthreads();
     if (*flag && threadIdx.x < 32) {
@@ -1111,6 +1118,8 @@ static int run_persistent(ed_batch *bt, cudaStream_t st, T *work, const T *x0, i
     P.queue = reinterpret_cast<unsigned long long *>(ints + 2 * bt->ninst + 2);   // 8-byte aligned
     P.alpha = alpha;
     P.beta = beta;
+    P.wait_ns = (unsigned long long)(bt->wait_s * 1e9);
+    P.stall_inst = bt->stall_inst;
     ED_CHECK_CUDA(cudaMemsetAsync(ints, 0, sizeof(int) * (2 * (size_t)bt->ninst + 4), st));
     if (bt->nblocks == 0) return ED_OK;
     const size_t smem = (size_t)bt->max_ld * staged_stride<T, R>() * sizeof(T);
@@ -1167,6 +1176,18 @@ extern "C" int ed_batch_lanczos_persistent(ed_batch *bt, void *stream, int dtype
     if (bt->rows == 4) return run_persistent<double, 4>(bt, st, w, x, nsteps, alpha, beta, sc, kp);
     if (bt->rows == 16) return run_persistent<double, 16>(bt, st, w, x, nsteps, alpha, beta, sc, kp);
     return run_persistent<double, 8>(bt, st, w, x, nsteps, alpha, beta, sc, kp);
+}
+
+extern "C" int ed_batch_persistent_watchdog(ed_batch *bt, double wait_seconds, int stall_instance)
+{
+    clear_error();
+    ED_REQUIRE(bt != nullptr, "batch is NULL");
+    ED_REQUIRE(wait_seconds > 0.0 && wait_seconds <= 60.0, "wait_seconds=%g outside (0, 60]", wait_seconds);
+    ED_REQUIRE(stall_instance >= -1 && stall_instance < bt->ninst, "stall_instance=%d outside -1..%d", stall_instance,
+               bt->ninst - 1);
+    bt->wait_s = wait_seconds;
+    bt->stall_inst = stall_instance;
+    return ED_OK;
 }
 
 extern "C" int ed_batch_persistent_status(const ed_batch *bt, const void *scratch, int *status)

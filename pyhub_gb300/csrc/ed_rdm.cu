@@ -176,8 +176,8 @@ __global__ void __launch_bounds__(256) rdm_uphop_kernel(const T *__restrict__ br
             double s = 0.0;
             for (int e = e0 + lane; e < e1; e += 32) {
                 const int2 en = __ldg(a.upl_ent + e);
-                const double v = (double)bs[en.x] * (double)ks[en.y & 0x7fffffff];
-                s += (en.y < 0) ? -v : v;
+                const double b = (double)bs[en.x];
+                s = fma((en.y < 0) ? -b : b, (double)ks[en.y & 0x7fffffff], s);   // one FP64 op per entry
             }
             s = warp_sum(s);
             if (lane == 0) acc[q] += s;
@@ -232,8 +232,8 @@ __global__ void __launch_bounds__(256) rdm_cross_kernel(const T *__restrict__ br
                 double s = 0.0;
                 for (int e = e0 + lane; e < e1; e += 32) {
                     const int2 en = __ldg(a.upl_ent + e);
-                    const double v = (double)bs[en.x] * (double)__ldg(k2 + (en.y & 0x7fffffff));
-                    s += (en.y < 0) ? -v : v;
+                    const double b = (double)bs[en.x];
+                    s = fma((en.y < 0) ? -b : b, (double)__ldg(k2 + (en.y & 0x7fffffff)), s);
                 }
                 s = warp_sum(s);
                 if (lane == 0) acc[2 * q + 1] -= (__popc(sd & btw) & 1) ? -s : s;
@@ -244,7 +244,8 @@ __global__ void __launch_bounds__(256) rdm_cross_kernel(const T *__restrict__ br
     for (int i = threadIdx.x; i < 2 * a.npairs; i += blockDim.x) partials[(int64_t)blockIdx.x * 2 * a.npairs + i] = acc[i];
 }
 
-static constexpr int kRdmBlocks = 256;
+static constexpr int kRdmBlocks = 256;   // partial rows of the Heisenberg passes (3 x 2 sums per pair each)
+static constexpr int kRdmRows = 1024;    // partial rows of each Hubbard part (4 and 2 sums per pair)
 
 template <typename T>
 static int rdm_hub(ed_sector *s, cudaStream_t st, int64_t ld, const T *bra, const T *ket, int npairs,
@@ -258,18 +259,23 @@ static int rdm_hub(ed_sector *s, cudaStream_t st, int64_t ld, const T *bra, cons
     a.dpl_off = s->dn.pl_off; a.dpl_ent = s->dn.pl_ent;
     a.npairs = npairs;
     for (int p = 0; p < npairs; ++p) { a.pj[p] = (int8_t)pairs[2 * p]; a.pk[p] = (int8_t)pairs[2 * p + 1]; }
-    int dev = 0, maxsm = 0;
+    int dev = 0, maxsm = 0, nsm = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    // ---- row-local sums: diagonal tiles then up-hop rows, their partials stacked for one reduction
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    nsm = std::max(nsm, 1);
+    // ---- row-local sums: diagonal tiles then up-hop rows, their partials stacked for one reduction.
+    // Each pass gets a few CTAs per SM (both are bound by the FP64 pipe of every SM they occupy);
+    // the partial rows of the two together stay within kRdmRows.
+    constexpr int kMaxTiles = kRdmRows / 2;
     const int ncx = (int)((s->nsup + kDiagThreads - 1) / kDiagThreads);
-    int nry = (int)std::max<int64_t>(1, std::min<int64_t>(s->nsdn, 128 / std::max(ncx, 1)));
-    if (ncx * nry > 128) nry = std::max(1, 128 / ncx);
+    if (ncx > kMaxTiles) { set_error("rows of %lld strings are too long for the RDM tiles", (long long)s->nsup); return ED_ERR_RANGE; }
+    int nry = (int)std::max<int64_t>(1, std::min<int64_t>(s->nsdn, std::min(2 * nsm, kMaxTiles) / ncx));
+    if (ncx * nry > kMaxTiles) nry = std::max(1, kMaxTiles / ncx);
     const int nbA = ncx * nry;
-    if (nbA > 128) { set_error("rows of %lld strings are too long for the RDM tiles", (long long)s->nsup); return ED_ERR_RANGE; }
     const bool small = s->norb <= 16;
     const size_t smemA = (size_t)((small ? 16 : 32) + 1) * kDiagThreads * sizeof(double) + (size_t)npairs * sizeof(double);
-    const int nbB = (int)std::min<int64_t>(s->nsdn, kRdmBlocks - nbA);
+    const int nbB = (int)std::min<int64_t>(s->nsdn, std::min(4 * nsm, kRdmRows - nbA));
     const size_t smemB = (size_t)npairs * sizeof(double) + (size_t)(bra == ket ? 1 : 2) * s->nsup * sizeof(T);
     if (smemA > (size_t)maxsm || smemB > (size_t)maxsm) {
         set_error("RDM pass of %lld strings exceeds shared memory", (long long)s->nsup);
@@ -296,8 +302,8 @@ static int rdm_hub(ed_sector *s, cudaStream_t st, int64_t ld, const T *bra, cons
         const size_t smem2 = (size_t)2 * npairs * sizeof(double) + (size_t)s->nsup * sizeof(T) + 16;
         if (smem2 > (size_t)maxsm) { set_error("cross-row RDM pass exceeds shared memory"); return ED_ERR_RANGE; }
         ED_CHECK_CUDA(cudaFuncSetAttribute(rdm_cross_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
-        const int nbC = (int)std::min<int64_t>(s->nsdn, kRdmBlocks);
-        double *part2 = scratch + (int64_t)kRdmBlocks * 4 * npairs;
+        const int nbC = (int)std::min<int64_t>(s->nsdn, std::min(4 * nsm, kRdmRows));
+        double *part2 = scratch + (int64_t)kRdmRows * 4 * npairs;
         rdm_cross_kernel<T><<<nbC, 256, smem2, st>>>(bra, ket, a, want_dn, want_sx, part2);
         ED_CHECK_LAUNCH();
         rc = launch_reduce(part2, nbC, 2 * npairs, out + 4 * npairs, st);
@@ -315,7 +321,10 @@ using namespace ed;
 extern "C" int64_t ed_rdm_scratch_bytes(int npairs)
 {
     if (npairs < 1) npairs = 1;
-    return (int64_t)kRdmBlocks * kRdmQ * npairs * (int64_t)sizeof(double) + 4096;
+    // Hubbard: kRdmRows rows of 4 sums and kRdmRows rows of 2 sums per pair; the Heisenberg
+    // passes' 3 * kRdmBlocks rows of 2 sums fit in the same space
+    static_assert(3 * kRdmBlocks * 2 <= kRdmRows * kRdmQ, "Heisenberg partials exceed the RDM scratch");
+    return (int64_t)kRdmRows * kRdmQ * npairs * (int64_t)sizeof(double) + 4096;
 }
 
 extern "C" int ed_rdm(ed_sector *s, void *stream, int dtype, int64_t ld, const void *bra, const void *ket,
@@ -341,6 +350,6 @@ extern "C" int ed_rdm(ed_sector *s, void *stream, int dtype, int64_t ld, const v
         return rdm_hub<double>(s, st, ld, (const double *)bra, (const double *)ket, npairs, pairs, flags, out,
                                (double *)scratch);
     }
-    // partials [blocks][npairs][2] fit in the kRdmBlocks*kRdmQ*npairs doubles of ed_rdm_scratch_bytes
+    // partials [<= 3 * kRdmBlocks][npairs][2] fit in the kRdmRows*kRdmQ*npairs doubles of ed_rdm_scratch_bytes
     return heis_struct_rdm(s, st, dtype, bra, ket, npairs, pairs, out, (double *)scratch, kRdmBlocks);
 }

@@ -327,6 +327,43 @@ def test_persistent_run_is_bit_identical(edlib, dtype, keep, rows):
     assert torch.equal(per.alpha, a0) and torch.equal(per.beta, b0)
 
 
+def test_persistent_wait_limit_sets_status(edlib):
+    """An instance whose first H*v phase never completes: the CTAs waiting on
+    it give up after the wait limit, the run stops with status 1 well within
+    the call, and the next run on the same context completes with the
+    four-launch alpha/beta."""
+    import time
+
+    import torch
+    from pyhub_gb300.core import greens_batched as GB
+    t, U, src, gs, secs, inst, _ = _setup(edlib, nsteps=25, dtype="f32")
+    ref = GB.BatchedLanczos(secs, 25, dtype=torch.float32, rows=8)
+    per = GB.BatchedLanczos(secs, 25, dtype=torch.float32, rows=8, persistent=True)
+    x0 = torch.rand(ref.batch.total, dtype=torch.float32, device="cuda")
+    for i, s in enumerate(secs):
+        ref.batch.view(x0, i).view(s.nsdn, -1)[:, s.nsup:] = 0
+    ref.x0.copy_(x0)
+    per.x0.copy_(x0)
+    ref.run()
+    torch.cuda.synchronize()
+    per.batch.persistent_watchdog(0.25, stall_instance=len(secs) // 2)
+    t0 = time.perf_counter()
+    per.run()
+    torch.cuda.synchronize()
+    took = time.perf_counter() - t0
+    assert per.batch.persistent_status(per.scratch) == 1
+    assert took < 5.0
+    per.batch.persistent_watchdog(10.0, -1)
+    per.run()
+    torch.cuda.synchronize()
+    assert per.batch.persistent_status(per.scratch) == 0
+    assert torch.equal(ref.alpha, per.alpha) and torch.equal(ref.beta, per.beta)
+    with pytest.raises(RuntimeError):
+        per.batch.persistent_watchdog(0.0)
+    with pytest.raises(RuntimeError):
+        per.batch.persistent_watchdog(1.0, stall_instance=len(secs))
+
+
 def test_persistent_run_full_size_clusters(edlib):
     """Two C4 clusters' particle/hole instances (sectors of 392,040 to
     853,776 elements, mixed shapes): persistent and four-launch runs agree

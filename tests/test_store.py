@@ -136,3 +136,13 @@ def test_restore_refuses_another_hamiltonian(tmp_path):
         FermiHubbard(4, 3, 2, a.t_matrix, U=4.0, T=0.5).restore(path)
     with pytest.raises(RuntimeError, match="kernel"):
         FermiHubbard(4, 2, 2, a.t_matrix, U=4.0).save(str(tmp_path / "none"))
+
+
+def test_nvtx_range_without_a_device():
+    from pyhub_gb300.trace import nvtx
+    with nvtx("pyhub.test"):
+        x = 1
+    assert x == 1
+    with pytest.raises(KeyError):
+        with nvtx("pyhub.test"):
+            raise KeyError("propagates")
