@@ -31,7 +31,7 @@ from . import lanczos as LZ
 from . import store
 from .basis import Basis
 from .reduced_quantities import (GreenFunction, StaticQuantities, all_pairs, assemble_heisenberg,
-                                 assemble_hubbard)
+                                 assemble_hubbard, lower_pairs, scatter_pairs)
 
 F32_TOL14 = float(np.float32(1e-14))
 F32_TOL8 = float(np.float32(1e-8))
@@ -285,8 +285,9 @@ class CoreSolver(Basis, GreenFunction, StaticQuantities):
             psi = self._state_device(b)
             if self._kind == _capi.ED_HUBBARD:
                 flags = 2 | (1 if self.nup[0] != self.ndown[0] else 0)
-                raw, _ = sec.rdm_raw(psi, pairs=all_pairs(N), flags=flags)
-                gu, gd, n_, sm = assemble_hubbard(raw, N, self.nup[0], self.ndown[0])
+                pairs = lower_pairs(N)   # K <= J, mirrored by the assembly, as the reference does
+                raw, _ = sec.rdm_raw(psi, pairs=pairs, flags=flags)
+                gu, gd, n_, sm = assemble_hubbard(scatter_pairs(raw, pairs, N), N, self.nup[0], self.ndown[0])
                 dm_up[b], dm_dn[b], ni[b], sisj[b] = gu, gd, n_, sm
                 if two_body:
                     vals, _ = sec.dbl_occ(psi, quads=quads)

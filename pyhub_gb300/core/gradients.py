@@ -31,6 +31,7 @@ import numpy as np
 
 from .. import _capi
 from . import lanczos as LZ
+from .reduced_quantities import all_pairs, lower_pairs, scatter_pairs
 
 
 def _torch():
@@ -115,13 +116,20 @@ def solve(params: HubbardParams, theta, nup: int, ndn: int, mode: str = "f64", s
 
 
 def one_rdm(sec, psi, norb: int, ket=None) -> dict:
-    pairs = [(J, K) for J in range(1, norb + 1) for K in range(1, norb + 1)]
+    # <psi|c+_J c_K|psi> of a real state is symmetric: the pairs K <= J, mirrored (as ONE_RDM
+    # forms it); a transition density <bra|.|ket> needs both orders and is symmetrised
+    pairs = lower_pairs(norb) if ket is None else all_pairs(norb)
     raw, _ = sec.rdm_raw(psi, ket, pairs=pairs, flags=1)
-    q = raw.reshape(norb, norb, 6)
+    q = scatter_pairs(raw, pairs, norb).reshape(norb, norb, 6)
     # <c^+_J c_K> sums: q[J-1][K-1][0] for J != K (hop K -> J), diagonal <n_J>
     gu = q[:, :, 0].copy()
     gd = q[:, :, 4].copy()
     gd[np.diag_indices(norb)] = q[np.arange(norb), np.arange(norb), 2]
+    if ket is None:
+        low = np.tril_indices(norb, -1)
+        gu.T[low] = gu[low]
+        gd.T[low] = gd[low]
+        return {"up": gu, "down": gd}
     return {"up": 0.5 * (gu + gu.T), "down": 0.5 * (gd + gd.T)}
 
 

@@ -20,8 +20,24 @@ def all_pairs(norb: int):
     return [(J, K) for J in range(1, norb + 1) for K in range(1, norb + 1)]
 
 
+def lower_pairs(norb: int):
+    """The pairs K <= J that ONE_RDM and J_SPIN evaluate before mirroring
+    (static_rq.f90:161-241, 331-393)."""
+    return [(J, K) for J in range(1, norb + 1) for K in range(1, J + 1)]
+
+
+def scatter_pairs(raw: np.ndarray, pairs, norb: int) -> np.ndarray:
+    """Raw per-pair sums of a pair list placed in the [norb*norb, nq] layout of
+    all_pairs (rows of pairs that were not evaluated are zero)."""
+    full = np.zeros((norb * norb, raw.shape[1]))
+    idx = [(J - 1) * norb + (K - 1) for J, K in pairs]
+    full[idx] = raw
+    return full
+
+
 def assemble_hubbard(raw: np.ndarray, norb: int, nup: int, ndn: int):
-    """Reference symmetrisation of the raw ed_rdm sums over all pairs:
+    """Reference symmetrisation of the raw ed_rdm sums in the all_pairs layout
+    (only the rows K <= J are read):
     DENS_MAT(J,K) computed for K<=J and mirrored, the down matrix copied from
     the up one when N_up == N_down (static_rq.f90:161-241), NI from the local
     branch (:307-316), SMATRIX(J,K) for K<=J mirrored (:331-393).

@@ -305,3 +305,38 @@ def test_long_lanczos_stays_bounded(edlib, dt):
                       np.random.default_rng(0).uniform(-0.5, 0.5, osec.dim), 600, 1e-12)["eigenvalues"][0]
     assert abs(r.ritz[0] - e) < (1e-5 if dt == "f32" else 1e-10)
     r.release()
+
+
+@pytest.mark.parametrize("case", [(7, 3, 2), (8, 4, 4), (9, 4, 5), (16, 8, 8)])
+def test_padded_and_reference_layouts_bit_identical(edlib, case):
+    """FP32 product in the padded layout (16-byte rows: the slab pass loads
+    four columns per lane) and in the reference layout (rows of C(n,k) = 2 mod 4
+    entries: one column per lane).  Both sum the same terms in the same order,
+    so the products agree bit for bit; the fused dots agree to rounding of
+    FP32 partial sums grouped differently (4x4 included, D = 165,636,900)."""
+    import torch
+    norb, nu, nd = case
+    if norb == 16:
+        t = O.square_pbc(4, 4)
+        U = np.full(16, 8.0)
+    else:
+        t, U, _ = _params(norb, 7 * norb + nu)
+    sec = edlib.Sector(norb, nu, nd, edlib.ED_HUBBARD, t=t, U=U)
+    assert sec.nsup % 4 != 0
+    g = torch.Generator(device="cuda")
+    g.manual_seed(11)
+    xr = torch.rand(sec.dim, generator=g, device="cuda", dtype=torch.float32) - 0.5
+    yr = torch.full_like(xr, float("nan"))
+    sc = torch.empty(edlib.scratch_bytes(sec.n, 1) // 8 + 1, dtype=torch.float64, device="cuda")
+    d_ref = torch.zeros(2, dtype=torch.float64, device="cuda")
+    sec.hv(xr, yr, dots=d_ref, scratch=sc, ld=sec.nsup)          # reference layout
+    xi = sec.from_ref(xr)
+    yi = torch.zeros_like(xi)
+    d_pad = torch.zeros(2, dtype=torch.float64, device="cuda")
+    sec.hv(xi, yi, dots=d_pad, scratch=sc)                       # padded layout
+    torch.cuda.synchronize()
+    assert torch.equal(sec.to_ref(yi), yr)
+    a, b = d_ref.cpu().numpy(), d_pad.cpu().numpy()
+    assert np.all(np.abs(a - b) <= 1e-5 * max(np.abs(a).max(), 1.0)), (a, b)
+    del xr, yr, xi, yi
+    torch.cuda.empty_cache()
