@@ -518,6 +518,17 @@ def self_energy_ref(Vk, ek, e, wgt, spgf: dict, w: float, eta: float, same_spin:
     return out
 
 
+def qpw_ref(Vk, ek, e, wgt, spgf: dict, mu: float, same_spin: bool, nb_sites: int) -> np.ndarray:
+    """GreenFunction.qpw (reduced_quantities.py:168-169): pinv(1 - Re S'(mu))
+    of the up self-energy at eta = 1e-4, S' by the published three-point
+    central difference that scipy.misc.derivative(order=3) applies,
+    (S(mu + dx) - S(mu - dx)) / (2 dx), dx = 1e-6."""
+    dx = 1.e-6
+    sp = self_energy_ref(Vk, ek, e, wgt, spgf, mu + dx, 1.e-4, same_spin)["up"]
+    sm = self_energy_ref(Vk, ek, e, wgt, spgf, mu - dx, 1.e-4, same_spin)["up"]
+    return np.linalg.pinv(np.identity(nb_sites) - np.real((sp - sm) / (2 * dx)))
+
+
 def lanczos_tridiag(hv, phi: np.ndarray, nsteps: int, reorth: bool = True):
     """Lanczos coefficients (a_n, b_n) from the normalised start phi, used for
     the continued fraction <phi|(z-H)^-1|phi>.  Full reorthogonalisation in

@@ -267,6 +267,25 @@ class GreenFunction:
             out[s] = (wts_t[None] / den).sum(dim=-1)
         return out
 
+    @property
+    def galitskii_migdal(self):
+        """Left unimplemented by the reference (reduced_quantities.py:164-166): None."""
+        return None
+
+    @property
+    def qpw(self) -> np.ndarray:
+        """Quasi-particle weight (reduced_quantities.py:168-169):
+        pinv(1 - Re dSigma_up/dw) at w = mu['up'], the derivative taken as the
+        reference takes it, scipy.misc.derivative(order=3, dx=1e-6): the
+        three-point central difference (Sigma(mu+dx) - Sigma(mu-dx)) / (2 dx),
+        of the self-energy at eta = 1e-4.  Both frequencies are evaluated in
+        one batched self_energy call."""
+        dx = 1.e-6
+        mu = float(self.mu["up"])
+        sig = self.self_energy(np.array([mu - dx, mu + dx]), eta=0.0001)["up"]   # [j][i][k]
+        d = (sig[:, :, 1] - sig[:, :, 0]).T / (2.0 * dx)
+        return np.linalg.pinv(np.identity(self.nb_sites) - np.real(d))
+
     def self_energy(self, w, eta=0.05):
         """Sigma(w) = pinv(G0(w)) - pinv(G(w)) (reduced_quantities.py:134-161):
         G0 from the hopping matrix's eigenpairs (ek, Vk), G from the uncleaned

@@ -322,3 +322,25 @@ def test_self_energy_matches_reference_formula(edlib, nu, nd):
             assert np.abs(G[s][k].cpu().numpy() - Gr).max() <= 1e-9 * np.abs(Gr).max(), (s, k)
             got = S[s][:, :, k].T
             assert np.abs(got - ref[s]).max() <= 1e-7 * np.abs(ref[s]).max(), (s, k, np.abs(got - ref[s]).max())
+    # the quasi-particle weight at the chemical potential: mu from the lowest N+-1 energies that the
+    # start vectors reach (poles of nonzero weight), as ip and ae take them
+    def lowest(part):
+        w = np.sum(sp[f"Q_{part}_up"][:, :, 0] ** 2, axis=0)
+        return float(np.min(sp[f"positions_{part}_up"][w > 1e-12]))
+    mu = 0.5 * ((lowest("greater") - e[0]) + (e[0] - lowest("lesser")))
+    assert abs(fh.mu["up"] - mu) < 1e-8
+    # 1 - Re Sigma'(mu) by the central difference, then its pseudo-inverse (compared where it is
+    # well conditioned: the pseudo-inverse amplifies differences by the condition number)
+    dx = 1.e-6
+    d_ref = np.identity(norb) - np.real(
+        (O.self_energy_ref(Vk, ek, e[:1], [1.0], sp, mu + dx, 1e-4, nu == nd)["up"]
+         - O.self_energy_ref(Vk, ek, e[:1], [1.0], sp, mu - dx, 1e-4, nu == nd)["up"]) / (2 * dx))
+    so = fh.self_energy(np.array([fh.mu["up"] - dx, fh.mu["up"] + dx]), eta=1e-4)["up"]
+    d_got = np.identity(norb) - np.real((so[:, :, 1] - so[:, :, 0]).T / (2 * dx))
+    assert np.abs(d_got - d_ref).max() <= 1e-4 * np.abs(d_ref).max(), np.abs(d_got - d_ref).max()
+    z_ref = O.qpw_ref(Vk, ek, e[:1], [1.0], sp, mu, nu == nd, norb)
+    assert np.allclose(z_ref, np.linalg.pinv(d_ref))
+    if np.linalg.cond(d_ref) < 1e6:
+        z = fh.qpw
+        assert np.abs(z - z_ref).max() <= 1e-3 * max(1.0, np.abs(z_ref).max()), np.abs(z - z_ref).max()
+    assert fh.galitskii_migdal is None
