@@ -45,6 +45,7 @@ enum { ED_HUBBARD = 0, ED_HEISENBERG = 1 };
 enum { ED_F32 = 0, ED_F64 = 1 };
 
 typedef struct ed_sector ed_sector;
+typedef struct ed_opspace ed_opspace;
 
 /* Last error message of the calling thread ("" when none). */
 const char *ed_last_error(void);
@@ -214,6 +215,33 @@ int ed_gf_start_sites(const ed_sector *src, const ed_sector *dst, void *stream, 
  * Vectors of all instances are concatenated: instance i occupies elements
  * [offsets[i], offsets[i] + nsdn_i*ld_i) with ld_i = nsup_i rounded up to 32
  * (the engine's internal row stride). */
+/* ---- generic operator engine (operators.x) ----
+ * The vector space of the reference's Operators: the up strings of every
+ * listed up-particle number (nups[0..nlist_up-1], each block in HILBERT
+ * order, concatenated in list order; compute_operators.f90:8-25 builds BUP
+ * the same way from basis.h5), the same for down; state (d, u) at
+ * d*nsup + u.  No particle number may be listed twice. */
+int ed_opspace_create(int norb, int nlist_up, const int *nups, int nlist_dn, const int *ndns, ed_opspace **out);
+int ed_opspace_dims(const ed_opspace *sp, int64_t *nsup, int64_t *nsdn);
+int ed_opspace_destroy(ed_opspace *sp);
+/* y = sum_t coeff[t] * (O_{t,last} ... O_{t,1}) x, PROGRAM OPERATOR
+ * (compute_operators.f90:28-66): terms with |coeff| <= 1e-14 are skipped; the
+ * factors of term t are ops[5*q .. 5*q+4] for q in [term_off[t],
+ * term_off[t+1]) = {code, site1, spin1, site2, spin2} exactly as the
+ * reference's _write_operator encodes them (_operators.py:420-462; sites
+ * 1-based, spin 1 = up, 2 = down), applied in list order, the first factor
+ * first: 1 C_DAGGER_C (c+_{site1} c_{site2}, spin1; operators.f90:1-59),
+ * 2 NI, 3 identity, 4 NIM1 (1 - n), 5 SZ_OPE, 6 / 7 C_DAGGER_C_UNRES with
+ * site1 on both sides (c+_{up} c_{down} / c+_{down} c_{up}), 9
+ * C_DAGGER_C_UNRES(site1, site2, spin2) (c+ of the other spin at site1,
+ * c_{site2, spin2}), 10 C_DAGGER, 11 C_; code 8 (SISJ) is refused, nothing
+ * in the operator algebra produces it.  Results of a factor outside the
+ * listed particle numbers are dropped, as the Fortran drops them.  x, y
+ * device FP64 [nsup*nsdn]; work device, at least 2*nsup*nsdn doubles; the
+ * term list is host memory, read before anything is enqueued. */
+int ed_ops_apply(const ed_opspace *sp, void *stream, int nterms, const int32_t *term_off, const int32_t *ops,
+                 const double *coeff, const double *x, double *y, double *work, int64_t work_bytes);
+
 typedef struct ed_batch ed_batch;
 int ed_batch_create(int ninst, ed_sector *const *secs, ed_batch **out);
 /* ed_batch_create with the H*v work split chosen by the caller: rows of one

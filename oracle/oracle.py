@@ -529,6 +529,159 @@ def qpw_ref(Vk, ek, e, wgt, spgf: dict, mu: float, same_spin: bool, nb_sites: in
     return np.linalg.pinv(np.identity(nb_sites) - np.real((sp - sm) / (2 * dx)))
 
 
+# ---------------------------------------------------------------- operators.x
+def _ops_site(norb: int, pos: int) -> int:
+    return 1 << (norb - pos)                         # ISHFT(1,NORB+1-POS-1)
+
+
+def _ops_anticom(norb: int, pos: int, state: int) -> float:
+    """ANTICOM (funcmod.f90:29-41): -1 per occupied site among 1..POS-1."""
+    a = 1.0
+    for i2 in range(1, pos):
+        if state & _ops_site(norb, i2):
+            a = -a
+    return a
+
+
+def _ops_kinop(norb: int, state: int, posi: int, posf: int) -> int:
+    """KINOP (funcmod.f90:18-27)."""
+    A, B = _ops_site(norb, posi), _ops_site(norb, posf)
+    new = 0
+    if state & A and not state & B:
+        new = state - A + B
+    if state & A and posi == posf:
+        new = state
+    return new
+
+
+def ops_space(norb: int, nups, ndns):
+    """BUP / BDOWN of PROGRAM OPERATOR (compute_operators.f90:8-25): the
+    strings of every listed particle number, concatenated in list order."""
+    bup = [int(s) for n in nups for s in hilbert(norb, n)]
+    bdn = [int(s) for n in ndns for s in hilbert(norb, n)]
+    return bup, bdn
+
+
+def ops_apply_ref(norb: int, nups, ndns, terms, psi: np.ndarray) -> np.ndarray:
+    """PROGRAM OPERATOR (compute_operators.f90:28-66) with the elementary
+    routines of operators.f90, loop for loop: terms = [(coeff, [(code, site1,
+    spin1, site2, spin2), ...])] as _write_operator encodes them; each term
+    restarts from psi, applies its factors in list order (the first one
+    first) and adds COEFF * result.  The position searches are the Fortran's
+    linear searches over BUP / BDOWN (a dict gives the same first match:
+    the strings of a list are distinct)."""
+    bup, bdn = ops_space(norb, nups, ndns)
+    nsup, nsdn = len(bup), len(bdn)
+    iu = {s: i for i, s in enumerate(bup)}
+    idn = {s: i for i, s in enumerate(bdn)}
+    out = np.zeros(nsup * nsdn)
+    for coeff, ops in terms:
+        if not abs(coeff) > 1e-14:
+            continue
+        v = np.array(psi, dtype=np.float64, copy=True)
+        for code, si, spi, sj, spj in ops:
+            if code in (0, 3):
+                continue
+            w = np.zeros_like(v)
+            if code == 1:                       # C_DAGGER_C(J=si, K=sj, SPIN=spi)  operators.f90:1-59
+                J, K = si, sj
+                if spi == 1:
+                    for i, b in enumerate(bup):
+                        new = _ops_kinop(norb, b, K, J)
+                        if new > 0 and new in iu:
+                            pos = iu[new]
+                            ac = _ops_anticom(norb, K, b) * _ops_anticom(norb, J, new)
+                            for l1 in range(nsdn):
+                                w[l1 * nsup + pos] += ac * v[l1 * nsup + i]
+                else:
+                    for l1, b in enumerate(bdn):
+                        new = _ops_kinop(norb, b, K, J)
+                        if new > 0 and new in idn:
+                            pos = idn[new]
+                            ac = _ops_anticom(norb, K, b) * _ops_anticom(norb, J, new)
+                            for i in range(nsup):
+                                w[pos * nsup + i] += ac * v[l1 * nsup + i]
+            elif code in (2, 4):                # NI / NIM1  operators.f90:150-175, 194-219
+                w = v.copy()
+                keep_occ = code == 2
+                if spi == 1:
+                    for u, b in enumerate(bup):
+                        if bool(b & _ops_site(norb, si)) != keep_occ:
+                            w[u::nsup] = 0.0
+                else:
+                    for d, b in enumerate(bdn):
+                        if bool(b & _ops_site(norb, si)) != keep_occ:
+                            w[d * nsup:(d + 1) * nsup] = 0.0
+            elif code == 5:                     # SZ_OPE  operators.f90:223-248
+                for u, b in enumerate(bup):
+                    if not b & _ops_site(norb, si):
+                        for d in range(nsdn):
+                            w[d * nsup + u] = w[d * nsup + u] + v[d * nsup + u] / 2.0
+                for d, b in enumerate(bdn):
+                    if not b & _ops_site(norb, si):
+                        for u in range(nsup):
+                            w[d * nsup + u] = w[d * nsup + u] - v[d * nsup + u] / 2.0
+            elif code in (6, 7, 9):             # C_DAGGER_C_UNRES(J, K, SPINK)  operators.f90:62-144
+                J = si
+                K = sj if code == 9 else si
+                spink = {6: 2, 7: 1}.get(code, spj)
+                if spink == 1:
+                    for i, b in enumerate(bup):
+                        if b & _ops_site(norb, K):
+                            new = b - _ops_site(norb, K)
+                            if new in iu:
+                                pos = iu[new]
+                                ac = _ops_anticom(norb, K, new)
+                                for l1, bd in enumerate(bdn):
+                                    if not bd & _ops_site(norb, J):
+                                        new2 = bd + _ops_site(norb, J)
+                                        if new2 in idn:
+                                            pos2 = idn[new2]
+                                            ac2 = _ops_anticom(norb, J, new2) * _ops_anticom(norb, 0, bd)
+                                            w[pos2 * nsup + pos] += ac * ac2 * v[l1 * nsup + i]
+                else:
+                    for i, bd in enumerate(bdn):
+                        if bd & _ops_site(norb, K):
+                            new = bd - _ops_site(norb, K)
+                            if new in idn:
+                                pos = idn[new]
+                                ac = _ops_anticom(norb, K, new)
+                                for l1, b in enumerate(bup):
+                                    if not b & _ops_site(norb, J):
+                                        new2 = b + _ops_site(norb, J)
+                                        if new2 in iu:
+                                            pos2 = iu[new2]
+                                            ac2 = _ops_anticom(norb, 0, new) * _ops_anticom(norb, J, new2)
+                                            w[pos * nsup + pos2] += ac * ac2 * v[i * nsup + l1]
+            elif code in (10, 11):              # C_DAGGER / C_  operators.f90:410-523
+                J = si
+                create = code == 10
+                if spi == 1:
+                    for i, b in enumerate(bup):
+                        if bool(b & _ops_site(norb, J)) != create:
+                            new = b + _ops_site(norb, J) if create else b - _ops_site(norb, J)
+                            if new in iu:
+                                pos = iu[new]
+                                ac = _ops_anticom(norb, J, b)
+                                for l2, bd in enumerate(bdn):
+                                    ac2 = _ops_anticom(norb, 0, bd)
+                                    w[l2 * nsup + pos] += ac * ac2 * v[l2 * nsup + i]
+                else:
+                    for i, bd in enumerate(bdn):
+                        if bool(bd & _ops_site(norb, J)) != create:
+                            new = bd + _ops_site(norb, J) if create else bd - _ops_site(norb, J)
+                            if new in idn:
+                                pos = idn[new]
+                                ac = _ops_anticom(norb, J, bd)
+                                for l1 in range(nsup):
+                                    w[pos * nsup + l1] += ac * v[i * nsup + l1]
+            else:
+                raise NotImplementedError(f"operator code {code}")
+            v = w
+        out = out + coeff * v
+    return out
+
+
 def lanczos_tridiag(hv, phi: np.ndarray, nsteps: int, reorth: bool = True):
     """Lanczos coefficients (a_n, b_n) from the normalised start phi, used for
     the continued fraction <phi|(z-H)^-1|phi>.  Full reorthogonalisation in

@@ -28,6 +28,10 @@ _SIGS = {
     "ed_rank": (_I64, [_I, _I, ctypes.c_uint32]),
     "ed_sector_create": (_I, [_I, _I, _I, _I, _P, _P, _P, ctypes.POINTER(_P)]),
     "ed_sector_destroy": (_I, [_P]),
+    "ed_opspace_create": (_I, [_I, _I, _P, _I, _P, ctypes.POINTER(_P)]),
+    "ed_opspace_dims": (_I, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
+    "ed_opspace_destroy": (_I, [_P]),
+    "ed_ops_apply": (_I, [_P, _P, _I, _P, _P, _P, _P, _P, _P, _I64]),
     "ed_sector_dims": (_I, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
     "ed_sector_strings": (_I, [_P, _P, _P]),
     "ed_sector_nnz": (_I, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
@@ -302,6 +306,62 @@ class Sector:
         if self.kind != ED_HUBBARD:
             return self.dim
         return (self.nsdn - 1) * int(ld) + self.nsup if self.nsdn > 0 else 0
+
+
+class OpSpace:
+    """ed_opspace: the vector space of the generic operator engine (every
+    listed up-particle number times every listed down-particle number,
+    state (d, u) at d*nsup + u)."""
+
+    def __init__(self, norb: int, nups, ndns):
+        self.norb = int(norb)
+        nu = np.ascontiguousarray(np.asarray(list(nups), dtype=np.int32))
+        nd = np.ascontiguousarray(np.asarray(list(ndns), dtype=np.int32))
+        h = _P()
+        check("ed_opspace_create", lib().ed_opspace_create(self.norb, len(nu), nu.ctypes.data, len(nd),
+                                                           nd.ctypes.data, ctypes.byref(h)))
+        self._h = h
+        a, b = _I64(), _I64()
+        check("ed_opspace_dims", lib().ed_opspace_dims(h, ctypes.byref(a), ctypes.byref(b)))
+        self.nsup, self.nsdn = a.value, b.value
+        self.nstates = self.nsup * self.nsdn
+        self._work = None
+
+    def apply(self, terms, x, y=None, stream=None):
+        """y = sum_t c_t (factors of t applied in list order) x.  terms:
+        [(coeff, [(code, site1, spin1, site2, spin2), ...]), ...] as the
+        reference's operator file encodes them; x, y device FP64 [nstates]."""
+        import torch
+        if x.dtype != torch.float64:
+            raise TypeError("the operator engine works in FP64")
+        if y is None:
+            y = torch.empty(self.nstates, dtype=torch.float64, device=x.device)
+        if self._work is None or self._work.device != x.device:
+            self._work = torch.empty(2 * max(self.nstates, 1), dtype=torch.float64, device=x.device)
+        off = np.zeros(len(terms) + 1, dtype=np.int32)
+        flat, coeff = [], np.zeros(max(len(terms), 1), dtype=np.float64)
+        for t, (c, ops) in enumerate(terms):
+            coeff[t] = float(c)
+            for o in ops:
+                flat.append([int(v) for v in o])
+            off[t + 1] = len(flat)
+        ops_arr = np.ascontiguousarray(np.asarray(flat if flat else [[0] * 5], dtype=np.int32).reshape(-1, 5))
+        wb = self._work.numel() * 8
+        check("ed_ops_apply", lib().ed_ops_apply(self._h, _stream(stream), len(terms), off.ctypes.data,
+                                                 ops_arr.ctypes.data, coeff.ctypes.data, _ptr(x, self.nstates, "x"),
+                                                 _ptr(y, self.nstates, "y"), _ptr(self._work), int(wb)))
+        return y
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().ed_opspace_destroy(self._h)
+            self._h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Batch:

@@ -1,28 +1,30 @@
-"""Operator algebra with the reference's API (pyhub/core/_operators.py:10-365),
-evaluated on the GPU when the operator has Hubbard form.
+"""Operator algebra with the reference's API (pyhub/core/_operators.py:10-705),
+evaluated on the GPU.
 
 The reference keeps an operator as a sum of products of elementary
-operators (c_dagger_c, n, 1_n, sz, id., ...) and applies it to a vector by
-writing the term list and the vector to operators.h5 and running the Fortran
-program operators.x once per product (`__call__`, :148-205; `to_matrix`,
-:254-281; `lanczos`, :283-322).  Here the same term list is kept in memory
-and recognised:
+operators (c_dagger_c, c_dagger, c, n, 1_n, sz, splus, sminus, id.) and
+applies it to a vector by writing the term list and the vector to
+operators.h5 and running the Fortran program operators.x
+(`__call__`, :145-205; `to_matrix`, :254-281; `lanczos`, :283-322).  Here the
+same term list is kept in memory and applied on the device:
 
-* Hubbard form -- sums of c^+_{i s} c_{j s} (both spins with the same
-  coefficient matrix), n_{i s} and n_{i up} n_{i down} terms and the
-  identity -- is a sector of the engine: ``@``, ``avg``, ``to_matrix`` and
-  ``lanczos`` run the GPU H*v of a sector built from the recognised
-  (t, U).  operators.x applies c^+_J c_K with the same KINOP/ANTICOM signs
-  and the same (d-1)*NSUP+u index as HPROD (operators.f90:1-60), so the
-  results are the reference's.
-* One-body terms of either spin, densities, n_{i up} n_{i down} and the
-  spin correlation sisj((i,),(j,)) built by pyhub.tools.operators.sisj are
-  evaluated by ``avg`` through the fused RDM kernel (ed_rdm).
-
-Other products (c_dagger, c, splus, sminus, operators mixing sectors) need
-the generic engine, which is not built: they raise NotImplementedError, as
-does a basis that holds more than one (N_up, N_down) sector or a selection
-of states.
+* Hubbard form on one (N_up, N_down) sector -- sums of c^+_{i s} c_{j s}
+  (both spins with the same coefficient matrix), n_{i s} and
+  n_{i up} n_{i down} terms and the identity -- runs as the H*v of a sector
+  built from the recognised (t, U).  operators.x applies c^+_J c_K with the
+  same KINOP/ANTICOM signs and the same (d-1)*NSUP+u index as HPROD
+  (operators.f90:1-59), so the results are the reference's.
+* Everything else -- any product of the elementary operators, on a basis of
+  several listed particle numbers or on a selection of its states -- runs on
+  the generic operator engine (ed_ops_apply), which restates operators.x
+  routine by routine: the factors of a product act in list order, the first
+  one first, and a factor whose result leaves the listed particle numbers
+  drops it, as the Fortran does.  Its `sz` element is SZ_OPE
+  (operators.f90:223-248), which multiplies by (n_down - n_up)/2; products
+  sz*sz, as sisj builds them, are the usual S^z_i S^z_j.
+* Expectation values of one-body terms of either spin, densities,
+  n_{i up} n_{i down} and the spin correlation sisj((i,),(j,)) on one sector
+  go through the fused RDM kernel (ed_rdm).
 """
 from __future__ import annotations
 
@@ -89,7 +91,7 @@ class Operators(Basis):
             mul.elem_index = self.elem_index
             mul.str_index = self.str_index
             if not self.op2write:
-                mul.set_basis(Basis(self.nb_sites, self.hilbert, self.order))
+                mul.set_basis(Basis(self.nb_sites, self.hilbert, self.order), selected=self.selected)
         return mul
 
     def __rmul__(self, other):
@@ -108,6 +110,142 @@ class Operators(Basis):
 
     def __rmatmul__(self, other):
         return self.__call__(other.conj())
+
+    def __rtruediv__(self, other):
+        # the reference forwards to a __rdiv__ it does not define (_operators.py:127-128)
+        raise TypeError("a number cannot be divided by an operator")
+
+    def __req__(self, other):
+        return self.__eq__(other)
+
+    def __iter__(self):
+        """Each term as its own operator: coeff * the product of its elements
+        (_operators.py:238-242)."""
+        iter_op = []
+        for i, coeff in enumerate(self.coeff):
+            iter_op.append(coeff * self.__multiplemul__([_operator_from_string(st, elem) for st, elem in
+                                                         zip(self.str_index[i], self.elem_index[i])]))
+        return iter_op.__iter__()
+
+    def __multiplemul__(self, other):
+        mul = Operators._idt()
+        for o in other:
+            mul *= o
+        return mul
+
+    def __getitem__(self, index):
+        """The operator on a selection of basis states (_operators.py:131-147):
+        vectors then hold the selected states' components, and products are
+        the reference's: the input is zero outside the selection and the
+        output is read on it."""
+        if isinstance(index, (list, np.ndarray)):
+            sel = np.asarray(index, dtype=int)
+            other = Operators.empty_operator()
+            other.coeff, other.elem_index, other.str_index = self.coeff, self.elem_index, self.str_index
+            other.set_basis(Basis(self.nb_sites, self.hilbert, self.order), selected=sel)
+            return other
+        return None
+
+    def __delitem__(self):
+        # the reference deletes the operator's group of operators.h5 (_operators.py:251-253); nothing is
+        # stored here
+        return None
+
+    # ------------------------------------------------------------ comparisons with a number
+    def _compare(self, other, op):
+        """[op(<s|O|s>, other) for every basis state s] in the reference's order:
+        the selected states, or every up string for every down string
+        (_operators.py:555-705)."""
+        if not isinstance(other, (float, int)):
+            raise TypeError(f"an operator compares with a number, not {type(other)}")
+        self._check_basis()
+        diag = self._diagonal()
+        if self.selected is None:
+            # the reference loops posu outer, posd inner; the diagonal is in d*nsup + u order
+            diag = diag.reshape(self.nsdown, self.nsup).T.reshape(-1)
+        return [bool(op(v, other)) for v in diag]
+
+    def __eq__(self, other):
+        return self._compare(other, lambda v, o: np.isclose(v, o))
+
+    def __ne__(self, other):
+        return [not e for e in self.__eq__(other)]
+
+    def __ge__(self, other):
+        return self._compare(other, lambda v, o: v >= o)
+
+    def __gt__(self, other):
+        return self._compare(other, lambda v, o: v > o)
+
+    def __le__(self, other):
+        return self._compare(other, lambda v, o: v <= o)
+
+    def __lt__(self, other):
+        return self._compare(other, lambda v, o: v < o)
+
+    __hash__ = None
+
+    # ------------------------------------------------------------ file bookkeeping of the reference
+    @property
+    def filename_operators(self):
+        return "operators.h5"
+
+    @property
+    def index_str(self):
+        return str(getattr(self, "_index", 1)).rjust(6, "0")
+
+    @property
+    def file_size(self):
+        """Size of the reference's operators.h5; nothing is written here."""
+        return 0.0
+
+    def _write_operator(self, max_len_ope=40):
+        # the reference writes the term list to operators.h5 (_operators.py:395-462); here the list is
+        # encoded per product (_encode)
+        self.op2write = False
+        self.max_len_ope = max_len_ope
+
+    def exec_operators(self):
+        # the reference runs operators.x (_operators.py:208-222); products run in process
+        self._check_basis()
+
+    def _set_basis_elem(self, posu, posd, up, down):
+        # the reference writes one basis element to operators.h5 for the basis-element mode; the
+        # comparisons and bit_repr take the diagonal directly
+        return None
+
+    @property
+    def T(self):
+        # unimplemented in the reference (_operators.py:380-382): None
+        return None
+
+    @property
+    def dagger(self):
+        return self.T
+
+    def bit_repr(self):
+        """The basis states (the selected ones when there is a selection) with
+        <s|O|s>, in the reference's layout (_operators.py:474-508)."""
+        self._check_basis()
+        select = self.selected if isinstance(self.selected, (list, np.ndarray)) else list(range(self.nstates))
+        diag = self._diagonal()
+        string = '-' * (3 * (self.nb_sites + 4)) + '\n'
+        string += 'empty        : 0\nuparrow      : 1\ndownarrow    :-1\nupdoawnarrow : 2\n'
+        string += '-' * (3 * (self.nb_sites + 4)) + '\n'
+        string += 'index | bit' + ' ' * (3 * (self.nb_sites - 1) - 1) + ' | <H> ' + '\n'
+        string += '------|----' + '-' * (3 * (self.nb_sites - 1) - 1) + '-|-----' + '\n'
+        for k, index in enumerate(self.basis[select]):
+            up, down = self.decompose(int(index))
+            string += "{:4d}  |".format(int(index))
+            for i in range(self.nb_sites):
+                u, d = (up >> i) & 1, (down >> i) & 1
+                string += ' 0 ' if (not u and not d) else (' 1 ' if (u and not d) else ('-1 ' if (d and not u) else ' 2 '))
+            string += f' | {np.around(diag[k], 4)}' + '\n'
+        return string
+
+    def find_stable_space(self):
+        # "Experimental function, do not use!" in the reference (_operators.py:510-553)
+        raise NotImplementedError("find_stable_space is experimental in the reference and not provided")
 
     @staticmethod
     def empty_operator():
@@ -155,11 +293,82 @@ class Operators(Basis):
     def _check_basis(self):
         if self.op2write:
             raise AttributeError("Set the basis set using self.set_basis(YourBasis:Basis)")
-        if self.selected is not None:
-            raise NotImplementedError("operators on a selection of basis states need the generic operator engine")
-        if len(self.n_up) != 1 or len(self.n_down) != 1:
-            raise NotImplementedError("operators on a basis of several (N_up, N_down) sectors need the generic "
-                                      "operator engine")
+
+    def _one_sector(self) -> bool:
+        """One (N_up, N_down) sector and no selection: the sector fast paths apply."""
+        return self.selected is None and len(self.n_up) == 1 and len(self.n_down) == 1
+
+    # ------------------------------------------------------------ generic engine
+    def _encode(self):
+        """The term list as _write_operator encodes it (_operators.py:420-462):
+        [(coeff, [(code, site1, spin1, site2, spin2), ...])], sites 1-based,
+        spin 1 = up, 2 = down."""
+        codes = {"n": 2, "id.": 3, "1_n": 4, "sz": 5, "splus": 6, "sminus": 7, "sisj": 8, "c_dagger": 10, "c": 11}
+        terms = []
+        for c, strs, elems in zip(self.coeff, self.str_index, self.elem_index):
+            ops = []
+            for st, idx in zip(strs, elems):
+                site1 = site2 = spin1 = spin2 = 0
+                try:
+                    site1 = idx[0][0] + 1
+                    site2 = idx[1][0] + 1
+                except (IndexError, TypeError):
+                    pass
+                try:
+                    spin1 = 1 if _is_up(idx[0][1]) else 2
+                    spin2 = 1 if _is_up(idx[1][1]) else 2
+                except (IndexError, TypeError):
+                    pass
+                if st == "c_dagger_c":
+                    code = 1 if idx[0][1] == idx[1][1] else 9
+                elif st in codes:
+                    code = codes[st]
+                else:
+                    raise NotImplementedError(f"operator element {st!r}")
+                ops.append((code, site1, spin1, site2, spin2))
+            terms.append((float(c), ops))
+        return terms
+
+    def _space(self):
+        key = (self.nb_sites, tuple(int(n) for n in self.n_up), tuple(int(n) for n in self.n_down))
+        sp = getattr(self, "_opspace", None)
+        if sp is None or sp[0] != key:
+            sp = (key, _capi.OpSpace(self.nb_sites, key[1], key[2]))
+            self._opspace = sp
+        return sp[1]
+
+    def _apply_generic_full(self, x_full: np.ndarray) -> np.ndarray:
+        """The operator applied to a vector of the whole space (the reference's
+        psi/input dataset), on the generic engine."""
+        torch = _torch()
+        sp = self._space()
+        x = torch.tensor(np.asarray(x_full, dtype=np.float64), device="cuda")
+        return sp.apply(self._encode(), x).cpu().numpy()
+
+    def _embed(self, psi: np.ndarray) -> np.ndarray:
+        """psi of the selected states placed in the whole space (zeros elsewhere),
+        as __call__ writes its input (_operators.py:155-160)."""
+        if self.selected is None:
+            return np.asarray(psi, dtype=np.float64)
+        full = np.zeros(self.nstates)
+        full[np.asarray(self.selected, dtype=int)] = psi
+        return full
+
+    def _restrict(self, v: np.ndarray) -> np.ndarray:
+        return v if self.selected is None else v[np.asarray(self.selected, dtype=int)]
+
+    def _diagonal(self) -> np.ndarray:
+        """<s|O|s> of every basis state (the selected ones when there is a
+        selection), in basis order: what the reference's basis-element mode
+        returns as avg_value one state at a time (_operators.py:474-508)."""
+        states = np.arange(self.nstates) if self.selected is None else np.asarray(self.selected, dtype=int)
+        out = np.zeros(len(states))
+        e = np.zeros(self.nstates)
+        for k, s_ in enumerate(states):
+            e[s_] = 1.0
+            out[k] = (self._apply_generic_full(e))[s_]
+            e[s_] = 0.0
+        return out
 
     # ------------------------------------------------------------ recognition
     def _classify(self):
@@ -173,7 +382,9 @@ class Operators(Basis):
         for c, strs, elems in zip(self.coeff, self.str_index, self.elem_index):
             if strs == ["id."]:
                 const += c
-            elif strs == ["c_dagger_c"] and _is_up(elems[0][0][1]) == _is_up(elems[0][1][1]):
+            elif strs == ["c_dagger_c"] and elems[0][0][1] == elems[0][1][1]:
+                # same spin label: C_DAGGER_C; different labels (even 'u' and 'up') are the spin-flip
+                # C_DAGGER_C_UNRES, as the reference's operator file encodes them (_operators.py:438-439)
                 (i, s), (j, _) = elems[0]
                 (tu if _is_up(s) else td)[i, j] += c
             elif strs == ["n"]:
@@ -207,6 +418,8 @@ class Operators(Basis):
 
     # ------------------------------------------------------------ application
     def _apply(self, psi: np.ndarray) -> np.ndarray:
+        if not self._one_sector() or self._hubbard() is None:
+            return self._restrict(self._apply_generic_full(self._embed(psi)))
         torch = _torch()
         sec, const = self._sector_of()
         x = sec.from_ref(torch.tensor(np.asarray(psi, dtype=np.float64), device="cuda"))
@@ -231,9 +444,15 @@ class Operators(Basis):
         return self.__call__(psi, avg=True)
 
     def _expectation(self, psi: np.ndarray) -> float:
+        if not self._one_sector():
+            full = self._embed(psi)
+            return float(full @ self._apply_generic_full(full))
         if self._hubbard() is not None:
             return float(psi @ self._apply(psi))
-        return self._rdm_expectation(psi)
+        try:
+            return self._rdm_expectation(psi)
+        except NotImplementedError:
+            return float(psi @ self._restrict(self._apply_generic_full(self._embed(psi))))
 
     def _rdm_expectation(self, psi: np.ndarray) -> float:
         """<psi|O|psi> from the fused RDM pass, for one-body terms of either
@@ -289,8 +508,18 @@ class Operators(Basis):
     @property
     def to_matrix(self):
         """Row i = the operator applied to basis state i (the reference fills
-        H[i,:] that way, _operators.py:267-279)."""
+        H[i,:] that way, _operators.py:254-281); on a selection, the rows and
+        columns of the selected states."""
         self._check_basis()
+        if not self._one_sector() or self._hubbard() is None:
+            states = np.arange(self.nstates) if self.selected is None else np.asarray(self.selected, dtype=int)
+            M = np.zeros((len(states), len(states)))
+            e = np.zeros(self.nstates)
+            for i, s_ in enumerate(states):
+                e[s_] = 1.0
+                M[i, :] = self._apply_generic_full(e)[states]
+                e[s_] = 0.0
+            return M
         n = self.nstates
         M = np.zeros((n, n))
         e = np.zeros(n)
@@ -310,9 +539,10 @@ class Operators(Basis):
         from ..core import lanczos as LZ
         torch = _torch()
         self._check_basis()
+        h = self._hubbard() if self._one_sector() else None
+        if h is None or h[2] != 0.0:
+            return self._lanczos_generic(maxstep, acc_lcz, neigen, init_states)
         sec, const = self._sector_of()
-        if const != 0.0:
-            raise NotImplementedError("lanczos of an operator with an identity term: shift the energies instead")
         v = (np.random.random(self.nb_selected) - 0.5) if not isinstance(init_states, np.ndarray) else init_states
         x = sec.from_ref(torch.tensor(np.asarray(v, dtype=np.float64), device="cuda"))
         rule = _OperatorRule(acc_lcz, neigen)
@@ -321,6 +551,36 @@ class Operators(Basis):
         ek = np.asarray(r.ritz[:neigen])
         psi = np.stack([sec.to_ref(p).cpu().numpy() for p in r.psis], axis=1)
         return ek, psi
+
+    def _lanczos_generic(self, maxstep, acc_lcz, neigen, init_states):
+        """The reference's loop as written (_operators.py:325-364), with the
+        products on the generic engine: plain three-term recurrence, checks
+        every 5 steps on the first neigen Ritz values, at most maxstep - 5
+        steps, psi = V^T Vk[:, :neigen]."""
+        from scipy.linalg import eigh_tridiagonal
+        v = (np.random.random(self.nb_selected) - .5) if not isinstance(init_states, np.ndarray) else init_states
+        v = np.asarray(v, dtype=np.float64)
+        alpha, beta, vecs = [], [np.linalg.norm(v)], []
+        v = v / beta[0]
+        v0 = np.zeros(self.nb_selected)
+        nstep, ek, ekm1 = 0, np.full(neigen, 100.), np.full(neigen, 0.)
+        Vk = np.zeros((0, 0))
+        nadd = 5
+        while nstep < maxstep - nadd and not np.linalg.norm(ek[:neigen] - ekm1) / neigen < acc_lcz:
+            ekm1 = np.copy(ek[:neigen])
+            for _ in range(nadd):
+                vecs.append(v)
+                v2 = self @ v
+                alpha.append(v2 @ v)
+                v2 = v2 - alpha[-1] * v - beta[-1] * v0
+                beta.append(np.linalg.norm(v2))
+                v0 = v
+                v = v2 / beta[-1]
+                nstep += 1
+            ek, Vk = eigh_tridiagonal(alpha, beta[1:nstep], eigvals_only=False, select='a')
+        self._lcz = type("GenericLanczos", (), {"alpha": np.array(alpha), "beta": np.array(beta[1:])})()
+        psi = np.array(vecs[:len(alpha)]).T @ Vk[:, :neigen]
+        return ek[:neigen], psi
 
     @property
     def alpha(self):
@@ -352,6 +612,17 @@ class _OperatorRule:
             self.converged = True
         self.prev = ek
         return self.converged
+
+
+def _operator_from_string(string, args):
+    """One elementary operator from its name and indices (_operators.py:708-733)."""
+    op = Operators(*args)
+    if string not in ("c_dagger_c", "c_dagger", "c", "n", "1_n", "sz", "sisj", "splus", "sminus", "id."):
+        raise ValueError(f"unknown operator element {string!r}")
+    op.str_index = [[string]]
+    if string == "id.":
+        op.elem_index = [[()]]
+    return op
 
 
 def _print_from_string(string, args):

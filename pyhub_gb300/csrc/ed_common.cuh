@@ -153,6 +153,21 @@ int launch_reduce(const double *partials, int nblocks, int m, double *out, cudaS
 
 }  // namespace ed
 
+// Product space of the generic operator engine (operators.x,
+// compute_operators.f90:8-25): the up strings of every listed up-particle
+// number concatenated in list order (each block in HILBERT order), the same
+// for down; state (d, u) at d * nsup + u.
+struct ed_opspace {
+    int norb = 0;
+    int64_t nsup = 0, nsdn = 0;
+    int64_t up_off[ed::kMaxSites + 1];   // first index of the strings with n up particles, -1 when n is not listed
+    int64_t dn_off[ed::kMaxSites + 1];
+    uint32_t *ustr = nullptr, *dstr = nullptr;   // device: the concatenated lists
+    const uint32_t *lut = nullptr;               // device rank table, shared with the sectors
+    void *pool = nullptr;
+    int device = 0;
+};
+
 struct ed_sector {
     int kind = ED_HUBBARD;
     int norb = 0, nup = 0, ndn = 0;

@@ -445,14 +445,14 @@ static int upload_hop(const HostHop &h, int norb, int ne, HopTable &d, TablePool
 static std::mutex g_lut_mu;
 static uint32_t *g_lut[64] = {};
 
-static int build_lut(ed_sector *s)
+static int device_lut(int device, uint32_t **out)
 {
     std::lock_guard<std::mutex> lk(g_lut_mu);
-    if (s->device < 0 || s->device >= 64) {
-        set_error("device %d outside 0..63", s->device);
+    if (device < 0 || device >= 64) {
+        set_error("device %d outside 0..63", device);
         return ED_ERR_RANGE;
     }
-    if (!g_lut[s->device]) {
+    if (!g_lut[device]) {
         // lut[b][c][x] = sum over the set bits q of byte x, taken in increasing
         // order with running index i = c+1, c+2, ..., of C(8b+q, i)
         std::vector<uint32_t> lut(4 * 33 * 256, 0u);
@@ -471,10 +471,18 @@ static int build_lut(ed_sector *s)
         void *base = nullptr;
         const int rc = pool.commit(&base);
         if (rc) return rc;
-        g_lut[s->device] = dev;
+        g_lut[device] = dev;
     }
-    s->lut = g_lut[s->device];
+    *out = g_lut[device];
     return ED_OK;
+}
+
+static int build_lut(ed_sector *s)
+{
+    uint32_t *lut = nullptr;
+    const int rc = device_lut(s->device, &lut);
+    if (rc == ED_OK) s->lut = lut;
+    return rc;
 }
 
 static int build_heis(ed_sector *s, const double *J)
@@ -639,6 +647,69 @@ int ed_sector_create(int norb, int nup, int ndn, int kind, const double *t, cons
         return rc;
     }
     *out = s;
+    return ED_OK;
+}
+
+int ed_opspace_create(int norb, int nlist_up, const int *nups, int nlist_dn, const int *ndns, ed_opspace **out)
+{
+    clear_error();
+    binom_init();
+    ED_REQUIRE(out != nullptr, "out is NULL");
+    *out = nullptr;
+    ED_REQUIRE(norb >= 1 && norb <= kMaxSites, "norb=%d outside 1..%d", norb, kMaxSites);
+    ED_REQUIRE(nlist_up >= 1 && nlist_up <= norb + 1 && nups != nullptr, "up-particle list of %d numbers", nlist_up);
+    ED_REQUIRE(nlist_dn >= 1 && nlist_dn <= norb + 1 && ndns != nullptr, "down-particle list of %d numbers", nlist_dn);
+    std::unique_ptr<ed_opspace> sp(new (std::nothrow) ed_opspace());
+    if (!sp) { set_error("host allocation failed"); return ED_ERR_MEM; }
+    sp->norb = norb;
+    std::vector<uint32_t> strs[2];
+    for (int side = 0; side < 2; ++side) {
+        const int nl = side ? nlist_dn : nlist_up;
+        const int *ns = side ? ndns : nups;
+        int64_t *off = side ? sp->dn_off : sp->up_off;
+        for (int n = 0; n <= kMaxSites; ++n) off[n] = -1;
+        std::vector<uint32_t> &v = strs[side];
+        for (int i = 0; i < nl; ++i) {
+            const int n = ns[i];
+            ED_REQUIRE(n >= 0 && n <= norb, "particle number %d outside 0..%d", n, norb);
+            ED_REQUIRE(off[n] < 0, "particle number %d listed twice", n);
+            const int64_t cnt = binom(norb, n);
+            ED_REQUIRE((int64_t)v.size() + cnt <= INT32_MAX, "string list of more than 2^31 entries");
+            off[n] = (int64_t)v.size();
+            v.resize(v.size() + (size_t)cnt);
+            enumerate_strings(norb, n, v.data() + off[n], cnt);
+        }
+    }
+    sp->nsup = (int64_t)strs[0].size();
+    sp->nsdn = (int64_t)strs[1].size();
+    cudaGetDevice(&sp->device);
+    uint32_t *lut = nullptr;
+    int rc = device_lut(sp->device, &lut);
+    if (rc) return rc;
+    sp->lut = lut;
+    TablePool pool;
+    pool.add(&sp->ustr, strs[0].data(), strs[0].size());
+    pool.add(&sp->dstr, strs[1].data(), strs[1].size());
+    rc = pool.commit(&sp->pool);
+    if (rc) return rc;
+    *out = sp.release();
+    return ED_OK;
+}
+
+int ed_opspace_dims(const ed_opspace *sp, int64_t *nsup, int64_t *nsdn)
+{
+    clear_error();
+    ED_REQUIRE(sp != nullptr, "operator space is NULL");
+    if (nsup) *nsup = sp->nsup;
+    if (nsdn) *nsdn = sp->nsdn;
+    return ED_OK;
+}
+
+int ed_opspace_destroy(ed_opspace *sp)
+{
+    if (!sp) return ED_OK;
+    if (sp->pool) cudaFree(sp->pool);   // the rank table is shared
+    delete sp;
     return ED_OK;
 }
 

@@ -110,9 +110,11 @@ def test_sisj_average(edlib, pair):
     assert abs(op.avg(psi) - ref) <= 1e-12 * max(1.0, abs(ref)), (op.avg(psi), ref)
 
 
-def test_heisenberg_model_average_and_refusals(edlib):
-    """heisenberg(J) on the fermionic basis: <H> through the RDM route; applying
-    it needs the generic engine and is refused, as is a multi-sector basis."""
+def test_heisenberg_model_average_and_application(edlib):
+    """heisenberg(J) on the fermionic basis: <H> through the RDM route, and H psi
+    on the generic operator engine, both against the Jordan-Wigner S_i.S_j; the
+    Hubbard model on a basis of two up-particle numbers on the engine, against
+    the oracle's HPROD of each sector."""
     from pyhub_gb300.core.basis import Basis
     from pyhub_gb300.tools.models import fermi_hubbard, heisenberg
     norb = 4
@@ -125,9 +127,16 @@ def test_heisenberg_model_average_and_refusals(edlib):
     H = heisenberg(J)
     H.set_basis(Basis(norb, (2, 2)))
     assert abs(H.avg(psi) - ref) <= 1e-12 * max(1.0, abs(ref))
-    with pytest.raises(NotImplementedError):
-        H @ psi
-    F = fermi_hubbard(O.ring(norb, -1.0), 2.0)
+    hpsi = sum(J[i, j] * (restrict(S(i, j)) @ psi) for i in range(norb) for j in range(norb))
+    np.testing.assert_allclose(H @ psi, hpsi, rtol=0, atol=1e-12 * max(1.0, np.abs(hpsi).max()))
+    t = O.ring(norb, -1.0)
+    F = fermi_hubbard(t, 2.0)
     F.set_basis(Basis(norb, ([1, 2], [2])))
-    with pytest.raises(NotImplementedError):
-        F @ np.ones(4)
+    x = rng.standard_normal(F.nstates)
+    y = F @ x
+    # the vector is [down string][up string] over up strings of 1 then 2 particles: each sector's part
+    n1, n2, nd = O.binom(norb, 1), O.binom(norb, 2), O.binom(norb, 2)
+    X, Y = x.reshape(nd, n1 + n2), y.reshape(nd, n1 + n2)
+    for nu, cols in ((1, slice(0, n1)), (2, slice(n1, n1 + n2))):
+        ref_s = O.hprod_hubbard(O.Sector(norb, nu, 2), t, 2.0, X[:, cols].reshape(-1))
+        np.testing.assert_allclose(Y[:, cols].reshape(-1), ref_s, rtol=0, atol=1e-12)
