@@ -117,6 +117,22 @@ class Basis:
     def filename_basis(self):
         return "basis.h5"
 
+    def exec_basis(self, elem2comp):
+        """The reference runs basis.x to enumerate the strings of the particle
+        numbers elem2comp into basis.h5 (basis.py:167-171); here they are
+        enumerated on demand by ed_basis, so this only warms the cache."""
+        for ne in elem2comp:
+            self._strings_of(int(ne))
+
+    def __basisremove__(self):
+        # the reference deletes basis.h5 (basis.py:85-89); no file is written here
+        self._strings = {}
+
+    @property
+    def file_size(self):
+        """Size of the reference's basis.h5; no file is written here."""
+        return 0.0
+
     @property
     def basis(self):
         order = self.spin_ordering if self.order == "spin" else self.site_ordering

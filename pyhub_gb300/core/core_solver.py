@@ -106,7 +106,7 @@ class CoreSolver(Basis, GreenFunction, StaticQuantities):
     # ----------------------------------------------------------- solve
     def kernel(self, max_lcz: int = 600, acc_lcz: float = 1.e-8, nb_comp_states=1, compute_rq=True,
                compute_spgf=False, nb_sites_comp=None, store_H=False, verbose=False, *, dtype: str = "auto",
-               reorth: str = "auto", seed: int = 0, refine_steps: int = 60):
+               reorth: str = "auto", seed: int = 0, refine_steps: int = 60, store_lanczos_vectors: bool = False):
         torch = _torch()
         self.max_lcz = max_lcz
         self.acc_lcz = acc_lcz
@@ -116,6 +116,7 @@ class CoreSolver(Basis, GreenFunction, StaticQuantities):
         self.compute_tprf = False
         self.store_H = store_H
         self.verbose = verbose
+        self._store_lcz = bool(store_lanczos_vectors)
         self.nb_sites_comp = self.nb_sites if nb_sites_comp is None else nb_sites_comp
         tall = pc()
         self._sectors = {}
@@ -176,11 +177,17 @@ class CoreSolver(Basis, GreenFunction, StaticQuantities):
             reorth = "full" if fits else "none"
         v0 = LZ.start_vector(sec, seed)
         rule = LZ.ReferenceRule(acc_lcz)
+        lcz = None
         nvec = max(1, int(nb_comp_states))
         if reorth == "full":
             if dtype == "f64":
                 r = LZ.lanczos_full(sec, v0, steps, torch.float64, rule=rule, want_vector=False, keep_basis=True)
                 psis = [r.ritz_vector(k) for k in range(min(nvec, r.steps))]
+                if getattr(self, "_store_lcz", False):
+                    # the normalised Krylov vectors q_j = s_j u_j, reference basis order, as LANCZOS
+                    # stores them in solver.h5 (lanczos.f90:42-49)
+                    lcz = np.stack([sec.to_ref(r.basis[j] * float(r.scales[j])).cpu().numpy()
+                                    for j in range(r.steps)], axis=1)
                 ritz, alpha, beta, steps_done, conv = r.ritz, r.alpha, r.beta, r.steps, r.converged
                 r.release()
             else:
@@ -218,9 +225,12 @@ class CoreSolver(Basis, GreenFunction, StaticQuantities):
                 psis = [r2.psis[0]] + list(psis[1:])
                 ritz = np.concatenate([[r2.ritz[0]], ritz[1:]])
             del storage
-        return {"eigenvalues": np.asarray(ritz), "psis": psis, "is_lanczos": True, "deg": rule.ndeg,
-                "alpha": alpha, "beta": beta, "nb_lcz": steps_done, "conv": rule.conv,
-                "converged": conv, "H": None, "nstates": sec.dim, "precision": dtype, "reorth": reorth}
+        out = {"eigenvalues": np.asarray(ritz), "psis": psis, "is_lanczos": True, "deg": rule.ndeg,
+               "alpha": alpha, "beta": beta, "nb_lcz": steps_done, "conv": rule.conv,
+               "converged": conv, "H": None, "nstates": sec.dim, "precision": dtype, "reorth": reorth}
+        if lcz is not None:
+            out["lcz_vectors"] = lcz
+        return out
 
     def _boltzmann(self, val, nb_comp_states):
         """BOLTZMANN (boltzmann.f90:1-29)."""
@@ -561,6 +571,26 @@ class CoreSolver(Basis, GreenFunction, StaticQuantities):
             raise StopIteration('Lanczos not converged, step,', lcz['step'],
                                 f' greater than the maximum wanted {self.max_lcz}')
         return lcz
+
+    @property
+    def lcz_vectors(self):
+        """The normalised Lanczos vectors [D, nb_lcz] in reference order
+        (core_solver.py:211-213).  They are kept only on request:
+        kernel(..., dtype='f64', store_lanczos_vectors=True) on a sector that
+        is solved by Lanczos (the full-reorthogonalisation run keeps them on
+        the device anyway; a mixed run's are FP32 vectors of another stage)."""
+        if not self._sol["is_lanczos"]:
+            raise KeyError("the sector was diagonalised densely (no Lanczos vectors)")
+        if "lcz_vectors" not in self._sol:
+            raise KeyError("the Lanczos vectors are kept only by kernel(..., dtype='f64', "
+                           "store_lanczos_vectors=True)")
+        return self._sol["lcz_vectors"]
+
+    def _exec(self):
+        """The reference writes the particle numbers to basis.h5 and runs the
+        Fortran solver as a process (core_solver.py:106-110); here kernel()
+        solves in process, so there is nothing to launch."""
+        return None
 
     @property
     def nb_lcz(self):

@@ -6,6 +6,8 @@ Sites are 0-based; spins 'u'/'up'/1/'+' are up, anything else down.
 """
 from __future__ import annotations
 
+import numpy as np
+
 from ..core._operators import Operators
 
 
@@ -94,3 +96,40 @@ def opesum(lst):
     for op in lst:
         H += op
     return H
+
+
+def opeexp(op, psi, ftol=1.e-6, unitary=False):
+    """exp(op) psi by its Taylor series (pyhub/tools/operators.py:91-111): terms
+    op^k psi / k! added until the squared norm of the sum changes by less than
+    ftol between terms (unitary: differs from ||psi|| by less than ftol),
+    at most 99 terms; the products op @ v run on the GPU."""
+    if isinstance(psi, (list, np.ndarray)):
+        psi = np.asarray(psi)
+        conv = False
+        new_psi, full_psi, i, val = np.copy(psi), np.copy(psi), 1, 1.e3
+        nmr0 = np.linalg.norm(psi)
+        while not conv and i < 100:
+            new_psi = op @ new_psi / i
+            full_psi += new_psi
+            i += 1
+            nmr = full_psi.conj() @ full_psi
+            if unitary:
+                if np.abs(nmr0 - nmr) < ftol:
+                    conv = True
+            else:
+                if np.abs(val - nmr) < ftol:
+                    conv = True
+                else:
+                    val = nmr
+        if i == 100:
+            raise ValueError('exponential operator does not converge')
+        return full_psi
+    # no vector: the matrix whose row i is exp(op) applied to basis state i
+    matrix = np.zeros((op.nb_selected, op.nb_selected))
+    psi0 = np.zeros(op.nb_selected)
+    for i in range(op.nb_selected):
+        psi0[i] = 1.
+        matrix[i, :] = opeexp(op, psi0)
+        psi0[i] = 0.
+    return matrix
+

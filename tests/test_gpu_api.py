@@ -344,3 +344,38 @@ def test_self_energy_matches_reference_formula(edlib, nu, nd):
         z = fh.qpw
         assert np.abs(z - z_ref).max() <= 1e-3 * max(1.0, np.abs(z_ref).max()), np.abs(z - z_ref).max()
     assert fh.galitskii_migdal is None
+
+
+def test_lanczos_vectors_and_operator_exponential(edlib):
+    """lcz_vectors (kept on request by an FP64 solve): orthonormal, V^T H V is
+    the tridiagonal of alpha/beta, and V times its lowest eigenvector is psi0.
+    opeexp: exp(O) psi by the Taylor series equals expm of the operator's
+    matrix applied to psi."""
+    import scipy.linalg as sl
+    from pyhub_gb300.core.basis import Basis
+    from pyhub_gb300.solver import FermiHubbard
+    from pyhub_gb300.tools import operators as OP
+    t = O.ring(8)
+    fh = FermiHubbard(8, 4, 4, t, 4.0)
+    fh.kernel(max_lcz=200, acc_lcz=1e-8, compute_rq=False, dtype="f64", reorth="full", store_lanczos_vectors=True)
+    V = fh.lcz_vectors
+    k = V.shape[1]
+    assert k == fh.nb_lcz
+    assert np.abs(V.T @ V - np.eye(k)).max() < 1e-10
+    osec = O.Sector(8, 4, 4)
+    HV = np.stack([O.hprod_hubbard(osec, t, 4.0, V[:, j], fast=True) for j in range(k)], axis=1)
+    lcz = fh.lcz_results
+    T = np.diag(lcz["alpha"][:k]) + np.diag(lcz["beta"][:k - 1], 1) + np.diag(lcz["beta"][:k - 1], -1)
+    assert np.abs(V.T @ HV - T).max() < 1e-9
+    e, y = np.linalg.eigh(T)
+    assert abs(abs((V @ y[:, 0]) @ fh.psi0) - 1.0) < 1e-8
+    fh2 = FermiHubbard(8, 4, 4, t, 4.0)
+    fh2.kernel(max_lcz=200, compute_rq=False)
+    with pytest.raises(KeyError):
+        fh2.lcz_vectors
+    op = 0.3 * (OP.c_dagger_c((0, 'u'), (1, 'u')) + OP.c_dagger_c((1, 'u'), (0, 'u'))) + 0.2 * OP.n((2, 'd'))
+    op.set_basis(Basis(4, hilbert=(2, 2)))
+    psi = np.random.default_rng(2).normal(size=op.nstates)
+    M = op.to_matrix
+    got = OP.opeexp(op, psi, ftol=1e-14)
+    np.testing.assert_allclose(got, sl.expm(M.T) @ psi, rtol=0, atol=1e-10)

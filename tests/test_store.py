@@ -146,3 +146,12 @@ def test_nvtx_range_without_a_device():
     with pytest.raises(KeyError):
         with nvtx("pyhub.test"):
             raise KeyError("propagates")
+
+
+def test_basis_file_helpers():
+    from pyhub_gb300.core.basis import Basis
+    b = Basis(4, hilbert=(2, 1))
+    b.exec_basis([2, 1])
+    assert b.file_size == 0.0
+    b.__basisremove__()
+    assert len(b.basis_up) == 6 and len(b.basis_down) == 4
