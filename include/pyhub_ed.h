@@ -215,6 +215,39 @@ int ed_gf_start_sites(const ed_sector *src, const ed_sector *dst, void *stream, 
  * Vectors of all instances are concatenated: instance i occupies elements
  * [offsets[i], offsets[i] + nsdn_i*ld_i) with ld_i = nsup_i rounded up to 32
  * (the engine's internal row stride). */
+/* ---- composite entry points for a host without the Python layer ----
+ * One step k of the full-reorthogonalisation Lanczos: ed_hv(u_k -> w),
+ * ed_multidot(V, k+1, w, z = u_k), ed_lanczos_coef(k), ed_update_wscaled(->
+ * u_{k+1}), enqueued on one stream with no host synchronisation.  V: device
+ * basis rows (stride ldv >= the vector length), row 0 = the start vector;
+ * state as ed_lanczos_coef documents it (zeroed, state[2] = 1/||u_0||);
+ * alpha, beta device FP64 [mmax]; k < mmax.  The scratch (at least
+ * ed_lanczos_step_scratch_bytes) must be the same for every step of a run: it
+ * carries ||u_k||^2 from one step to the next.  Replaces the LANCZOS loop body
+ * (lanczos.f90:50-58). */
+int64_t ed_lanczos_step_scratch_bytes(const ed_sector *s, int mmax);
+int ed_lanczos_step(ed_sector *s, void *stream, int dtype, int64_t ld, void *V, int64_t ldv, int k, int mmax,
+                    void *w, double *state, double *alpha, double *beta, void *scratch, int64_t scratch_bytes);
+/* The reduced quantities of one state as the reference stores them: Hubbard
+ * gamma (host [2][N][N], up then down, symmetric), docc (host [N], NI of
+ * TWO_RDM) and sisj (host [N][N], J_SPIN) from the pairs K <= J mirrored
+ * (static_rq.f90:153-395; the down matrix is the up one when N_up == N_down,
+ * :237-239); Heisenberg sisj only (SMATRIX in the Python view,
+ * static_rq_heis.f90:58-116; gamma and docc may be NULL).  Synchronises the
+ * stream (the sums are copied to the host). */
+int64_t ed_rdm1_scratch_bytes(const ed_sector *s);
+int ed_rdm1(ed_sector *s, void *stream, int dtype, int64_t ld, const void *psi, double *gamma, double *docc,
+            double *sisj, void *scratch, int64_t scratch_bytes);
+/* Hellmann-Feynman gradient of <psi|H|psi> for a Hubbard sector: g_t[b] =
+ * dE/dt for bond b (bonds: host int32 [2*nbonds], 1-based, t_ij = t_ji one
+ * parameter) = sum_s <c+_is c_js + c+_js c_is>; g_u[i] = <n_i,up n_i,down>;
+ * g_eps[i] = sum_s <n_is> (the diagonal of t).  Both spins are summed (no
+ * N_up == N_down shortcut).  Host outputs; scratch as ed_rdm1; synchronises
+ * the stream.  No reference counterpart (the differentiation of the north
+ * star). */
+int ed_hf_grad(ed_sector *s, void *stream, int dtype, int64_t ld, const void *psi, int nbonds, const int32_t *bonds,
+               double *g_t, double *g_u, double *g_eps, void *scratch, int64_t scratch_bytes);
+
 /* ---- generic operator engine (operators.x) ----
  * The vector space of the reference's Operators: the up strings of every
  * listed up-particle number (nups[0..nlist_up-1], each block in HILBERT

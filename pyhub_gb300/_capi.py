@@ -28,6 +28,11 @@ _SIGS = {
     "ed_rank": (_I64, [_I, _I, ctypes.c_uint32]),
     "ed_sector_create": (_I, [_I, _I, _I, _I, _P, _P, _P, ctypes.POINTER(_P)]),
     "ed_sector_destroy": (_I, [_P]),
+    "ed_lanczos_step_scratch_bytes": (_I64, [_P, _I]),
+    "ed_lanczos_step": (_I, [_P, _P, _I, _I64, _P, _I64, _I, _I, _P, _P, _P, _P, _P, _I64]),
+    "ed_rdm1_scratch_bytes": (_I64, [_P]),
+    "ed_rdm1": (_I, [_P, _P, _I, _I64, _P, _P, _P, _P, _P, _I64]),
+    "ed_hf_grad": (_I, [_P, _P, _I, _I64, _P, _I, _P, _P, _P, _P, _P, _I64]),
     "ed_opspace_create": (_I, [_I, _I, _P, _I, _P, ctypes.POINTER(_P)]),
     "ed_opspace_dims": (_I, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
     "ed_opspace_destroy": (_I, [_P]),
@@ -236,6 +241,55 @@ class Sector:
         else:
             out[..., : self.dim] = r
         return out
+
+    # -------------------------------------------------------- composite entry points
+    def rdm1(self, psi, ld: int | None = None, stream=None):
+        """ed_rdm1: (gamma [2, N, N], docc [N], sisj [N, N]) as the reference
+        stores them (Heisenberg: gamma and docc are None)."""
+        import torch
+        N = self.norb
+        nb = int(lib().ed_rdm1_scratch_bytes(self._h))
+        scratch = torch.empty((nb + 7) // 8, dtype=torch.float64, device=psi.device)
+        hub = self.kind == ED_HUBBARD
+        gamma = np.zeros((2, N, N)) if hub else None
+        docc = np.zeros(N) if hub else None
+        sisj = np.zeros((N, N))
+        ld = self.ld if ld is None else ld
+        check("ed_rdm1", lib().ed_rdm1(self._h, _stream(stream), dtype_code(psi.dtype), int(ld),
+                                       _ptr(psi, self._need(ld), "psi"),
+                                       None if gamma is None else gamma.ctypes.data,
+                                       None if docc is None else docc.ctypes.data, sisj.ctypes.data,
+                                       _ptr(scratch), nb))
+        return gamma, docc, sisj
+
+    def hf_grad(self, psi, bonds, ld: int | None = None, stream=None):
+        """ed_hf_grad: (g_t [nbonds], g_u [N], g_eps [N]) of <psi|H|psi>; bonds
+        1-based (i, j) pairs."""
+        import torch
+        N = self.norb
+        b = np.ascontiguousarray(np.asarray(bonds, dtype=np.int32).reshape(-1, 2))
+        nb = int(lib().ed_rdm1_scratch_bytes(self._h))
+        scratch = torch.empty((nb + 7) // 8, dtype=torch.float64, device=psi.device)
+        gt, gu, ge = np.zeros(max(len(b), 1)), np.zeros(N), np.zeros(N)
+        ld = self.ld if ld is None else ld
+        check("ed_hf_grad", lib().ed_hf_grad(self._h, _stream(stream), dtype_code(psi.dtype), int(ld),
+                                             _ptr(psi, self._need(ld), "psi"), len(b), b.ctypes.data,
+                                             gt.ctypes.data, gu.ctypes.data, ge.ctypes.data, _ptr(scratch), nb))
+        return gt[:len(b)], gu, ge
+
+    def lanczos_step(self, V, k: int, mmax: int, w, state, alpha, beta, scratch, ld: int | None = None,
+                     stream=None):
+        """ed_lanczos_step: step k of the full-reorthogonalisation Lanczos on the
+        basis rows V (device [mmax+1, n]); scratch as ed_lanczos_step_scratch_bytes,
+        the same for every step of a run."""
+        ld = self.ld if ld is None else ld
+        check("ed_lanczos_step", lib().ed_lanczos_step(
+            self._h, _stream(stream), dtype_code(V.dtype), int(ld), _ptr(V), int(V.stride(0)), int(k), int(mmax),
+            _ptr(w), _ptr(state), _ptr(alpha), _ptr(beta), _ptr(scratch),
+            int(scratch.numel() * scratch.element_size())))
+
+    def lanczos_step_scratch_bytes(self, mmax: int) -> int:
+        return int(lib().ed_lanczos_step_scratch_bytes(self._h, int(mmax)))
 
     # -------------------------------------------------------- products
     def rdm_raw(self, bra, ket=None, pairs=None, flags: int = 3, ld: int | None = None, stream=None):

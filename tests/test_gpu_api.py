@@ -379,3 +379,87 @@ def test_lanczos_vectors_and_operator_exponential(edlib):
     M = op.to_matrix
     got = OP.opeexp(op, psi, ftol=1e-14)
     np.testing.assert_allclose(got, sl.expm(M.T) @ psi, rtol=0, atol=1e-10)
+
+
+def test_ring_energy_approaches_bethe_ansatz(edlib):
+    """Half-filled Hubbard rings (U = 4, closed shells L = 4n + 2) against the
+    thermodynamic energy per site that the reference's bethe_anzatz.E_bessel(4)
+    returns (golden value from the reference's own Python): the finite-size
+    error shrinks from L = 10 to L = 14, and the 1/L^2 extrapolation of the two
+    lands within 2e-3 of it (a loose physics pin, as the reference's examples
+    use it)."""
+    import os
+    from pyhub_gb300.solver import FermiHubbard
+    eb = float(np.load(os.path.join(os.path.dirname(__file__), "golden", "pole_golden.npz"))["e_bessel_U4"])
+    e = {}
+    for L in (10, 14):
+        fh = FermiHubbard(L, L // 2, L // 2, O.ring(L), 4.0)
+        fh.kernel(max_lcz=300, acc_lcz=1e-10, compute_rq=False)
+        e[L] = fh.e0 / L
+    assert abs(e[10] - (-0.5834322635772545)) < 1e-9      # the oracle's Lanczos on the same ring
+    assert abs(e[14] - eb) < abs(e[10] - eb) < 0.011
+    e_inf = (14 ** 2 * e[14] - 10 ** 2 * e[10]) / (14 ** 2 - 10 ** 2)
+    assert abs(e_inf - eb) < 2e-3, (e, e_inf, eb)
+
+
+@pytest.mark.parametrize("case", [(6, 3, 3), (6, 2, 4)])
+def test_composite_entry_points(edlib, case):
+    """ed_rdm1 equals the Python assembly of the same ed_rdm sums bit for bit;
+    ed_hf_grad equals the Hellmann-Feynman gradient of core.gradients to
+    1e-12; m calls of ed_lanczos_step give lanczos_full's alpha/beta bit for
+    bit (same kernels, same order)."""
+    import torch
+    from pyhub_gb300.core import gradients as GRD
+    from pyhub_gb300.core import lanczos as LZ
+    from pyhub_gb300.core.reduced_quantities import (all_pairs, assemble_heisenberg, assemble_hubbard,
+                                                     lower_pairs, scatter_pairs)
+    norb, nu, nd = case
+    t, U, rng = _state(norb, nu, nd, 3 * norb + nu)
+    sec = edlib.Sector(norb, nu, nd, edlib.ED_HUBBARD, t=t, U=U)
+    osec = O.Sector(norb, nu, nd)
+    psi = rng.standard_normal(osec.dim)
+    psi /= np.linalg.norm(psi)
+    x = sec.from_ref(torch.tensor(psi, device="cuda"))
+    gamma, docc, sisj = sec.rdm1(x)
+    pairs = lower_pairs(norb)
+    raw, _ = sec.rdm_raw(x, pairs=pairs, flags=2 | (1 if nu != nd else 0))
+    gu, gd, ni, sm = assemble_hubbard(scatter_pairs(raw, pairs, norb), norb, nu, nd)
+    assert np.array_equal(gamma[0], gu) and np.array_equal(gamma[1], gd)
+    assert np.array_equal(docc, ni) and np.array_equal(sisj, sm)
+    # gradient: bonds of t, both spins summed
+    bonds = [(i, j) for i in range(norb) for j in range(i + 1, norb) if abs(t[i, j]) > 0.3]
+    params = GRD.HubbardParams(norb, bonds)
+    raw2, _ = sec.rdm_raw(x, pairs=params.pairs(), flags=1)
+    g_ref = params.contract(raw2)
+    g_t, g_u, g_e = sec.hf_grad(x, [(i + 1, j + 1) for i, j in bonds])
+    nb = len(bonds)
+    np.testing.assert_allclose(g_t, g_ref[:nb], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(g_u, g_ref[nb:nb + norb], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(g_e, g_ref[nb + norb:], rtol=0, atol=1e-12)
+    # Heisenberg: sisj only
+    hs = edlib.Sector(norb, norb // 2, 0, edlib.ED_HEISENBERG, J=O.ring(norb, 1.0))
+    y = torch.tensor(rng.standard_normal(hs.dim), device="cuda")
+    g0, d0, s0 = hs.rdm1(y)
+    rawh, _ = hs.rdm_raw(y, pairs=all_pairs(norb))
+    assert g0 is None and d0 is None and np.array_equal(s0, assemble_heisenberg(rawh, norb))
+    # Lanczos steps through the C ABI against lanczos_full
+    m = 30
+    v0 = LZ.start_vector(sec, 4)
+    ref = LZ.lanczos_full(sec, v0, m, torch.float64, rule=None, want_vector=False)
+    V = torch.zeros((m + 1, sec.n), dtype=torch.float64, device="cuda")
+    V[0].copy_(v0)
+    w = torch.zeros(sec.n, dtype=torch.float64, device="cuda")
+    sc = torch.zeros((sec.lanczos_step_scratch_bytes(m) + 7) // 8, dtype=torch.float64, device="cuda")
+    n0 = torch.zeros(2, dtype=torch.float64, device="cuda")
+    buf = torch.empty(edlib.scratch_bytes(sec.n, 2) // 8 + 1, dtype=torch.float64, device="cuda")
+    edlib.multidot(V, 1, V[0], n0, buf)
+    state = torch.zeros(edlib.lanczos_state_doubles(m), dtype=torch.float64, device="cuda")
+    state[2] = 1.0 / float(n0[0].item()) ** 0.5
+    ab = torch.zeros((2, m), dtype=torch.float64, device="cuda")
+    for k in range(m):
+        sec.lanczos_step(V, k, m, w, state, ab[0], ab[1], sc)
+    torch.cuda.synchronize()
+    a = ab[0].cpu().numpy()
+    b = ab[1].cpu().numpy()
+    assert np.array_equal(a, np.asarray(ref.alpha)[:m]), np.abs(a - np.asarray(ref.alpha)[:m]).max()
+    assert np.array_equal(b[:m - 1], np.asarray(ref.beta)[:m - 1])
