@@ -267,8 +267,10 @@ int ed_opspace_destroy(ed_opspace *sp);
  * 2 NI, 3 identity, 4 NIM1 (1 - n), 5 SZ_OPE, 6 / 7 C_DAGGER_C_UNRES with
  * site1 on both sides (c+_{up} c_{down} / c+_{down} c_{up}), 9
  * C_DAGGER_C_UNRES(site1, site2, spin2) (c+ of the other spin at site1,
- * c_{site2, spin2}), 10 C_DAGGER, 11 C_; code 8 (SISJ) is refused, nothing
- * in the operator algebra produces it.  Results of a factor outside the
+ * c_{site2, spin2}), 10 C_DAGGER, 11 C_, and 12 SZ_BASIS (+S^z, the sz of the
+ * reference's basis-element mode, operators_basis.f90:134-145; SZ_OPE, code 5,
+ * multiplies by (n_down - n_up)/2); code 8 (SISJ) is refused, nothing in the
+ * operator algebra produces it.  Results of a factor outside the
  * listed particle numbers are dropped, as the Fortran drops them.  x, y
  * device FP64 [nsup*nsdn]; work device, at least 2*nsup*nsdn doubles; the
  * term list is host memory, read before anything is enqueued. */

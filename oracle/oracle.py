@@ -621,6 +621,15 @@ def ops_apply_ref(norb: int, nups, ndns, terms, psi: np.ndarray) -> np.ndarray:
                     if not b & _ops_site(norb, si):
                         for u in range(nsup):
                             w[d * nsup + u] = w[d * nsup + u] - v[d * nsup + u] / 2.0
+            elif code == 12:                    # SZ_BASIS  operators_basis.f90:134-145: VAL * SZ
+                for d, bd in enumerate(bdn):
+                    for u, b in enumerate(bup):
+                        sz = 0.0
+                        if b & _ops_site(norb, si):
+                            sz = sz + 0.5
+                        if bd & _ops_site(norb, si):
+                            sz = sz - 0.5
+                        w[d * nsup + u] = v[d * nsup + u] * sz
             elif code in (6, 7, 9):             # C_DAGGER_C_UNRES(J, K, SPINK)  operators.f90:62-144
                 J = si
                 K = sj if code == 9 else si

@@ -21,7 +21,9 @@ same term list is kept in memory and applied on the device:
   one first, and a factor whose result leaves the listed particle numbers
   drops it, as the Fortran does.  Its `sz` element is SZ_OPE
   (operators.f90:223-248), which multiplies by (n_down - n_up)/2; products
-  sz*sz, as sisj builds them, are the usual S^z_i S^z_j.
+  sz*sz, as sisj builds them, are the usual S^z_i S^z_j.  to_matrix, the
+  comparisons and bit_repr use the reference's basis-element routines
+  (operators_basis.f90), whose sz (SZ_BASIS) is +S^z.
 * Expectation values of one-body terms of either spin, densities,
   n_{i up} n_{i down} and the spin correlation sisj((i,),(j,)) on one sector
   go through the fused RDM kernel (ed_rdm).
@@ -299,11 +301,15 @@ class Operators(Basis):
         return self.selected is None and len(self.n_up) == 1 and len(self.n_down) == 1
 
     # ------------------------------------------------------------ generic engine
-    def _encode(self):
+    def _encode(self, basis_mode: bool = False):
         """The term list as _write_operator encodes it (_operators.py:420-462):
         [(coeff, [(code, site1, spin1, site2, spin2), ...])], sites 1-based,
-        spin 1 = up, 2 = down."""
-        codes = {"n": 2, "id.": 3, "1_n": 4, "sz": 5, "splus": 6, "sminus": 7, "sisj": 8, "c_dagger": 10, "c": 11}
+        spin 1 = up, 2 = down.  basis_mode: the reference's basis-element
+        routines (operators_basis.f90), which differ from the vector routines
+        in one place: their sz multiplies by +S^z (SZ_BASIS, engine code 12)
+        where SZ_OPE gives (n_down - n_up)/2."""
+        codes = {"n": 2, "id.": 3, "1_n": 4, "sz": 12 if basis_mode else 5, "splus": 6, "sminus": 7, "sisj": 8,
+                 "c_dagger": 10, "c": 11}
         terms = []
         for c, strs, elems in zip(self.coeff, self.str_index, self.elem_index):
             ops = []
@@ -337,13 +343,15 @@ class Operators(Basis):
             self._opspace = sp
         return sp[1]
 
-    def _apply_generic_full(self, x_full: np.ndarray) -> np.ndarray:
+    def _apply_generic_full(self, x_full: np.ndarray, basis_mode: bool = False) -> np.ndarray:
         """The operator applied to a vector of the whole space (the reference's
-        psi/input dataset), on the generic engine."""
+        psi/input dataset), on the generic engine; basis_mode: with the
+        semantics of the basis-element routines (to_matrix, the comparisons,
+        bit_repr)."""
         torch = _torch()
         sp = self._space()
         x = torch.tensor(np.asarray(x_full, dtype=np.float64), device="cuda")
-        return sp.apply(self._encode(), x).cpu().numpy()
+        return sp.apply(self._encode(basis_mode), x).cpu().numpy()
 
     def _embed(self, psi: np.ndarray) -> np.ndarray:
         """psi of the selected states placed in the whole space (zeros elsewhere),
@@ -366,7 +374,7 @@ class Operators(Basis):
         e = np.zeros(self.nstates)
         for k, s_ in enumerate(states):
             e[s_] = 1.0
-            out[k] = (self._apply_generic_full(e))[s_]
+            out[k] = (self._apply_generic_full(e, basis_mode=True))[s_]
             e[s_] = 0.0
         return out
 
@@ -517,7 +525,7 @@ class Operators(Basis):
             e = np.zeros(self.nstates)
             for i, s_ in enumerate(states):
                 e[s_] = 1.0
-                M[i, :] = self._apply_generic_full(e)[states]
+                M[i, :] = self._apply_generic_full(e, basis_mode=True)[states]
                 e[s_] = 0.0
             return M
         n = self.nstates

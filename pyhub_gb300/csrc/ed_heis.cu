@@ -587,7 +587,6 @@ __global__ void __launch_bounds__(kRdmThreads) heis_rdm_row_kernel(const T *__re
             const uint32_t ha = __ldg(a.col_pat + cbase + c);
             const uint64_t h = (uint64_t)ha | ((uint64_t)hb << nA);   // bit j: site j+1 is down
             const T kv = __ldg(ket + off + c);
-            const T bk = xs[c] * kv;
 #pragma unroll
             for (int q = 0; q < kRdmP; ++q) {
                 if (q >= np) break;
@@ -598,10 +597,10 @@ __global__ void __launch_bounds__(kRdmThreads) heis_rdm_row_kernel(const T *__re
                 uint32_t ma = 0;
                 if (J < nA) ma |= 1u << J;
                 if (K < nA) ma |= 1u << K;
-                const T sg = ((J + K) & 1) ? (T)-1 : (T)1;   // (-1)^((J+1)+(K+1))
                 const int cs = ma ? __ldg(a.rankA + (ha ^ ma)) : c;
                 const T bv = (soff[q] == off) ? xs[cs] : __ldg(bra + soff[q] + cs);
-                r0[q] += sg * bv * kv;
+                // sign (-1)^((J+1)+(K+1)) folded into the FMA's operand: one operation per flip
+                r0[q] = ((J + K) & 1) ? fma(-bv, kv, r0[q]) : fma(bv, kv, r0[q]);
             }
         }
 #pragma unroll

@@ -32,7 +32,8 @@ enum OpCode : int {
     kOpSisj = 8,      // SISJ: no producer in the Python API
     kOpHopFlip = 9,   // c^+_{i, other spin of s_j} c_{j s_j}
     kOpCdag = 10,     // c^+_{i s}
-    kOpC = 11         // c_{i s}
+    kOpC = 11,        // c_{i s}
+    kOpSzBasis = 12   // SZ_BASIS (operators_basis.f90:134-145): the basis-element form of sz, + S^z
 };
 
 struct OpArgs {
@@ -106,6 +107,15 @@ __global__ void __launch_bounds__(256) ops_elem_kernel(const OpArgs a, int code,
             if (!(su & b)) v = v + x / 2.0;
             if (!(sd & b)) v = v - x / 2.0;
             out[idx] = v;
+            break;
+        }
+        case kOpSzBasis: {
+            // VAL = VAL * SZ(NORB, SI, BUP, BDOWN): +1/2 for an up particle, -1/2 for a down one
+            const uint32_t b = site_bit_dev(norb, si);
+            double sz = 0.0;
+            if (su & b) sz = sz + 0.5;
+            if (sd & b) sz = sz - 0.5;
+            out[idx] = x * sz;
             break;
         }
         case kOpSplus:
@@ -194,7 +204,7 @@ extern "C" int ed_ops_apply(const ed_opspace *sp, void *stream, int nterms, cons
         for (int q = term_off[t]; q < term_off[t + 1]; ++q) {
             const int32_t *o = ops + 5 * (int64_t)q;
             const int code = o[0];
-            ED_REQUIRE(code >= 0 && code <= kOpC, "operator code %d of term %d", code, t);
+            ED_REQUIRE(code >= 0 && code <= kOpSzBasis, "operator code %d of term %d", code, t);
             ED_REQUIRE(code != kOpSisj, "operator code 8 (SISJ) has no producer in the operator algebra; "
                                         "build S_i.S_j from c_dagger_c and sz terms");
             if (code == 0 || code == kOpId) continue;

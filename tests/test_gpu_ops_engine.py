@@ -22,7 +22,7 @@ def _random_terms(rng, norb, nterms=6, maxlen=3):
     for _ in range(nterms):
         ops = []
         for _ in range(int(rng.integers(1, maxlen + 1))):
-            code = int(rng.choice([1, 2, 4, 5, 6, 7, 9, 10, 11, 3]))
+            code = int(rng.choice([1, 2, 4, 5, 6, 7, 9, 10, 11, 12, 3]))
             i, j = (int(v) for v in rng.integers(1, norb + 1, size=2))
             s1, s2 = (int(v) for v in rng.integers(1, 3, size=2))
             ops.append((code, i, s1, j, s2))
@@ -46,7 +46,7 @@ def test_engine_matches_oracle_bit_for_bit(edlib, space):
         ref = O.ops_apply_ref(norb, nups, ndns, terms, psi)
         np.testing.assert_array_equal(got, ref, err_msg=str(terms))
     # every code alone, every site and spin
-    for code in (1, 2, 4, 5, 6, 7, 9, 10, 11):
+    for code in (1, 2, 4, 5, 6, 7, 9, 10, 11, 12):
         for i in range(1, norb + 1):
             for s1 in (1, 2):
                 t = [(1.0, [(code, i, s1, (i % norb) + 1, 3 - s1)])]
@@ -58,7 +58,7 @@ def test_engine_refuses_bad_terms(edlib):
     sp = edlib.OpSpace(4, [2], [2])
     x = torch.zeros(sp.nstates, dtype=torch.float64, device="cuda")
     for bad in ([(1.0, [(8, 1, 1, 2, 1)])], [(1.0, [(1, 5, 1, 1, 1)])], [(1.0, [(2, 1, 3, 0, 0)])],
-                [(1.0, [(12, 1, 1, 0, 0)])]):
+                [(1.0, [(13, 1, 1, 0, 0)])]):
         with pytest.raises(edlib.EDError):
             sp.apply(bad, x)
     with pytest.raises(edlib.EDError):
@@ -83,12 +83,15 @@ def test_operators_generic_paths_match_oracle(edlib):
     z = psi + 1j * rng.normal(size=op.nstates)
     np.testing.assert_allclose(op @ z, O.ops_apply_ref(norb, nups, ndns, terms, z.real)
                                + 1j * O.ops_apply_ref(norb, nups, ndns, terms, z.imag), atol=1e-12)
-    # to_matrix: row i = the operator applied to basis state i
+    # to_matrix: row i = the operator applied to basis state i, with the basis-element routines (their sz is
+    # SZ_BASIS, + S^z, where the vector routines' SZ_OPE gives (n_down - n_up)/2)
     M = op.to_matrix
+    bterms = op._encode(basis_mode=True)
+    assert [c for _, ops in bterms for c, *_ in ops].count(12) == 1
     for i in (0, 7, op.nstates - 1):
         e = np.zeros(op.nstates)
         e[i] = 1.0
-        np.testing.assert_allclose(M[i], O.ops_apply_ref(norb, nups, ndns, terms, e), atol=1e-12)
+        np.testing.assert_allclose(M[i], O.ops_apply_ref(norb, nups, ndns, bterms, e), atol=1e-12)
     # comparisons: the diagonal, up string outer and down string inner
     diag = np.array([M[d * op.nsup + u, d * op.nsup + u] for u in range(op.nsup) for d in range(op.nsdown)])
     assert (op == 1.25) == [bool(np.isclose(v, 1.25)) for v in diag]

@@ -62,6 +62,12 @@ def test_sz_is_sz_ope(psi):
         np.testing.assert_allclose(_ap([(5, i, 0, 0, 0)], psi), ref, rtol=0, atol=1e-15)
 
 
+def test_sz_basis_is_minus_sz_ope(psi):
+    """The basis-element sz (SZ_BASIS, engine code 12) multiplies by +S^z."""
+    for i in range(1, NORB + 1):
+        np.testing.assert_array_equal(_ap([(12, i, 0, 0, 0)], psi), -_ap([(5, i, 0, 0, 0)], psi))
+
+
 def test_terms_restart_from_psi_and_drop_unlisted_sectors():
     bup, bdn = O.ops_space(NORB, [1, 2], [2])
     psi = np.random.default_rng(1).normal(size=len(bup) * len(bdn))
