@@ -258,7 +258,8 @@ int ed_opspace_create(int norb, int nlist_up, const int *nups, int nlist_dn, con
 int ed_opspace_dims(const ed_opspace *sp, int64_t *nsup, int64_t *nsdn);
 int ed_opspace_destroy(ed_opspace *sp);
 /* y = sum_t coeff[t] * (O_{t,last} ... O_{t,1}) x, PROGRAM OPERATOR
- * (compute_operators.f90:28-66): terms with |coeff| <= 1e-14 are skipped; the
+ * (compute_operators.f90:28-66): terms with |coeff| <= 1e-14 (the single-
+ * precision literal 1.E-14, promoted) are skipped; the
  * factors of term t are ops[5*q .. 5*q+4] for q in [term_off[t],
  * term_off[t+1]) = {code, site1, spin1, site2, spin2} exactly as the
  * reference's _write_operator encodes them (_operators.py:420-462; sites

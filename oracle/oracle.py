@@ -576,7 +576,7 @@ def ops_apply_ref(norb: int, nups, ndns, terms, psi: np.ndarray) -> np.ndarray:
     idn = {s: i for i, s in enumerate(bdn)}
     out = np.zeros(nsup * nsdn)
     for coeff, ops in terms:
-        if not abs(coeff) > 1e-14:
+        if not abs(coeff) > F32_TOL14:                  # 1.E-14, a default-real literal
             continue
         v = np.array(psi, dtype=np.float64, copy=True)
         for code, si, spi, sj, spj in ops:

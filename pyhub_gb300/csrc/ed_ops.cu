@@ -234,7 +234,8 @@ extern "C" int ed_ops_apply(const ed_opspace *sp, void *stream, int nterms, cons
     const unsigned blocks = (unsigned)std::min<int64_t>((nst + 255) / 256, (int64_t)nsm * 8);
     double *A = work, *B = work + nst;
     for (int t = 0; t < nterms; ++t) {
-        if (!(fabs(coeff[t]) > 1e-14)) continue;   // IF (ABS(COEFF(I)) .GT. 1.E-14)
+        // IF (ABS(COEFF(I)) .GT. 1.E-14): a default-real literal, compared after promotion
+        if (!(fabs(coeff[t]) > (double)1e-14f)) continue;
         ED_CHECK_CUDA(cudaMemcpyAsync(A, x, sizeof(double) * (size_t)nst, cudaMemcpyDeviceToDevice, st));
         for (int q = term_off[t]; q < term_off[t + 1]; ++q) {
             const int32_t *o = ops + 5 * (int64_t)q;
