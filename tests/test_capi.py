@@ -102,3 +102,32 @@ def test_new_entry_points_reject_bad_arguments(edlib):
     assert "nsites" in L.ed_last_error().decode()
     assert L.ed_batch_ritz_sum(None, None, 0, None, 10, None, None, None) == ARG
     assert L.ed_batch_lanczos_kept(None, None, 0, None, None, None, 10, None, None, None, 0) == ARG
+
+
+def test_composite_and_operator_entry_points_reject_bad_arguments(edlib):
+    """The composite calls (one Lanczos step, the assembled RDMs, the
+    Hellmann-Feynman gradient) and the operator engine refuse a missing
+    sector, space or buffer, and a malformed operator space, with a message,
+    before anything touches a GPU."""
+    L = edlib.lib()
+    ARG = edlib.ED_ERR_ARG
+    assert L.ed_lanczos_step_scratch_bytes(None, 10) == 0
+    assert L.ed_rdm1_scratch_bytes(None) == 0
+    assert L.ed_lanczos_step(None, None, edlib.ED_F32, 0, None, 0, 0, 10, None, None, None, None, None, 0) == ARG
+    assert "sector" in L.ed_last_error().decode()
+    assert L.ed_rdm1(None, None, edlib.ED_F64, 0, None, None, None, None, None, 0) == ARG
+    assert L.ed_hf_grad(None, None, edlib.ED_F64, 0, None, 0, None, None, None, None, None, 0) == ARG
+    assert "Hubbard" in L.ed_last_error().decode()
+    assert L.ed_ops_apply(None, None, 0, None, None, None, None, None, None, 0) == ARG
+    assert "space" in L.ed_last_error().decode()
+    out = ctypes.c_void_p()
+    nu = (ctypes.c_int * 2)(2, 2)
+    nd = (ctypes.c_int * 1)(1)
+    assert L.ed_opspace_create(40, 1, nu, 1, nd, ctypes.byref(out)) == ARG        # more sites than 32
+    assert "norb" in L.ed_last_error().decode()
+    assert L.ed_opspace_create(4, 2, nu, 1, nd, ctypes.byref(out)) == ARG         # 2 listed twice
+    assert "twice" in L.ed_last_error().decode()
+    bad = (ctypes.c_int * 1)(5)
+    assert L.ed_opspace_create(4, 1, bad, 1, nd, ctypes.byref(out)) == ARG        # 5 particles on 4 sites
+    assert "outside" in L.ed_last_error().decode()
+    assert not out.value
