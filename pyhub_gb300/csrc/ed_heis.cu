@@ -21,6 +21,8 @@
 // with the fused <x,y>, <y,y> partials.
 #include "ed_common.cuh"
 
+#include <cstdlib>
+
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -407,6 +409,156 @@ __global__ void __launch_bounds__(kHeisRowThreads, 4) heis_row_kernel(const T *_
                 if (src >= 0) acc += ab_c[q] * __ldg(x + src + __ldg(a.rankA + (ha ^ (1u << a.ab_pa[q]))));
             }
             if (ok) y[off + c] = (d * xs[cc] + acc) * sc;
+        }
+    }
+}
+
+constexpr int kHeisCol4Threads = 1024;
+
+// bytes of the four rows' A-B bond facts ahead of the staged columns (16-byte aligned)
+__host__ __device__ inline size_t heis_col4_head_bytes(int nab)
+{
+    const size_t b = (size_t)nab * (4 * sizeof(int64_t) + 4 * sizeof(float) + sizeof(float));
+    return (b + 15) / 16 * 16;
+}
+
+// G A-A flip slots of one lane (table entries at, at+32, ...) applied to the
+// four staged rows; the G table loads are issued before the first gather.
+template <int G>
+__device__ __forceinline__ void heis_col4_group(const HsArgs &a, int at, const float4 *xs4, float (&acc)[4])
+{
+    int q[G];
+    float c[G];
+#pragma unroll
+    for (int i = 0; i < G; ++i) {
+        const int2 pk = __ldg(a.aa_pk32 + at + i * 32);
+        q[i] = pk.x;
+        c[i] = __int_as_float(pk.y);
+    }
+#pragma unroll
+    for (int i = 0; i < G; ++i) {
+        const float4 v = xs4[q[i]];
+        acc[0] += c[i] * v.x;
+        acc[1] += c[i] * v.y;
+        acc[2] += c[i] * v.z;
+        acc[3] += c[i] * v.w;
+    }
+}
+
+// Pass R for FP32 with four rows of one hole count per CTA (packed A-B path):
+// the four rows' entries of column c are staged as one 16-byte column xs4[c],
+// so one A-A flip slot (an 8-byte table load) and one 128-bit gather serve all
+// four rows.  Each row's sums are the one-row kernel's, in its order (slots,
+// then the antiparallel A-B bonds in increasing order), so the product is the same.
+// Work items are groups of four rows of rows_of_m, hole count by hole count.
+__global__ void __launch_bounds__(kHeisCol4Threads, 1) heis_row_col4_kernel(const float *__restrict__ x,
+                                                                          float *__restrict__ y, const HsArgs a,
+                                                                          int64_t nitems)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    int64_t *ab_src = reinterpret_cast<int64_t *>(smem_raw);      // [4][nab] source row offset, -1 if impossible
+    float *ab_c = reinterpret_cast<float *>(ab_src + 4 * a.nab);   // [4][nab] flip element
+    float *ab_w2 = ab_c + 4 * a.nab;                               // [nab] zz/2: drop of an antiparallel bond
+    float4 *xs4 = reinterpret_cast<float4 *>(smem_raw + heis_col4_head_bytes(a.nab));
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = kHeisCol4Threads / 32;
+    const float sc = (float)a.scale;
+    const float *dA32 = static_cast<const float *>(a.diagA), *dB32 = static_cast<const float *>(a.diagB);
+    for (int64_t it = blockIdx.x; it < nitems; it += gridDim.x) {
+        int m = 0;
+        int64_t g = it;
+        for (;;) {
+            const int64_t ng = (a.row_base[m + 1] - a.row_base[m] + 3) / 4;
+            if (g < ng) break;
+            g -= ng;
+            ++m;
+        }
+        const int nr = (int)min((int64_t)4, a.row_base[m + 1] - a.row_base[m] - 4 * g);
+        int64_t off[4];
+        float db[4];
+        uint32_t rbits[4], hb[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int32_t row = __ldg(a.rows_of_m + a.row_base[m] + 4 * g + (r < nr ? r : 0));
+            off[r] = __ldg(a.row_off + row);
+            db[r] = __ldg(dB32 + row);
+            rbits[r] = __ldg(a.row_bbits + row);
+            hb[r] = __ldg(a.row_pat + row);
+        }
+        const int len = (int)a.ncol[m];
+        const int64_t cbase = a.col_base[m];
+        const int64_t sbase = a.slice_base[m];
+        __syncthreads();   // the previous group's readers are done with xs4 / ab_*
+        for (int c = threadIdx.x; c < len; c += blockDim.x) {
+            float *dst = reinterpret_cast<float *>(xs4 + c);
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                if (r < nr) cp_async_elem(dst + r, x + off[r] + c);
+                else dst[r] = 0.f;
+            }
+        }
+        for (int k = threadIdx.x; k < 4 * a.nab; k += blockDim.x) {
+            const int r = k / a.nab, q = k - r * a.nab;
+            int64_t src = -1;
+            float cf = 0.f;
+            if (r < nr) {
+                const uint32_t h = (r == 0) ? hb[0] : (r == 1) ? hb[1] : (r == 2) ? hb[2] : hb[3];
+                const uint32_t hk = (h >> a.ab_pb[q]) & 1u;
+                const int32_t r2 = __ldg(a.rowidx + (h ^ (1u << a.ab_pb[q])));
+                src = (r2 >= 0) ? __ldg(a.row_off + r2) : (int64_t)-1;
+                cf = (float)(hk ? a.ab_fkj[q] : a.ab_fjk[q]);
+            }
+            ab_src[k] = src;
+            ab_c[k] = cf;
+            if (r == 0) ab_w2[q] = (float)(2.0 * a.ab_zz[q]);
+        }
+        cp_async_wait_all();
+        __syncthreads();
+        const int nsl = (len + 31) / 32;
+        for (int sl = warp; sl < nsl; sl += nwarps) {
+            const int c = sl * 32 + lane;
+            const bool ok = c < len;
+            const int cc = ok ? c : len - 1;
+            const float dA = __ldg(dA32 + cbase + cc);
+            float d[4], acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int r = 0; r < 4; ++r) d[r] = dA + db[r];
+            const int s0 = __ldg(a.aa_off + sbase + sl), ns = __ldg(a.aa_off + sbase + sl + 1) - s0;
+            // slots in groups: all table loads of a group are in flight before its first gather
+            const int at0 = s0 * 32 + lane;
+            int q = 0;
+            for (; q + 8 <= ns; q += 8) heis_col4_group<8>(a, at0 + q * 32, xs4, acc);
+            if (q + 4 <= ns) {
+                heis_col4_group<4>(a, at0 + q * 32, xs4, acc);
+                q += 4;
+            }
+            for (; q < ns; ++q) heis_col4_group<1>(a, at0 + q * 32, xs4, acc);
+            // antiparallel A-B bonds of each row: the set bits of (column's A bits ^ row's B bits)
+            const uint32_t ca = __ldg(a.col_abbits + cbase + cc);
+            uint32_t diff[4], any = 0u;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                diff[r] = (r < nr) ? (ca ^ rbits[r]) : 0u;
+                any |= diff[r];
+            }
+            while (any) {
+                const int q = __ffs(any) - 1;
+                any &= any - 1;
+                const int rk = __ldg(a.ab_rank + q * a.ncols + cbase + cc);
+#pragma unroll
+                for (int r = 0; r < 4; ++r) {
+                    if (!((diff[r] >> q) & 1u)) continue;
+                    d[r] -= ab_w2[q];
+                    const int64_t src = ab_src[r * a.nab + q];
+                    if (src >= 0) acc[r] += ab_c[r * a.nab + q] * __ldg(x + src + rk);
+                }
+            }
+            if (ok) {
+                const float4 xv = xs4[cc];
+                const float xr[4] = {xv.x, xv.y, xv.z, xv.w};
+#pragma unroll
+                for (int r = 0; r < 4; ++r)
+                    if (r < nr) y[off[r] + c] = (d[r] * xr[r] + acc[r]) * sc;
+            }
         }
     }
 }
@@ -825,11 +977,35 @@ static int heis_struct_run(ed_sector *s, cudaStream_t st, const T *x, T *y, doub
     a.scale = scale;
     const int nsm = num_sms();
     // ---- pass R
-    const size_t smem = heis_row_head_bytes(h.nab, sizeof(T)) + (size_t)std::max<int64_t>(h.max_len, 1) * sizeof(T);
-    ED_CHECK_CUDA(cudaFuncSetAttribute(heis_row_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int64_t blocks = std::min<int64_t>(h.nrows, (int64_t)nsm * 4);
-    if (blocks < 1) blocks = 1;
-    heis_row_kernel<T><<<(unsigned)blocks, kHeisRowThreads, smem, st>>>(x, y, a);
+    int maxsm = 0;
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    }
+    const size_t smem4 = heis_col4_head_bytes(h.nab) + (size_t)std::max<int64_t>(h.max_len, 1) * 16;
+    // FP32 with the packed A-B path: four rows of one hole count per CTA when their columns
+    // fit (PYHUB_ED_HEIS_ROWS=1 selects the one-row pass; both give the same product)
+    const char *one = std::getenv("PYHUB_ED_HEIS_ROWS");
+    if (sizeof(T) == 4 && h.ab_fast && smem4 <= (size_t)maxsm && !(one && one[0] == '1')) {
+        int64_t nitems = 0;
+        for (int m = 0; m <= h.nA; ++m) nitems += (h.row_base[m + 1] - h.row_base[m] + 3) / 4;
+        ED_CHECK_CUDA(cudaFuncSetAttribute(heis_row_col4_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem4));
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, heis_row_col4_kernel, kHeisCol4Threads, smem4);
+        if (per_sm < 1) per_sm = 1;
+        int64_t blocks = std::min<int64_t>(nitems, (int64_t)nsm * per_sm);
+        if (blocks < 1) blocks = 1;
+        heis_row_col4_kernel<<<(unsigned)blocks, kHeisCol4Threads, smem4, st>>>(
+            reinterpret_cast<const float *>(x), reinterpret_cast<float *>(y), a, nitems);
+    } else {
+        const size_t smem = heis_row_head_bytes(h.nab, sizeof(T)) + (size_t)std::max<int64_t>(h.max_len, 1) * sizeof(T);
+        ED_CHECK_CUDA(cudaFuncSetAttribute(heis_row_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int64_t blocks = std::min<int64_t>(h.nrows, (int64_t)nsm * 4);
+        if (blocks < 1) blocks = 1;
+        heis_row_kernel<T><<<(unsigned)blocks, kHeisRowThreads, smem, st>>>(x, y, a);
+    }
     ED_CHECK_LAUNCH();
     // ---- pass S
     SlabPlan p;

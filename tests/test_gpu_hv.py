@@ -233,6 +233,40 @@ def test_heisenberg_integer_exact(edlib, norb):
         assert np.array_equal(y, yref)
 
 
+@pytest.mark.parametrize("case", ["4x4", "4x6", "ring13", "ring14_extra"])
+def test_heisenberg_four_row_pass_equals_one_row_pass(edlib, monkeypatch, case):
+    """FP32: the row pass with four rows of one hole count per CTA and the
+    one-row pass (PYHUB_ED_HEIS_ROWS=1) give the same product bit for bit.
+    Every case has at most 32 bonds between the halves (the packed path both
+    passes need), so the four-row pass runs."""
+    import torch
+    rng = np.random.default_rng(7)
+    if case == "4x4":
+        norb, J = 16, O.square_pbc(4, 4, 1.0)
+    elif case == "4x6":
+        norb, J = 24, O.square_pbc(4, 6, 1.0)
+    elif case == "ring13":
+        norb = 13
+        J = O.ring(13, 1.0) + np.diag(rng.standard_normal(13))
+    else:
+        norb = 14
+        J = O.ring(14, 0.7)
+        for _ in range(12):
+            i, j = rng.choice(14, size=2, replace=False)
+            J[i, j] = J[j, i] = rng.uniform(0.2, 1.5)
+    sec = edlib.Sector(norb, norb // 2, 0, edlib.ED_HEISENBERG, J=J)
+    xi = sec.from_ref(torch.tensor(rng.standard_normal(sec.dim), dtype=torch.float32, device="cuda"))
+    out = []
+    for mode in ("0", "1"):
+        monkeypatch.setenv("PYHUB_ED_HEIS_ROWS", mode)
+        y = torch.zeros_like(xi)
+        sec.hv(xi, y, scale=0.75)
+        torch.cuda.synchronize()
+        out.append(y.cpu().numpy())
+    monkeypatch.delenv("PYHUB_ED_HEIS_ROWS")
+    assert np.array_equal(out[0], out[1])
+
+
 @pytest.mark.parametrize("dt", ["f32", "f64"])
 def test_multidot_and_update(edlib, dt):
     import torch
